@@ -1,0 +1,156 @@
+/*
+ * pbrinkman.h -- C ABI of the GB300 periodic regularized Brinkman evaluator.
+ *
+ * Plain pointers and sizes only.  Layouts follow the reference project
+ * hoangngan82/periodicBrinkman: a "3 x N column-major matrix" is an array of N
+ * xyz triples (cuda/periodicBrinkman.h:16-17); the mobility matrix A is
+ * 3m x 3n column-major with the (r, c) entry of the block of target i and
+ * source j at A[(3j + c) * 3m + 3i + r] (cuda/periodicBrinkman.h:304).
+ *
+ * Every function returns PB_OK (0) or a negative PB_ERR_* code;
+ * pb_last_error() gives a one-line message for the calling thread.
+ * Nothing falls back to the CPU: without a CUDA device every compute entry
+ * point returns PB_ERR_CUDA.
+ */
+#ifndef PBRINKMAN_H
+#define PBRINKMAN_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PB_OK 0
+#define PB_ERR_INVALID -1     /* bad argument (sizes, NaN, L <= 0, alpha <= 0, ...) */
+#define PB_ERR_CUDA -2        /* CUDA runtime error or no device */
+#define PB_ERR_NOMEM -3       /* device allocation failed */
+#define PB_ERR_UNSUPPORTED -4 /* valid but outside what this build supports */
+#define PB_ERR_BUDGET -5      /* request exceeds the memory budget of a server */
+#define PB_ERR_BUSY -6        /* server queue full */
+
+/* precision */
+#define PB_PREC_FP64 0  /* all FP64 ("plain"): reference closed forms, FP64 grids */
+#define PB_PREC_MIXED 1 /* FP32 bulk: polynomial pair kernel, FP32 grids; FP64 series/self/sum */
+
+/* flags */
+#define PB_REAL_SPACE 1 /* real-space sum (incl. self term) */
+#define PB_KSPACE 2     /* k-space sum (k != 0) */
+#define PB_ZERO_MODE 4  /* add the k = 0 mean-flow mode  sum_j f_j / (alpha^2 tau) */
+#define PB_FLAGS_DEFAULT (PB_REAL_SPACE | PB_KSPACE)
+
+/* memory location of user buffers */
+#define PB_HOST 0
+#define PB_DEVICE 1
+
+/* One solve: velocities at n_tgt targets induced by n_src point forces in the
+ * periodic box L with Brinkman alpha (inverse permeability length) and blob
+ * width eps (eps = 0: singular point forces).  Zero-valued tuning fields are
+ * chosen by the autotuner from (n, L, tol). */
+typedef struct pb_solve_params {
+    int n_src;     /* number of point forces */
+    int n_tgt;     /* number of targets; 0 = the targets are the sources */
+    double L[3];   /* box */
+    double alpha;  /* Brinkman alpha > 0 */
+    double eps;    /* blob width >= 0 */
+    double tol;    /* target max relative velocity error (autotuner); 0 -> 1e-6 */
+    double d;      /* Ewald splitting blob width d = 1/xi; 0 = autotune */
+    double rc;     /* real-space cutoff; 0 = autotune */
+    int M[3];      /* FFT grid (powers of two >= 8); 0 = autotune */
+    int P;         /* Gaussian support points per axis (even, 4..32); 0 = autotune */
+    double m_std;  /* support half-width in Gaussian standard deviations; 0 = from tol */
+    int precision; /* PB_PREC_FP64 or PB_PREC_MIXED */
+    int flags;     /* PB_REAL_SPACE | PB_KSPACE | PB_ZERO_MODE; 0 = default */
+} pb_solve_params;
+
+/* Resolved parameters of one instance of a plan. */
+typedef struct pb_instance_info {
+    double d, rc, eta, m_std;
+    int M[3];
+    int P;
+    int ncell[3];
+    int npoly;            /* polynomial terms of the FP32 pair kernel */
+    long long pairs_est;  /* estimated real-space pairs inside rc */
+} pb_instance_info;
+
+typedef struct pb_plan_s* pb_plan;
+
+/* ---- reference-facing entry points ------------------------------------ */
+
+/* Replaces periodicBrinkman(dA, dx, dx0, a, d, e, M, N, L, maxBlockSize)
+ * (cuda/periodicBrinkman.h:432-513).  DEVICE pointers: dA (3m x 3n,
+ * column-major) is ACCUMULATED into (A += real + k-space sums); dx is 3 x m
+ * targets, dx0 is 3 x n sources; L has 3 entries (host).  Real images over
+ * [-M,M]^3 and wave vectors over [-N,N]^3 \ {0}, both rescaled per axis from
+ * the sorted box as the reference does (cuda/periodicBrinkman.h:457-487).
+ * M < 0 skips the real part, N <= 0 skips the k part.  The k-space sum is
+ * divided by tau = Lx Ly Lz like the reference's host twin fourierShells
+ * (cuda/periodicBrinkman.h:745); the reference's GPU kernelFourier omits it,
+ * the two agree for L = (1,1,1).  maxBlockSize must be > 0 (it tuned the
+ * reference's block size; it has no effect here).  Runs on the current
+ * stream 0 and synchronises before returning. */
+int pb_periodic_brinkman(double* dA, const double* dx, int m, const double* dx0, int n, double a, double d,
+                         double e, int M, int N, const double* L, int maxBlockSize);
+
+/* As pb_periodic_brinkman with explicit per-axis shell counts Mx[3], Nx[3]
+ * and tau_scaled = 0 to reproduce kernelFourier's missing 1/tau. */
+int pb_periodic_brinkman_ex(double* dA, const double* dx, int m, const double* dx0, int n, double a, double d,
+                            double e, const int* Mx, const int* Nx, const double* L, int tau_scaled, void* stream);
+
+/* Replaces fftBrinkman(U, y, f, xn, L, M, P, m, C, e, tol, d, alpha)
+ * (cuda/fftBrinkman.h:34-50).  HOST pointers: U (3 x m_tgt, overwritten),
+ * y (3 x m_tgt targets), f (3 x n forces), xn (3 x n force locations),
+ * L[3], grid M[3], support P[3] (P[0] used for all axes, as the reference's
+ * eta uses P[0]), msd = support half-width in standard deviations, C unused
+ * (as in the reference), e = blob width, tol only reported, d = splitting
+ * blob width, alpha.  Computes, like the reference, the k-space part only
+ * (k != 0), but with a centred support window, no conjugation of the scaled
+ * spectrum (cuda/fftBrinkman.h:209-216) and a gather over each target's own
+ * support instead of the whole grid (cuda/fftBrinkman.h:253-272). */
+int pb_fft_brinkman(double* U, const double* y, int m_tgt, const double* f, const double* xn, int n,
+                    const double* L, const int* M, const int* P, int msd, int C, double e, double tol, double d,
+                    double alpha);
+
+/* ---- evaluator ----------------------------------------------------------- */
+
+/* One-shot solve.  x, f: 3 x n_src; y: 3 x n_tgt (NULL when n_tgt == 0);
+ * U: 3 x n_tgt (or 3 x n_src), overwritten.  where = PB_HOST or PB_DEVICE for
+ * all four buffers.  stream: cudaStream_t or NULL (default stream). */
+int pb_solve(const pb_solve_params* p, const double* x, const double* f, const double* y, double* U, int where,
+             void* stream);
+
+/* A plan holds device buffers, kernel tables and FFT twiddles for `count`
+ * instances solved together (a batch; count = 1 for a single solve).  Its
+ * execution is captured into a CUDA graph on the second call and replayed. */
+int pb_plan_create(const pb_solve_params* p, int count, pb_plan* out);
+/* Packed inputs: instances back to back in the order of creation. */
+int pb_plan_execute(pb_plan plan, const double* x, const double* f, const double* y, double* U, int where,
+                    void* stream);
+int pb_plan_instance_info(pb_plan plan, int i, pb_instance_info* info);
+/* Device bytes held by the plan. */
+long long pb_plan_device_bytes(pb_plan plan);
+/* CUDA kernels one execution launches (kernel nodes of the captured graph;
+ * 0 before the graph exists, i.e. before the second pb_plan_execute). */
+int pb_plan_kernel_count(pb_plan plan);
+/* Bytes a plan for these parameters would hold (for admission control). */
+long long pb_plan_estimate_bytes(const pb_solve_params* p, int count);
+/* Per-stage device time of the last pb_plan_execute (ms), if timing was
+ * enabled with pb_plan_set_timing: [0] sort, [1] real space, [2] spread,
+ * [3] FFT + Green, [4] gather, [5] combine. */
+int pb_plan_set_timing(pb_plan plan, int enable);
+int pb_plan_stage_ms(pb_plan plan, double* ms6);
+int pb_plan_destroy(pb_plan plan);
+
+/* ---- misc ----------------------------------------------------------------- */
+const char* pb_last_error(void);
+const char* pb_version(void);
+/* Build the FP32 real-space tables of one instance on the host and evaluate
+ * the pair kernel H1, H2 at n radii exactly as the GPU polynomial path does
+ * (FP32 Horner), for testing the tables without a GPU. */
+int pb_debug_pair_kernel(double alpha, double d, double eps, double rc, int n, const double* r, double* H1,
+                         double* H2);
+/* Number of CUDA devices visible (0 without a GPU). */
+int pb_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,48 @@
+"""GB300-native periodic regularized Brinkman evaluator (spectral Ewald).
+
+The compute path is the CUDA library ``_lib/libpbrinkman.so`` (C ABI declared
+in ``include/pbrinkman.h``), built by ``periodicbrinkman_gb300.build``.  This
+module is the host-side mirror of the reference's entry points:
+
+* ``periodicBrinkman(dA, dx, dx0, a, d, e, M, N, L, maxBlockSize=256)`` --
+  the dense mobility matrix of cuda/periodicBrinkman.h:432-513 (device
+  arrays, accumulates into dA);
+* ``fftBrinkman(U, y, f, xn, L, M, P, m, C, e, tol, d, alpha=1)`` -- the
+  k-space velocities of cuda/fftBrinkman.h:34-287 (host arrays, U overwritten);
+
+plus the full evaluator (real + k space + self), batched plans and the
+continuous-batching server.  There is no CPU fallback: without the built
+library or a CUDA device every compute call raises.
+"""
+from __future__ import annotations
+
+from ._lib import (  # noqa: F401
+    PB_DEVICE,
+    PB_FLAGS_DEFAULT,
+    PB_HOST,
+    PB_KSPACE,
+    PB_PREC_FP64,
+    PB_PREC_MIXED,
+    PB_REAL_SPACE,
+    PB_ZERO_MODE,
+    PbError,
+    SolveParams,
+    device_count,
+    lib,
+    lib_path,
+)
+from .api import Plan, fftBrinkman, pair_kernel_tables, periodicBrinkman, solve, shell_counts  # noqa: F401
+
+__all__ = [
+    "PbError",
+    "Plan",
+    "SolveParams",
+    "fftBrinkman",
+    "periodicBrinkman",
+    "solve",
+    "shell_counts",
+    "pair_kernel_tables",
+    "device_count",
+    "lib",
+    "lib_path",
+]

@@ -1,0 +1,135 @@
+"""ctypes binding of the C ABI in include/pbrinkman.h."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_ROOT = os.path.dirname(_HERE)
+_LIB_PATH = os.path.join(_HERE, "_lib", "libpbrinkman.so")
+_HEADER = os.path.join(_ROOT, "include", "pbrinkman.h")
+
+PB_OK = 0
+PB_ERR_INVALID = -1
+PB_ERR_CUDA = -2
+PB_ERR_NOMEM = -3
+PB_ERR_UNSUPPORTED = -4
+PB_ERR_BUDGET = -5
+PB_ERR_BUSY = -6
+PB_PREC_FP64 = 0
+PB_PREC_MIXED = 1
+PB_REAL_SPACE = 1
+PB_KSPACE = 2
+PB_ZERO_MODE = 4
+PB_FLAGS_DEFAULT = PB_REAL_SPACE | PB_KSPACE
+PB_HOST = 0
+PB_DEVICE = 1
+
+_ERRNAMES = {
+    PB_ERR_INVALID: "PB_ERR_INVALID",
+    PB_ERR_CUDA: "PB_ERR_CUDA",
+    PB_ERR_NOMEM: "PB_ERR_NOMEM",
+    PB_ERR_UNSUPPORTED: "PB_ERR_UNSUPPORTED",
+    PB_ERR_BUDGET: "PB_ERR_BUDGET",
+    PB_ERR_BUSY: "PB_ERR_BUSY",
+}
+
+
+class PbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_ERRNAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SolveParams(C.Structure):
+    _fields_ = [
+        ("n_src", C.c_int),
+        ("n_tgt", C.c_int),
+        ("L", C.c_double * 3),
+        ("alpha", C.c_double),
+        ("eps", C.c_double),
+        ("tol", C.c_double),
+        ("d", C.c_double),
+        ("rc", C.c_double),
+        ("M", C.c_int * 3),
+        ("P", C.c_int),
+        ("m_std", C.c_double),
+        ("precision", C.c_int),
+        ("flags", C.c_int),
+    ]
+
+
+class InstanceInfo(C.Structure):
+    _fields_ = [
+        ("d", C.c_double),
+        ("rc", C.c_double),
+        ("eta", C.c_double),
+        ("m_std", C.c_double),
+        ("M", C.c_int * 3),
+        ("P", C.c_int),
+        ("ncell", C.c_int * 3),
+        ("npoly", C.c_int),
+        ("pairs_est", C.c_longlong),
+    ]
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _LIB_PATH
+
+
+def header_functions() -> list[str]:
+    """Names of the functions declared in include/pbrinkman.h."""
+    txt = open(_HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(pb_[a-z0-9_]+)\s*\(", txt)))
+
+
+def lib():
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise RuntimeError(
+            f"CUDA library not built: {_LIB_PATH} is missing (run periodicbrinkman_gb300/build.py or "
+            "__graft_entry__.build())"
+        )
+    L = C.CDLL(_LIB_PATH)
+    dp, ip, vp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_void_p
+    L.pb_last_error.restype = C.c_char_p
+    L.pb_version.restype = C.c_char_p
+    L.pb_device_count.restype = C.c_int
+    L.pb_periodic_brinkman.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                                       C.c_int, dp, C.c_int]
+    L.pb_periodic_brinkman_ex.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_double, C.c_double, C.c_double, ip, ip,
+                                          dp, C.c_int, vp]
+    L.pb_fft_brinkman.argtypes = [dp, dp, C.c_int, dp, dp, C.c_int, dp, ip, ip, C.c_int, C.c_int, C.c_double,
+                                  C.c_double, C.c_double, C.c_double]
+    L.pb_solve.argtypes = [C.POINTER(SolveParams), vp, vp, vp, vp, C.c_int, vp]
+    L.pb_plan_create.argtypes = [C.POINTER(SolveParams), C.c_int, C.POINTER(vp)]
+    L.pb_plan_execute.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp]
+    L.pb_plan_instance_info.argtypes = [vp, C.c_int, C.POINTER(InstanceInfo)]
+    L.pb_plan_device_bytes.restype = C.c_longlong
+    L.pb_plan_device_bytes.argtypes = [vp]
+    L.pb_plan_kernel_count.argtypes = [vp]
+    L.pb_plan_estimate_bytes.restype = C.c_longlong
+    L.pb_plan_estimate_bytes.argtypes = [C.POINTER(SolveParams), C.c_int]
+    L.pb_plan_set_timing.argtypes = [vp, C.c_int]
+    L.pb_plan_stage_ms.argtypes = [vp, dp]
+    L.pb_plan_destroy.argtypes = [vp]
+    L.pb_debug_pair_kernel.argtypes = [C.c_double] * 4 + [C.c_int, dp, dp, dp]
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != PB_OK:
+        raise PbError(rc, lib().pb_last_error().decode())
+
+
+def device_count() -> int:
+    return int(lib().pb_device_count())

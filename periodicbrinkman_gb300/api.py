@@ -1,0 +1,231 @@
+"""Host-side mirror of the reference's entry points over the C ABI.
+
+Host buffers are numpy float64 arrays, device buffers are torch CUDA float64
+tensors; a "3 x N column-major matrix" of the reference is an (N, 3) array.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from ._lib import (
+    PB_DEVICE,
+    PB_HOST,
+    PB_PREC_FP64,
+    PB_PREC_MIXED,
+    InstanceInfo,
+    SolveParams,
+    check,
+    lib,
+)
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+def _where(arrs) -> int:
+    dev = [_is_torch(a) and a.is_cuda for a in arrs if a is not None]
+    if all(dev):
+        return PB_DEVICE
+    if not any(dev):
+        return PB_HOST
+    raise ValueError("mix of host and device buffers")
+
+
+def _ptr(a) -> int | None:
+    if a is None:
+        return None
+    if _is_torch(a):
+        if a.dtype.__str__() != "torch.float64" or not a.is_contiguous():
+            raise ValueError("device buffers must be contiguous float64 tensors")
+        return a.data_ptr()
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise ValueError("host buffers must be C-contiguous float64 arrays")
+    return a.ctypes.data
+
+
+def make_params(n_src: int, L, alpha: float, eps: float, n_tgt: int = 0, tol: float = 0.0, d: float = 0.0,
+                rc: float = 0.0, M=(0, 0, 0), P: int = 0, m_std: float = 0.0, precision: str | int = "mixed",
+                flags: int = 0) -> SolveParams:
+    p = SolveParams()
+    p.n_src = int(n_src)
+    p.n_tgt = int(n_tgt)
+    Lv = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
+    Mv = np.broadcast_to(np.asarray(M, dtype=np.int64), (3,))
+    for a in range(3):
+        p.L[a] = float(Lv[a])
+        p.M[a] = int(Mv[a])
+    p.alpha = float(alpha)
+    p.eps = float(eps)
+    p.tol = float(tol)
+    p.d = float(d)
+    p.rc = float(rc)
+    p.P = int(P)
+    p.m_std = float(m_std)
+    if isinstance(precision, str):
+        precision = {"mixed": PB_PREC_MIXED, "fp64": PB_PREC_FP64}[precision]
+    p.precision = int(precision)
+    p.flags = int(flags)
+    return p
+
+
+class Plan:
+    """Device buffers, tables and a CUDA graph for a batch of instances."""
+
+    def __init__(self, params: SolveParams | Sequence[SolveParams]):
+        if isinstance(params, SolveParams):
+            params = [params]
+        self.params = list(params)
+        arr = (SolveParams * len(self.params))(*self.params)
+        h = C.c_void_p()
+        check(lib().pb_plan_create(arr, len(self.params), C.byref(h)))
+        self._h = h
+        self.n_src = sum(p.n_src for p in self.params)
+        self.n_tgt = sum(p.n_tgt if p.n_tgt > 0 else p.n_src for p in self.params)
+        self.n_y = sum(p.n_tgt for p in self.params)
+
+    def execute(self, x, f, y=None, U=None, stream=None):
+        """Packed inputs of all instances; returns U (n_tgt_total, 3)."""
+        if U is None:
+            if _is_torch(x):
+                import torch
+
+                U = torch.empty((self.n_tgt, 3), dtype=torch.float64, device=x.device)
+            else:
+                U = np.empty((self.n_tgt, 3))
+        where = _where([x, f, y, U])
+        s = None
+        if stream is not None:
+            s = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        check(lib().pb_plan_execute(self._h, _ptr(x), _ptr(f), _ptr(y), _ptr(U), where, s))
+        return U
+
+    def info(self, i: int = 0) -> dict:
+        inf = InstanceInfo()
+        check(lib().pb_plan_instance_info(self._h, i, C.byref(inf)))
+        return {"d": inf.d, "rc": inf.rc, "eta": inf.eta, "m_std": inf.m_std, "M": list(inf.M), "P": inf.P,
+                "ncell": list(inf.ncell), "npoly": inf.npoly, "pairs_est": int(inf.pairs_est)}
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().pb_plan_device_bytes(self._h))
+
+    @property
+    def kernel_count(self) -> int:
+        return int(lib().pb_plan_kernel_count(self._h))
+
+    def set_timing(self, on: bool = True) -> None:
+        check(lib().pb_plan_set_timing(self._h, 1 if on else 0))
+
+    def stage_ms(self) -> list[float]:
+        out = np.zeros(6)
+        check(lib().pb_plan_stage_ms(self._h, out.ctypes.data_as(_dp)))
+        return out.tolist()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().pb_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def estimate_bytes(params: SolveParams | Iterable[SolveParams]) -> int:
+    if isinstance(params, SolveParams):
+        params = [params]
+    params = list(params)
+    arr = (SolveParams * len(params))(*params)
+    v = int(lib().pb_plan_estimate_bytes(arr, len(params)))
+    if v < 0:
+        check(v)
+    return v
+
+
+def solve(x, f, L, alpha, eps, y=None, **kw):
+    """Velocities (m, 3) at targets y (default: the sources x) of forces f at x."""
+    n = int(x.shape[0])
+    m = int(y.shape[0]) if y is not None else 0
+    p = make_params(n, L, alpha, eps, n_tgt=m, **kw)
+    with Plan(p) as plan:
+        U = plan.execute(x, f, y)
+    return U
+
+
+def periodicBrinkman(dA, dx, dx0, a, d, e, M, N, L, maxBlockSize: int = 256):
+    """Mirror of periodicBrinkman (cuda/periodicBrinkman.h:432-441).
+
+    dA: torch CUDA float64 (3m, 3n) in column-major storage (dA.t() contiguous),
+    accumulated into.  dx: (m, 3), dx0: (n, 3) CUDA float64 (3 x m / 3 x n
+    column-major).  L: 3 host numbers."""
+    if not (_is_torch(dA) and dA.is_cuda):
+        raise ValueError("periodicBrinkman works on device tensors")
+    m, n = int(dx.shape[0]), int(dx0.shape[0])
+    if tuple(dA.shape) != (3 * m, 3 * n) or not dA.t().is_contiguous():
+        raise ValueError("dA must be (3m, 3n) column-major")
+    Lv = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), (3,)))
+    check(lib().pb_periodic_brinkman(dA.data_ptr(), _ptr(dx), m, _ptr(dx0), n, float(a), float(d), float(e), int(M),
+                                     int(N), Lv.ctypes.data_as(_dp), int(maxBlockSize)))
+    return dA
+
+
+def fftBrinkman(U, y, f, xn, L, M, P, m, C_, e, tol, d, alpha=1.0):
+    """Mirror of fftBrinkman (cuda/fftBrinkman.h:34-50): k-space velocities.
+
+    Host numpy arrays: U (mt, 3) overwritten, y (mt, 3), f (n, 3), xn (n, 3);
+    L, M, P: 3 entries; m: support half-width in standard deviations."""
+    Lv = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), (3,)))
+    Mv = np.ascontiguousarray(np.broadcast_to(np.asarray(M, dtype=np.int32), (3,)))
+    Pv = np.ascontiguousarray(np.broadcast_to(np.asarray(P, dtype=np.int32), (3,)))
+    for a_ in (U, y, f, xn):
+        _ptr(a_)
+    check(lib().pb_fft_brinkman(U.ctypes.data_as(_dp), y.ctypes.data_as(_dp), int(y.shape[0]),
+                                f.ctypes.data_as(_dp), xn.ctypes.data_as(_dp), int(xn.shape[0]),
+                                Lv.ctypes.data_as(_dp), Mv.ctypes.data_as(_ip), Pv.ctypes.data_as(_ip), int(m), int(C_),
+                                float(e), float(tol), float(d), float(alpha)))
+    return U
+
+
+def shell_counts(L, M: int, N: int):
+    """Per-axis (real, Fourier) shell counts used by periodicBrinkman
+    (cuda/periodicBrinkman.h:457-487)."""
+    L = [float(v) for v in np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))]
+    idL = [0, 1, 2]
+    if L[idL[0]] > L[idL[1]]:
+        idL[0], idL[1] = idL[1], idL[0]
+    if L[idL[2]] <= L[idL[0]]:
+        idL = [idL[2], idL[0], idL[1]]
+    elif L[idL[2]] < L[idL[1]]:
+        idL[1], idL[2] = idL[2], idL[1]
+    Mx, Nx = [M] * 3, [N] * 3
+    Mx[idL[2]] = int(np.ceil(M * L[idL[0]] / L[idL[2]]))
+    Mx[idL[1]] = int(np.ceil(M * L[idL[0]] / L[idL[1]]))
+    Nx[idL[0]] = int(np.ceil(N * L[idL[2]] / L[idL[0]]))
+    Nx[idL[1]] = int(np.ceil(N * L[idL[2]] / L[idL[1]]))
+    return Mx, Nx
+
+
+def pair_kernel_tables(alpha: float, d: float, eps: float, rc: float, r) -> tuple[np.ndarray, np.ndarray]:
+    """H1(r), H2(r) of the FP32 polynomial tables, evaluated on the host as the
+    GPU does (for testing the tables without a GPU)."""
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    h1 = np.zeros_like(r)
+    h2 = np.zeros_like(r)
+    check(lib().pb_debug_pair_kernel(alpha, d, eps, rc, r.size, r.ctypes.data_as(_dp), h1.ctypes.data_as(_dp),
+                                     h2.ctypes.data_as(_dp)))
+    return h1, h2

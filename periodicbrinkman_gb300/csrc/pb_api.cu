@@ -1,0 +1,944 @@
+// C ABI of the evaluator: parameter resolution (autotuner), plans (device
+// buffers, tables, twiddles, CUDA-graph replay), the one-shot solve and the
+// reference-facing entry points.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pb_kernel_math.h"
+#include "pb_kernels.h"
+#include "pbrinkman.h"
+
+using namespace pb;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define PB_CK(call)                                                                              \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) return fail(PB_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+bool finite(double v) { return std::isfinite(v); }
+
+int pow2ceil(int v)
+{
+    int p = 8;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+bool is_pow2(int v) { return v >= 4 && (v & (v - 1)) == 0; }
+
+struct Resolved {
+    double d, rc, eta, m, tol;
+    int M[3];
+    int P;
+    int nc[3], S[3];
+    double h[3];
+    int n_src, n_tgt;  // n_tgt: effective targets (n_src when targets are the sources)
+    int same;
+    int flags;
+    long long pairs_est;
+};
+
+// Per-unit device costs (seconds) used by the splitting choice.
+struct CostModel {
+    double pair, grid, support;
+};
+
+CostModel cost_model(int prec)
+{
+    if (prec == PB_PREC_MIXED) return {3.0e-12, 2.5e-11, 1.0e-11};
+    return {1.5e-10, 6.0e-11, 3.0e-11};
+}
+
+int validate(const pb_solve_params& p)
+{
+    if (p.n_src < 0 || p.n_tgt < 0) return fail(PB_ERR_INVALID, "negative particle count");
+    for (int a = 0; a < 3; a++)
+        if (!finite(p.L[a]) || !(p.L[a] > 0)) return fail(PB_ERR_INVALID, "box length L[%d] must be > 0", a);
+    if (!finite(p.alpha) || !(p.alpha > 0)) return fail(PB_ERR_INVALID, "alpha must be > 0");
+    if (!finite(p.eps) || p.eps < 0) return fail(PB_ERR_INVALID, "eps must be >= 0");
+    if (!finite(p.tol) || p.tol < 0 || p.tol >= 1) return fail(PB_ERR_INVALID, "tol must be in [0, 1)");
+    if (!finite(p.d) || p.d < 0) return fail(PB_ERR_INVALID, "d must be >= 0");
+    if (!finite(p.rc) || p.rc < 0) return fail(PB_ERR_INVALID, "rc must be >= 0");
+    if (!finite(p.m_std) || p.m_std < 0) return fail(PB_ERR_INVALID, "m_std must be >= 0");
+    for (int a = 0; a < 3; a++)
+        if (p.M[a] != 0 && (!is_pow2(p.M[a]) || p.M[a] < 8 || p.M[a] > 1024))
+            return fail(PB_ERR_UNSUPPORTED, "grid M[%d]=%d: powers of two in [8, 1024] are supported", a, p.M[a]);
+    if (p.P != 0 && (p.P < 4 || p.P > 32 || (p.P & 1)))
+        return fail(PB_ERR_UNSUPPORTED, "support P=%d: even values in [4, 32] are supported", p.P);
+    if (p.precision != PB_PREC_FP64 && p.precision != PB_PREC_MIXED) return fail(PB_ERR_INVALID, "bad precision");
+    if (p.flags & ~(PB_REAL_SPACE | PB_KSPACE | PB_ZERO_MODE)) return fail(PB_ERR_INVALID, "bad flags");
+    return PB_OK;
+}
+
+// Choose the grid for splitting width d (tuning fields the user left at 0).
+void grid_for(const pb_solve_params& p, double d, double m, int P, double kconst, int* M)
+{
+    for (int a = 0; a < 3; a++) {
+        if (p.M[a] > 0) {
+            M[a] = p.M[a];
+            continue;
+        }
+        // k-space truncation exp(-kmax^2 d^2/4) <= tol with kmax = 2 pi (M/2 - 1)/L,
+        // and Gaussian deconvolution eta < d^2/2  <=>  P L/(M m) < d.
+        double nk = 2.0 * std::sqrt(kconst) / d * p.L[a] / (2 * M_PI) + 1.0;
+        double mk = 2.0 * nk + 2.0;
+        double md = 1.15 * P * p.L[a] / (m * d);
+        M[a] = pow2ceil((int)std::ceil(std::max(mk, md)));
+    }
+}
+
+int resolve(const pb_solve_params& p, Resolved& R)
+{
+    int rc_ = validate(p);
+    if (rc_) return rc_;
+    const double tol = p.tol > 0 ? p.tol : 1e-6;
+    R.tol = tol;
+    R.flags = p.flags ? p.flags : PB_FLAGS_DEFAULT;
+    R.n_src = p.n_src;
+    R.same = (p.n_tgt == 0);
+    R.n_tgt = R.same ? p.n_src : p.n_tgt;
+    const double kconst = std::log(10.0 / tol);
+    const double zeta = std::sqrt(std::log(1.0 / tol)) + 0.35;
+    R.m = p.m_std > 0 ? p.m_std : std::sqrt(2.0 * kconst);
+    int P = p.P;
+    if (P == 0) {
+        P = (int)std::ceil(R.m * std::sqrt(2.0 * kconst) / M_PI) + 1;
+        P += (P & 1);
+        P = std::max(4, std::min(32, P));
+    }
+    R.P = P;
+    const double tau = p.L[0] * p.L[1] * p.L[2];
+    const double Lmin = std::min(p.L[0], std::min(p.L[1], p.L[2]));
+    const CostModel C = cost_model(p.precision);
+    auto real_cut = [&](double d) {
+        double rc = p.rc > 0 ? p.rc : zeta * d;
+        if (p.rc == 0 && p.eps > 0) rc = std::max(rc, zeta * p.eps);
+        return rc;
+    };
+    double d = p.d;
+    if (d == 0) {
+        // scan d on a log grid for the lowest modelled cost
+        double best = 1e300, bestd = Lmin / 8;
+        for (int k = 0; k < 160; k++) {
+            double dd = Lmin * std::pow(2.0, -1.0 - k * 0.0625);
+            if (dd < 1e-6) break;
+            int M[3];
+            grid_for(p, dd, R.m, P, kconst, M);
+            bool ok = true;
+            for (int a = 0; a < 3; a++) {
+                if (M[a] > 1024) ok = false;
+                if (p.M[a] > 0) {  // fixed grid: d must satisfy its k-space and deconvolution limits
+                    double kmax = 2 * M_PI * (M[a] / 2 - 1) / p.L[a];
+                    if (kmax * dd / 2 < std::sqrt(kconst)) ok = false;
+                    if (1.1 * P * p.L[a] / (M[a] * R.m) > dd) ok = false;
+                }
+            }
+            if (!ok) continue;
+            double rc = real_cut(dd);
+            double pairs = (double)R.n_tgt * p.n_src * (4 * M_PI / 3) * rc * rc * rc / tau;
+            double grid = (double)M[0] * M[1] * M[2];
+            double cost = C.pair * pairs + C.grid * grid * std::log2(std::max(grid, 2.0)) / 21.0 +
+                          C.support * (double)(p.n_src + R.n_tgt) * P * P * P;
+            if ((R.flags & PB_KSPACE) == 0) cost = C.pair * pairs;
+            if (cost < best) {
+                best = cost;
+                bestd = dd;
+            }
+        }
+        d = bestd;
+    }
+    R.d = d;
+    R.rc = real_cut(d);
+    grid_for(p, d, R.m, P, kconst, R.M);
+    for (int a = 0; a < 3; a++)
+        if (R.M[a] > 1024)
+            return fail(PB_ERR_UNSUPPORTED, "grid %d needed along axis %d exceeds 1024", R.M[a], a);
+    for (int a = 0; a < 3; a++)
+        if (R.P > R.M[a]) return fail(PB_ERR_UNSUPPORTED, "support P=%d exceeds grid M[%d]=%d", R.P, a, R.M[a]);
+    double h0 = p.L[0] / R.M[0];
+    R.eta = (R.P * h0) * (R.P * h0) / (2 * R.m * R.m);
+    // cell list: cells at least rc wide (capped at 128 per axis)
+    long long ncell = 1;
+    for (int a = 0; a < 3; a++) {
+        int nc = (int)std::floor(p.L[a] / R.rc);
+        nc = std::max(1, std::min(128, nc));
+        R.nc[a] = nc;
+        R.h[a] = p.L[a] / nc;
+        R.S[a] = (int)std::ceil(R.rc / R.h[a] - 1e-12);
+        ncell *= nc;
+    }
+    (void)ncell;
+    R.pairs_est = (long long)((double)R.n_tgt * p.n_src * (4 * M_PI / 3) * R.rc * R.rc * R.rc / tau);
+    return PB_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Plans
+// ---------------------------------------------------------------------------
+struct Bucket {
+    int M[3];
+    std::vector<int> inst;
+    int* d_inst = nullptr;
+    void* d_tw = nullptr;
+};
+
+struct pb_plan_s {
+    int count = 0, prec = 0, dev = 0, nsm = 148;
+    bool all_same = true, any_real = false, any_k = false, any_zero = false;
+    std::vector<pb_solve_params> par;
+    std::vector<Resolved> res;
+    std::vector<PbInst> hinst;
+    std::vector<PbTables> htab;
+    std::vector<int> src_off, tgt_off, cell_off, y_off;
+    int n_src = 0, n_tgt = 0, ncell = 0, npoly = 16, n_y = 0;
+    std::vector<Bucket> buckets;
+    size_t grid_elems = 0, spec_elems = 0;
+
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    PbInst* d_inst = nullptr;
+    PbTables* d_tab = nullptr;
+    int *d_src_off = nullptr, *d_tgt_off = nullptr, *d_cell_off = nullptr, *d_y_off = nullptr;
+    double *x = nullptr, *f = nullptr, *y = nullptr, *ypack = nullptr, *U = nullptr;
+    int *cell_of_s = nullptr, *cnt_s = nullptr, *start_s = nullptr, *fill_s = nullptr, *perm_s = nullptr,
+        *perm_tmp_s = nullptr;
+    int *cell_of_t = nullptr, *cnt_t = nullptr, *start_t = nullptr, *fill_t = nullptr, *perm_t = nullptr,
+        *perm_tmp_t = nullptr;
+    int *chunks = nullptr, *chunk_start = nullptr, *scan_tmp = nullptr, *counter = nullptr;
+    int4* items = nullptr;
+    void *spos_a = nullptr, *spos_b = nullptr, *sfrc = nullptr, *tpos_a = nullptr, *tpos_b = nullptr;
+    float *u_s = nullptr, *u_c = nullptr;
+    double *u_near = nullptr, *u_real = nullptr, *fsum = nullptr;
+    void *u_k = nullptr, *grid = nullptr, *spec = nullptr;
+
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int exec_count = 0;
+    int graph_kernels = 0;  // kernel nodes in the captured graph
+    bool timing = false;
+    cudaEvent_t tev[7] = {};
+    double stage_ms[6] = {};
+};
+
+namespace {
+
+size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+struct Layout {
+    size_t off = 0;
+    template <class T>
+    size_t take(size_t n)
+    {
+        size_t o = off;
+        off += align_up(n * sizeof(T) + 16);
+        return o;
+    }
+};
+
+// Plan sizes; fills offsets when `P` has an arena.
+size_t plan_layout(pb_plan_s* P, bool assign)
+{
+    Layout L;
+    const bool mixed = P->prec == PB_PREC_MIXED;
+    const int ns = std::max(P->n_src, 1), nt = std::max(P->n_tgt, 1), nc = std::max(P->ncell, 1);
+    const int q = P->count;
+    size_t o_inst = L.take<PbInst>(q), o_tab = L.take<PbTables>(q);
+    size_t o_so = L.take<int>(q + 1), o_to = L.take<int>(q + 1), o_co = L.take<int>(q + 1), o_yo = L.take<int>(q + 1);
+    size_t o_x = L.take<double>(3 * (size_t)ns), o_f = L.take<double>(3 * (size_t)ns);
+    size_t o_y = P->all_same ? 0 : L.take<double>(3 * (size_t)std::max(P->n_y, 1));
+    size_t o_yp = P->all_same ? 0 : L.take<double>(3 * (size_t)nt);
+    size_t o_U = L.take<double>(3 * (size_t)nt);
+    size_t o_cs = L.take<int>(ns), o_cnts = L.take<int>(nc + 1), o_sts = L.take<int>(nc + 1),
+           o_fs = L.take<int>(nc + 1), o_ps = L.take<int>(ns), o_pts = L.take<int>(ns);
+    size_t o_ct = 0, o_cntt = 0, o_stt = 0, o_ft = 0, o_pt = 0, o_ptt = 0;
+    if (!P->all_same) {
+        o_ct = L.take<int>(nt);
+        o_cntt = L.take<int>(nc + 1);
+        o_stt = L.take<int>(nc + 1);
+        o_ft = L.take<int>(nc + 1);
+        o_pt = L.take<int>(nt);
+        o_ptt = L.take<int>(nt);
+    }
+    size_t o_ch = L.take<int>(nc + 1), o_chs = L.take<int>(nc + 2), o_st = L.take<int>(scan_tmp_ints(nc + 1));
+    size_t o_cnt = L.take<int>(4), o_it = L.take<int4>(nt + 1);
+    size_t o_sa, o_sb = 0, o_sf, o_ta = 0, o_tb = 0;
+    if (mixed) {
+        o_sa = L.take<float4>(ns);
+        o_sb = L.take<float4>(ns);
+        o_sf = L.take<float4>(ns);
+        if (!P->all_same) {
+            o_ta = L.take<float4>(nt);
+            o_tb = L.take<float4>(nt);
+        }
+    } else {
+        o_sa = L.take<Dbl4>(ns);
+        o_sf = L.take<Dbl4>(ns);
+        if (!P->all_same) o_ta = L.take<Dbl4>(nt);
+    }
+    size_t o_us = 0, o_uc = 0, o_un = 0, o_ur = 0, o_uk;
+    if (mixed) {
+        o_us = L.take<float>(3 * (size_t)nt);
+        o_uc = L.take<float>(3 * (size_t)nt);
+        o_un = L.take<double>(3 * (size_t)nt);
+        o_uk = L.take<float>(3 * (size_t)nt);
+    } else {
+        o_ur = L.take<double>(3 * (size_t)nt);
+        o_uk = L.take<double>(3 * (size_t)nt);
+    }
+    size_t o_fsum = L.take<double>(3 * (size_t)q);
+    size_t esz = mixed ? 4 : 8;
+    size_t o_grid = L.off;
+    L.off += align_up(P->grid_elems * esz + 16);
+    size_t o_spec = L.off;
+    L.off += align_up(P->spec_elems * 2 * esz + 16);
+    std::vector<size_t> o_tw(P->buckets.size()), o_bi(P->buckets.size());
+    for (size_t b = 0; b < P->buckets.size(); b++) {
+        o_tw[b] = L.off;
+        L.off += align_up(twiddle_bytes(P->buckets[b].M, !mixed) + 16);
+        o_bi[b] = L.take<int>(P->buckets[b].inst.size());
+    }
+    if (assign) {
+        char* A = P->arena;
+        P->d_inst = (PbInst*)(A + o_inst);
+        P->d_tab = (PbTables*)(A + o_tab);
+        P->d_src_off = (int*)(A + o_so);
+        P->d_tgt_off = (int*)(A + o_to);
+        P->d_cell_off = (int*)(A + o_co);
+        P->d_y_off = (int*)(A + o_yo);
+        P->x = (double*)(A + o_x);
+        P->f = (double*)(A + o_f);
+        P->y = P->all_same ? nullptr : (double*)(A + o_y);
+        P->ypack = P->all_same ? P->x : (double*)(A + o_yp);
+        P->U = (double*)(A + o_U);
+        P->cell_of_s = (int*)(A + o_cs);
+        P->cnt_s = (int*)(A + o_cnts);
+        P->start_s = (int*)(A + o_sts);
+        P->fill_s = (int*)(A + o_fs);
+        P->perm_s = (int*)(A + o_ps);
+        P->perm_tmp_s = (int*)(A + o_pts);
+        if (!P->all_same) {
+            P->cell_of_t = (int*)(A + o_ct);
+            P->cnt_t = (int*)(A + o_cntt);
+            P->start_t = (int*)(A + o_stt);
+            P->fill_t = (int*)(A + o_ft);
+            P->perm_t = (int*)(A + o_pt);
+            P->perm_tmp_t = (int*)(A + o_ptt);
+        } else {
+            P->start_t = P->start_s;
+            P->perm_t = P->perm_s;
+        }
+        P->chunks = (int*)(A + o_ch);
+        P->chunk_start = (int*)(A + o_chs);
+        P->scan_tmp = (int*)(A + o_st);
+        P->counter = (int*)(A + o_cnt);
+        P->items = (int4*)(A + o_it);
+        P->spos_a = A + o_sa;
+        P->spos_b = mixed ? (void*)(A + o_sb) : nullptr;
+        P->sfrc = A + o_sf;
+        if (P->all_same) {
+            P->tpos_a = P->spos_a;
+            P->tpos_b = P->spos_b;
+        } else {
+            P->tpos_a = A + o_ta;
+            P->tpos_b = mixed ? (void*)(A + o_tb) : nullptr;
+        }
+        if (mixed) {
+            P->u_s = (float*)(A + o_us);
+            P->u_c = (float*)(A + o_uc);
+            P->u_near = (double*)(A + o_un);
+        } else {
+            P->u_real = (double*)(A + o_ur);
+        }
+        P->u_k = A + o_uk;
+        P->fsum = (double*)(A + o_fsum);
+        P->grid = A + o_grid;
+        P->spec = A + o_spec;
+        for (size_t b = 0; b < P->buckets.size(); b++) {
+            P->buckets[b].d_tw = A + o_tw[b];
+            P->buckets[b].d_inst = (int*)(A + o_bi[b]);
+        }
+    }
+    return L.off;
+}
+
+int build_plan_host(const pb_solve_params* p, int count, pb_plan_s* P)
+{
+    if (count <= 0) return fail(PB_ERR_INVALID, "count must be >= 1");
+    P->count = count;
+    P->prec = p[0].precision;
+    P->par.assign(p, p + count);
+    P->res.resize(count);
+    P->hinst.resize(count);
+    P->htab.resize(count);
+    P->src_off.assign(count + 1, 0);
+    P->tgt_off.assign(count + 1, 0);
+    P->cell_off.assign(count + 1, 0);
+    P->y_off.assign(count + 1, -1);
+    P->all_same = true;
+    for (int q = 0; q < count; q++) {
+        if (p[q].precision != P->prec) return fail(PB_ERR_INVALID, "all instances of a plan share one precision");
+        int rc = resolve(p[q], P->res[q]);
+        if (rc) return rc;
+        if (!P->res[q].same) P->all_same = false;
+    }
+    long long ns = 0, nt = 0, nc = 0, ny = 0;
+    for (int q = 0; q < count; q++) {
+        const Resolved& R = P->res[q];
+        P->src_off[q] = (int)ns;
+        P->tgt_off[q] = (int)nt;
+        P->cell_off[q] = (int)nc;
+        if (!R.same) {
+            P->y_off[q] = (int)ny;
+            ny += R.n_tgt;
+        }
+        ns += R.n_src;
+        nt += R.n_tgt;
+        nc += (long long)R.nc[0] * R.nc[1] * R.nc[2];
+    }
+    if (ns > (1LL << 30) || nt > (1LL << 30) || nc > (1LL << 30))
+        return fail(PB_ERR_UNSUPPORTED, "batch too large");
+    P->src_off[count] = (int)ns;
+    P->tgt_off[count] = (int)nt;
+    P->cell_off[count] = (int)nc;
+    P->n_src = (int)ns;
+    P->n_tgt = (int)nt;
+    P->ncell = (int)nc;
+    P->n_y = (int)ny;
+    // FFT buckets by grid size; grids/spectra contiguous per bucket
+    P->grid_elems = 0;
+    P->spec_elems = 0;
+    P->any_real = P->any_k = P->any_zero = false;
+    for (int q = 0; q < count; q++) {
+        const Resolved& R = P->res[q];
+        if (R.flags & PB_REAL_SPACE) P->any_real = true;
+        if (R.flags & PB_KSPACE) P->any_k = true;
+        if (R.flags & PB_ZERO_MODE) P->any_zero = true;
+        int b = -1;
+        for (size_t k = 0; k < P->buckets.size(); k++)
+            if (!std::memcmp(P->buckets[k].M, R.M, sizeof(R.M))) b = (int)k;
+        if (b < 0) {
+            Bucket B;
+            std::memcpy(B.M, R.M, sizeof(R.M));
+            P->buckets.push_back(B);
+            b = (int)P->buckets.size() - 1;
+        }
+        P->buckets[b].inst.push_back(q);
+    }
+    for (size_t b = 0; b < P->buckets.size(); b++) {
+        Bucket& B = P->buckets[b];
+        size_t gsz = (size_t)B.M[0] * B.M[1] * B.M[2], ssz = (size_t)B.M[0] * B.M[1] * (B.M[2] / 2 + 1);
+        for (int q : B.inst) {
+            PbInst& I = P->hinst[q];
+            I.grid_off = (long long)P->grid_elems;
+            I.spec_off = (long long)P->spec_elems;
+            I.bucket = (int)b;
+            P->grid_elems += 3 * gsz;
+            P->spec_elems += 3 * ssz;
+        }
+    }
+    if (!P->any_k) P->grid_elems = P->spec_elems = 0;
+    int npoly = 16;
+    for (int q = 0; q < count; q++) {
+        const Resolved& R = P->res[q];
+        PbInst& I = P->hinst[q];
+        for (int a = 0; a < 3; a++) {
+            I.L[a] = p[q].L[a];
+            I.h[a] = R.h[a];
+            I.gh[a] = p[q].L[a] / R.M[a];
+            I.nc[a] = R.nc[a];
+            I.S[a] = R.S[a];
+            I.M[a] = R.M[a];
+            I.zero_mode[a] = 0;
+        }
+        I.alpha = p[q].alpha;
+        I.eps = p[q].eps;
+        I.d = R.d;
+        I.rc = R.rc;
+        I.eta = R.eta;
+        double Mtot = (double)R.M[0] * R.M[1] * R.M[2];
+        I.kfac = I.gh[0] * I.gh[1] * I.gh[2] / (Mtot * std::pow(M_PI * R.eta, 3.0));
+        I.P = R.P;
+        I.n_src = R.n_src;
+        I.n_tgt = R.n_tgt;
+        I.src_off = P->src_off[q];
+        I.tgt_off = P->tgt_off[q];
+        I.cell_off = P->cell_off[q];
+        I.ncell = R.nc[0] * R.nc[1] * R.nc[2];
+        I.flags = R.flags;
+        I.same = R.same;
+        int trc = build_tables(p[q].alpha, R.d, p[q].eps, R.rc, 1e-9, &P->htab[q]);
+        if (trc) return fail(PB_ERR_INVALID, "table construction failed");
+        npoly = std::max(npoly, P->htab[q].nd);
+    }
+    P->npoly = npoly;
+    return PB_OK;
+}
+
+void plan_free(pb_plan_s* P)
+{
+    if (!P) return;
+    if (P->gexec) cudaGraphExecDestroy(P->gexec);
+    if (P->arena) cudaFree(P->arena);
+    if (P->ev_in) cudaEventDestroy(P->ev_in);
+    if (P->ev_out) cudaEventDestroy(P->ev_out);
+    for (auto& e : P->tev)
+        if (e) cudaEventDestroy(e);
+    if (P->stream) cudaStreamDestroy(P->stream);
+    delete P;
+}
+
+int plan_alloc(pb_plan_s* P)
+{
+    PB_CK(cudaGetDevice(&P->dev));
+    PB_CK(cudaDeviceGetAttribute(&P->nsm, cudaDevAttrMultiProcessorCount, P->dev));
+    P->arena_bytes = plan_layout(P, false);
+    cudaError_t e = cudaMalloc(&P->arena, P->arena_bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        P->arena = nullptr;
+        return fail(PB_ERR_NOMEM, "device allocation of %zu bytes failed: %s", P->arena_bytes, cudaGetErrorString(e));
+    }
+    plan_layout(P, true);
+    PB_CK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+    PB_CK(cudaEventCreateWithFlags(&P->ev_in, cudaEventDisableTiming));
+    PB_CK(cudaEventCreateWithFlags(&P->ev_out, cudaEventDisableTiming));
+    for (auto& ev : P->tev) PB_CK(cudaEventCreate(&ev));
+    // static data
+    PB_CK(cudaMemcpy(P->d_inst, P->hinst.data(), sizeof(PbInst) * P->count, cudaMemcpyHostToDevice));
+    PB_CK(cudaMemcpy(P->d_tab, P->htab.data(), sizeof(PbTables) * P->count, cudaMemcpyHostToDevice));
+    PB_CK(cudaMemcpy(P->d_src_off, P->src_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
+    PB_CK(cudaMemcpy(P->d_tgt_off, P->tgt_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
+    PB_CK(cudaMemcpy(P->d_cell_off, P->cell_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
+    PB_CK(cudaMemcpy(P->d_y_off, P->y_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
+    const bool fp64 = P->prec == PB_PREC_FP64;
+    for (auto& B : P->buckets) {
+        std::vector<char> tw(twiddle_bytes(B.M, fp64));
+        fill_twiddles(B.M, fp64, tw.data());
+        PB_CK(cudaMemcpy(B.d_tw, tw.data(), tw.size(), cudaMemcpyHostToDevice));
+        PB_CK(cudaMemcpy(B.d_inst, B.inst.data(), sizeof(int) * B.inst.size(), cudaMemcpyHostToDevice));
+    }
+    return PB_OK;
+}
+
+void bin_and_sort(pb_plan_s* P, const double* pos, int n, const int* d_off, int* cell_of, int* cnt, int* start,
+                  int* fill, int* perm_tmp, int* perm, cudaStream_t s)
+{
+    cudaMemsetAsync(cnt, 0, sizeof(int) * (P->ncell + 1), s);
+    cudaMemsetAsync(fill, 0, sizeof(int) * (P->ncell + 1), s);
+    launch_bin(pos, n, d_off, P->d_inst, P->count, cell_of, cnt, s);
+    launch_exclusive_scan(cnt, start, P->ncell, P->scan_tmp, s);
+    launch_scatter(cell_of, n, start, fill, perm_tmp, s);
+    launch_sort_cells(perm_tmp, perm, start, P->ncell, s);
+}
+
+void record(pb_plan_s* P, int k, cudaStream_t s)
+{
+    if (P->timing) cudaEventRecord(P->tev[k], s);
+}
+
+// The device work of one execution (inputs already in P->x/f/y).
+void run_compute(pb_plan_s* P, cudaStream_t s)
+{
+    const bool mixed = P->prec == PB_PREC_MIXED;
+    record(P, 0, s);
+    bin_and_sort(P, P->x, P->n_src, P->d_src_off, P->cell_of_s, P->cnt_s, P->start_s, P->fill_s, P->perm_tmp_s,
+                 P->perm_s, s);
+    if (mixed)
+        launch_prepare_mixed(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count, (float4*)P->spos_a,
+                             (float4*)P->spos_b, (float4*)P->sfrc, s);
+    else
+        launch_prepare_fp64(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count, (Dbl4*)P->spos_a,
+                            (Dbl4*)P->sfrc, s);
+    if (!P->all_same) {
+        launch_pack_targets(P->x, P->y, P->n_tgt, P->d_tgt_off, P->d_src_off, P->d_y_off, P->count, P->ypack, s);
+        bin_and_sort(P, P->ypack, P->n_tgt, P->d_tgt_off, P->cell_of_t, P->cnt_t, P->start_t, P->fill_t,
+                     P->perm_tmp_t, P->perm_t, s);
+        if (mixed)
+            launch_prepare_mixed(P->ypack, nullptr, P->perm_t, P->n_tgt, P->d_tgt_off, P->d_inst, P->count,
+                                 (float4*)P->tpos_a, (float4*)P->tpos_b, nullptr, s);
+        else
+            launch_prepare_fp64(P->ypack, nullptr, P->perm_t, P->n_tgt, P->d_tgt_off, P->d_inst, P->count,
+                                (Dbl4*)P->tpos_a, nullptr, s);
+    }
+    launch_count_chunks(P->start_t, P->ncell, P->chunks, s);
+    launch_exclusive_scan(P->chunks, P->chunk_start, P->ncell, P->scan_tmp, s);
+    launch_emit_items(P->start_t, P->chunk_start, P->ncell, P->d_cell_off, P->count, P->items, s);
+    record(P, 1, s);
+    if (P->any_real) {
+        const int* nitems = P->chunk_start + P->ncell;
+        if (mixed)
+            launch_real_mixed(P->npoly, P->d_inst, P->d_tab, P->items, nitems, P->n_tgt, (const float4*)P->spos_a,
+                              (const float4*)P->spos_b, (const float4*)P->sfrc, P->start_s, (const float4*)P->tpos_a,
+                              (const float4*)P->tpos_b, P->u_s, P->u_c, P->u_near, P->counter, P->nsm, s);
+        else
+            launch_real_fp64(P->d_inst, P->d_tab, P->items, nitems, P->n_tgt, (const Dbl4*)P->spos_a,
+                             (const Dbl4*)P->sfrc, P->start_s, (const Dbl4*)P->tpos_a, P->u_real, P->counter,
+                             P->nsm, s);
+    }
+    record(P, 2, s);
+    if (P->any_k) {
+        size_t esz = mixed ? 4 : 8;
+        cudaMemsetAsync(P->grid, 0, P->grid_elems * esz, s);
+        if (mixed)
+            launch_spread<float>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
+                                 (float*)P->grid, s);
+        else
+            launch_spread<double>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
+                                  (double*)P->grid, s);
+        record(P, 3, s);
+        for (auto& B : P->buckets) {
+            const PbInst& I0 = P->hinst[B.inst[0]];
+            if (mixed)
+                launch_kspace_fft<float>(P->d_inst, B.d_inst, (int)B.inst.size(), I0.spec_off, B.M,
+                                         (float*)P->grid + I0.grid_off, (float2*)P->spec + I0.spec_off, B.d_tw, s);
+            else
+                launch_kspace_fft<double>(P->d_inst, B.d_inst, (int)B.inst.size(), I0.spec_off, B.M,
+                                          (double*)P->grid + I0.grid_off, (double2*)P->spec + I0.spec_off, B.d_tw,
+                                          s);
+        }
+        record(P, 4, s);
+        if (mixed)
+            launch_gather<float>(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->tpos_a, P->tpos_b,
+                                 (const float*)P->grid, (float*)P->u_k, s);
+        else
+            launch_gather<double>(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->tpos_a, P->tpos_b,
+                                  (const double*)P->grid, (double*)P->u_k, s);
+    } else {
+        record(P, 3, s);
+        record(P, 4, s);
+    }
+    record(P, 5, s);
+    if (P->any_zero) launch_force_sums(P->f, P->d_src_off, P->count, P->fsum, s);
+    if (mixed)
+        launch_combine_mixed(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->perm_t, P->u_s, P->u_c, P->u_near,
+                             (const float*)P->u_k, P->any_real, P->any_k, P->fsum, P->U, s);
+    else
+        launch_combine_fp64(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->perm_t, P->u_real,
+                            (const double*)P->u_k, P->any_real, P->any_k, P->fsum, P->U, s);
+    record(P, 6, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pb_last_error(void) { return g_err.c_str(); }
+
+const char* pb_version(void) { return "periodicbrinkman_gb300 0.1 (sm_103a)"; }
+
+int pb_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+long long pb_plan_estimate_bytes(const pb_solve_params* p, int count)
+{
+    if (!p || count <= 0) return fail(PB_ERR_INVALID, "bad arguments");
+    pb_plan_s tmp;
+    int rc = build_plan_host(p, count, &tmp);
+    if (rc) return rc;
+    return (long long)plan_layout(&tmp, false);
+}
+
+int pb_plan_create(const pb_solve_params* p, int count, pb_plan* out)
+{
+    if (!p || !out || count <= 0) return fail(PB_ERR_INVALID, "bad arguments");
+    *out = nullptr;
+    if (pb_device_count() <= 0) return fail(PB_ERR_CUDA, "no CUDA device");
+    pb_plan_s* P = new pb_plan_s();
+    int rc = build_plan_host(p, count, P);
+    if (!rc) rc = plan_alloc(P);
+    if (rc) {
+        plan_free(P);
+        return rc;
+    }
+    *out = P;
+    return PB_OK;
+}
+
+int pb_plan_destroy(pb_plan plan)
+{
+    if (plan) {
+        cudaStreamSynchronize(plan->stream);
+        plan_free(plan);
+    }
+    return PB_OK;
+}
+
+long long pb_plan_device_bytes(pb_plan plan) { return plan ? (long long)plan->arena_bytes : 0; }
+
+int pb_plan_kernel_count(pb_plan plan) { return plan ? plan->graph_kernels : 0; }
+
+int pb_plan_instance_info(pb_plan plan, int i, pb_instance_info* info)
+{
+    if (!plan || !info || i < 0 || i >= plan->count) return fail(PB_ERR_INVALID, "bad arguments");
+    const Resolved& R = plan->res[i];
+    info->d = R.d;
+    info->rc = R.rc;
+    info->eta = R.eta;
+    info->m_std = R.m;
+    for (int a = 0; a < 3; a++) {
+        info->M[a] = R.M[a];
+        info->ncell[a] = R.nc[a];
+    }
+    info->P = R.P;
+    info->npoly = plan->htab[i].nd;
+    info->pairs_est = R.pairs_est;
+    return PB_OK;
+}
+
+int pb_plan_set_timing(pb_plan plan, int enable)
+{
+    if (!plan) return fail(PB_ERR_INVALID, "null plan");
+    plan->timing = enable != 0;
+    return PB_OK;
+}
+
+int pb_plan_stage_ms(pb_plan plan, double* ms6)
+{
+    if (!plan || !ms6) return fail(PB_ERR_INVALID, "bad arguments");
+    for (int k = 0; k < 6; k++) ms6[k] = plan->stage_ms[k];
+    return PB_OK;
+}
+
+int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y, double* U, int where,
+                    void* stream_v)
+{
+    if (!P) return fail(PB_ERR_INVALID, "null plan");
+    if ((P->n_src > 0 && (!x || !f)) || (P->n_tgt > 0 && !U) || (!P->all_same && P->n_y > 0 && !y))
+        return fail(PB_ERR_INVALID, "null buffer");
+    if (where != PB_HOST && where != PB_DEVICE) return fail(PB_ERR_INVALID, "bad memory location");
+    cudaStream_t us = (cudaStream_t)stream_v;
+    cudaStream_t s = P->stream;
+    if (where == PB_HOST) {
+        for (size_t i = 0; i < 3 * (size_t)P->n_src; i++)
+            if (!std::isfinite(x[i]) || !std::isfinite(f[i])) return fail(PB_ERR_INVALID, "non-finite input");
+        if (!P->all_same)
+            for (size_t i = 0; i < 3 * (size_t)P->n_y; i++)
+                if (!std::isfinite(y[i])) return fail(PB_ERR_INVALID, "non-finite target");
+    }
+    PB_CK(cudaEventRecord(P->ev_in, us));
+    PB_CK(cudaStreamWaitEvent(s, P->ev_in, 0));
+    cudaMemcpyKind kin = where == PB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if (P->n_src > 0) {
+        PB_CK(cudaMemcpyAsync(P->x, x, sizeof(double) * 3 * P->n_src, kin, s));
+        PB_CK(cudaMemcpyAsync(P->f, f, sizeof(double) * 3 * P->n_src, kin, s));
+    }
+    if (!P->all_same && P->n_y > 0) PB_CK(cudaMemcpyAsync(P->y, y, sizeof(double) * 3 * P->n_y, kin, s));
+    if (P->n_tgt > 0) {
+        if (P->timing || P->exec_count < 1) {
+            run_compute(P, s);
+        } else {
+            if (!P->gexec) {
+                cudaGraph_t g;
+                PB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                run_compute(P, s);
+                PB_CK(cudaStreamEndCapture(s, &g));
+                size_t nn = 0;
+                cudaGraphGetNodes(g, nullptr, &nn);
+                std::vector<cudaGraphNode_t> nodes(nn);
+                cudaGraphGetNodes(g, nodes.data(), &nn);
+                P->graph_kernels = 0;
+                for (auto nd : nodes) {
+                    cudaGraphNodeType ty;
+                    if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+                        P->graph_kernels++;
+                }
+                cudaError_t e = cudaGraphInstantiate(&P->gexec, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) return fail(PB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+            }
+            PB_CK(cudaGraphLaunch(P->gexec, s));
+        }
+        PB_CK(cudaGetLastError());
+        cudaMemcpyKind kout = where == PB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        PB_CK(cudaMemcpyAsync(U, P->U, sizeof(double) * 3 * P->n_tgt, kout, s));
+    }
+    P->exec_count++;
+    PB_CK(cudaEventRecord(P->ev_out, s));
+    PB_CK(cudaStreamWaitEvent(us, P->ev_out, 0));
+    if (where == PB_HOST || P->timing) PB_CK(cudaStreamSynchronize(s));
+    if (P->timing) {
+        float ms;
+        for (int k = 0; k < 6; k++) {
+            cudaEventElapsedTime(&ms, P->tev[k], P->tev[k + 1]);
+            P->stage_ms[k] = ms;
+        }
+    }
+    return PB_OK;
+}
+
+int pb_solve(const pb_solve_params* p, const double* x, const double* f, const double* y, double* U, int where,
+             void* stream)
+{
+    pb_plan P = nullptr;
+    int rc = pb_plan_create(p, 1, &P);
+    if (rc) return rc;
+    rc = pb_plan_execute(P, x, f, y, U, where, stream);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(P->stream);
+        if (e != cudaSuccess) rc = fail(PB_ERR_CUDA, "%s", cudaGetErrorString(e));
+    }
+    pb_plan_destroy(P);
+    return rc;
+}
+
+// ---- reference-facing entry points ----
+
+int pb_periodic_brinkman_ex(double* dA, const double* dx, int m, const double* dx0, int n, double a, double d,
+                            double e, const int* Mx, const int* Nx, const double* L, int tau_scaled, void* stream)
+{
+    if (m < 0 || n < 0 || !L || !Mx || !Nx) return fail(PB_ERR_INVALID, "bad arguments");
+    if ((m > 0 && !dx) || (n > 0 && !dx0) || (m > 0 && n > 0 && !dA)) return fail(PB_ERR_INVALID, "null buffer");
+    for (int q = 0; q < 3; q++)
+        if (!std::isfinite(L[q]) || !(L[q] > 0)) return fail(PB_ERR_INVALID, "L must be > 0");
+    if (!std::isfinite(a) || !(a > 0) || !std::isfinite(d) || !(d > 0) || !std::isfinite(e) || e < 0)
+        return fail(PB_ERR_INVALID, "need alpha > 0, d > 0, e >= 0");
+    if (pb_device_count() <= 0) return fail(PB_ERR_CUDA, "no CUDA device");
+    int rc = launch_dense_matrix(dA, dx, m, dx0, n, a, d, e, Mx, Nx, L, tau_scaled, (cudaStream_t)stream);
+    if (rc) return fail(PB_ERR_UNSUPPORTED, "more than 256 Fourier shells per axis");
+    PB_CK(cudaGetLastError());
+    return PB_OK;
+}
+
+int pb_periodic_brinkman(double* dA, const double* dx, int m, const double* dx0, int n, double a, double d,
+                         double e, int M, int N, const double* L, int maxBlockSize)
+{
+    if (maxBlockSize <= 0) return fail(PB_ERR_INVALID, "maxBlockSize must be > 0");
+    if (!L) return fail(PB_ERR_INVALID, "null L");
+    // per-axis shell counts (cuda/periodicBrinkman.h:457-487)
+    int Mx[3] = {M, M, M}, Nx[3] = {N, N, N}, idL[3] = {0, 1, 2}, t;
+    if (L[idL[0]] > L[idL[1]]) {
+        t = idL[0];
+        idL[0] = idL[1];
+        idL[1] = t;
+    }
+    if (L[idL[2]] <= L[idL[0]]) {
+        t = idL[2];
+        idL[2] = idL[1];
+        idL[1] = idL[0];
+        idL[0] = t;
+    } else if (L[idL[2]] < L[idL[1]]) {
+        t = idL[1];
+        idL[1] = idL[2];
+        idL[2] = t;
+    }
+    Mx[idL[2]] = (int)std::ceil(M * L[idL[0]] / L[idL[2]]);
+    Mx[idL[1]] = (int)std::ceil(M * L[idL[0]] / L[idL[1]]);
+    Nx[idL[0]] = (int)std::ceil(N * L[idL[2]] / L[idL[0]]);
+    Nx[idL[1]] = (int)std::ceil(N * L[idL[2]] / L[idL[1]]);
+    if (M < 0) Mx[0] = Mx[1] = Mx[2] = -1;
+    if (N <= 0) Nx[0] = Nx[1] = Nx[2] = 0;
+    int rc = pb_periodic_brinkman_ex(dA, dx, m, dx0, n, a, d, e, Mx, Nx, L, 1, nullptr);
+    if (rc) return rc;
+    PB_CK(cudaStreamSynchronize(nullptr));
+    return PB_OK;
+}
+
+int pb_fft_brinkman(double* U, const double* y, int m_tgt, const double* f, const double* xn, int n,
+                    const double* L, const int* M, const int* P, int msd, int C, double e, double tol, double d,
+                    double alpha)
+{
+    (void)C;
+    (void)tol;
+    if (!L || !M || !P || msd <= 0) return fail(PB_ERR_INVALID, "bad arguments");
+    pb_solve_params p;
+    std::memset(&p, 0, sizeof(p));
+    p.n_src = n;
+    p.n_tgt = m_tgt;
+    if (m_tgt == 0) return PB_OK;
+    for (int a = 0; a < 3; a++) {
+        p.L[a] = L[a];
+        p.M[a] = M[a];
+    }
+    p.alpha = alpha;
+    p.eps = e;
+    p.d = d;
+    p.P = P[0];
+    p.m_std = msd;
+    p.tol = 1e-6;
+    p.rc = d;  // unused: k space only
+    p.precision = PB_PREC_FP64;
+    p.flags = PB_KSPACE;
+    return pb_solve(&p, xn, f, y, U, PB_HOST, nullptr);
+}
+
+int pb_debug_pair_kernel(double alpha, double d, double eps, double rc, int n, const double* r, double* H1,
+                         double* H2)
+{
+    PbTables T;
+    if (build_tables(alpha, d, eps, rc, 1e-9, &T)) return fail(PB_ERR_INVALID, "bad kernel parameters");
+    for (int i = 0; i < n; i++) {
+        float rf = (float)r[i];
+        float r2 = rf * rf;
+        if (r2 < T.rtiny2f || r2 == 0.f) {
+            double rr = (double)rf * rf, h1 = 0, h2 = 0;
+            if (T.blob) {
+                double p1 = T.ser1[kNumSeries - 1], p2 = T.ser2[kNumSeries - 1];
+                for (int m = kNumSeries - 2; m >= 0; m--) {
+                    p1 = p1 * rr + T.ser1[m];
+                    p2 = p2 * rr + T.ser2[m];
+                }
+                h1 = p1;
+                h2 = p2;
+            } else {
+                h1 = T.self1;
+            }
+            H1[i] = h1;
+            H2[i] = h2;
+            continue;
+        }
+        float ri = 1.0f / rf;
+        float t = rf * T.td_scale + T.td_off;
+        float T1 = T.pd1[T.nd - 1], T2 = T.pd2[T.nd - 1];
+        for (int k = T.nd - 2; k >= 0; k--) {
+            T1 = std::fma(T1, t, T.pd1[k]);
+            T2 = std::fma(T2, t, T.pd2[k]);
+        }
+        if (r2 < T.rs2) {
+            float te = rf * T.te_scale + T.te_off;
+            float E1 = T.pe1[T.ne - 1], E2 = T.pe2[T.ne - 1];
+            for (int k = T.ne - 2; k >= 0; k--) {
+                E1 = std::fma(E1, te, T.pe1[k]);
+                E2 = std::fma(E2, te, T.pe2[k]);
+            }
+            T1 -= E1;
+            T2 -= E2;
+        }
+        H1[i] = T1 * ri;
+        H2[i] = T2 * (ri * ri * ri);
+    }
+    return PB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,297 @@
+// Host-side FP64 mathematics of the regularized Brinkman kernel: closed forms,
+// stable small-r expansions and the FP32 polynomial tables of the real-space
+// pair kernel.  See pb_kernel_math.h.
+#include "pb_kernel_math.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace pb {
+
+static const double kPi = 3.14159265358979323846264338327950288;
+static const double kSqrtPi = 1.77245385090551602729816748334114518;
+
+double phihat(double kn, double a, double d)
+{
+    double a1 = -std::expm1(-a * a * d * d / 4);
+    return (1.0 + a1 * kn / (a * a)) * std::exp(-d * d * kn / 4);
+}
+
+// exp(2xz) erfc(z + x), zero where both are large and xz >= 0
+// (cuda/periodicBrinkman.h:19-25).
+static double experf(double x, double z)
+{
+    if ((x * z < 0) || (x * x + z * z < 700)) return std::exp(2 * x * z) * std::erfc(z + x);
+    return 0.0;
+}
+
+void diffH_closed(double r, double a, double d, double* h1, double* h2)
+{
+    // cuda/periodicBrinkman.h:91-104
+    double r2 = r * r;
+    double ex = std::exp(-r2 / (d * d)) * (-std::expm1(-a * a * d * d / 4));
+    double ec = std::erfc(r / d);
+    double em = experf(-a * d / 2, r / d), ep = experf(a * d / 2, r / d);
+    double pre = 1.0 / (8 * kPi * a * a * r2 * r);
+    double g = 1.0 / (2 * a * a * d * d * d * kPi * kSqrtPi);
+    double H1 = -2 * pre * ec;
+    H1 -= (d * d + 2 * r2) * g / r2 * ex;
+    H1 += pre * (1 + a * r + a * a * r2) * em;
+    H1 += pre * (1 - a * r + a * a * r2) * ep;
+    double H2 = 6 * pre / r2 * ec;
+    H2 += (3 * d * d + 2 * r2) * g / (r2 * r2) * ex;
+    H2 -= pre / r2 * (3 + 3 * a * r + a * a * r2) * em;
+    H2 -= pre / r2 * (3 - 3 * a * r + a * a * r2) * ep;
+    *h1 = H1;
+    *h2 = H2;
+}
+
+void scaled_singular(double r, double a, double* rS1, double* r3S2)
+{
+    // r S1 = A1(u)/(4 pi), r^3 S2 = A2(u)/(4 pi), u = a r, from the singular
+    // Brinkmanlet of cuda/periodicBrinkman.h:41-42; power series below u = 0.5.
+    double u = a * r, A1, A2;
+    if (u < 0.5) {
+        double s1 = 0, s2 = 0, p = 1, fact = 2;
+        for (int k = 2; k < 40; k++) {
+            double sg = (k & 1) ? -1.0 : 1.0;
+            double t1 = sg * (k - 1.0) * (k - 1.0) / fact * p;
+            double t2 = -sg * (k - 1.0) * (k - 3.0) / fact * p;
+            s1 += t1;
+            s2 += t2;
+            if (k > 4 && std::fabs(t1) < 1e-19 * std::fabs(s1) && std::fabs(t2) < 1e-19 * std::fabs(s2)) break;
+            p *= u;
+            fact *= (k + 1);
+        }
+        A1 = s1;
+        A2 = s2;
+    } else {
+        double em = std::exp(-u);
+        A1 = (-1 + em * (1 + u + u * u)) / (u * u);
+        A2 = (3 - em * (3 + 3 * u + u * u)) / (u * u);
+    }
+    *rS1 = A1 / (4 * kPi);
+    *r3S2 = A2 / (4 * kPi);
+}
+
+// 16-point Gauss-Legendre rule on [-1, 1].
+static void gauss_legendre16(double* x, double* w)
+{
+    const int n = 16;
+    for (int i = 0; i < n; i++) {
+        double z = std::cos(kPi * (i + 0.75) / (n + 0.5)), dp = 1;
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1, p1 = z;
+            for (int k = 2; k <= n; k++) {
+                double p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (z * p1 - p0) / (z * z - 1);
+            double dz = p1 / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-17) break;
+        }
+        x[i] = z;
+        w[i] = 2 / ((1 - z * z) * dp * dp);
+    }
+}
+
+// Dimensionless moments Kt_j = int_0^inf [1 + c q^2/b^2] e^{-q^2/4} q^{2j}/(q^2+b^2) dq,
+// b = a*delta, c = 1 - e^{-b^2/4}; K_j = delta^{1-2j} Kt_j.
+static void scaled_moments(double b, int nj, double* Kt)
+{
+    double gx[16], gw[16];
+    gauss_legendre16(gx, gw);
+    double c = -std::expm1(-b * b / 4);
+    double qmax = 2 * std::sqrt((double)nj) + 18.0;
+    std::vector<double> edges;
+    for (double q = 0; q < qmax; q += 0.5) edges.push_back(q);
+    edges.push_back(qmax);
+    for (int j = -6; j <= 4; j++) {
+        double e = b * std::ldexp(1.0, j);
+        if (e > 0 && e < qmax) edges.push_back(e);
+    }
+    std::sort(edges.begin(), edges.end());
+    for (int j = 0; j < nj; j++) Kt[j] = 0;
+    for (size_t p = 0; p + 1 < edges.size(); p++) {
+        double lo = edges[p], hi = edges[p + 1];
+        if (hi - lo < 1e-15) continue;
+        double mid = 0.5 * (lo + hi), h = 0.5 * (hi - lo);
+        for (int q = 0; q < 16; q++) {
+            double k = mid + h * gx[q], k2 = k * k;
+            double g = (1.0 + c * k2 / (b * b)) * std::exp(-k2 / 4) / (k2 + b * b) * gw[q] * h;
+            double pw = 1;
+            for (int j = 0; j < nj; j++) {
+                Kt[j] += g * pw;
+                pw *= k2;
+            }
+        }
+    }
+}
+
+void blob_moments(double a, double delta, int nj, double* K)
+{
+    std::vector<double> Kt(nj);
+    scaled_moments(a * delta, nj, Kt.data());
+    for (int j = 0; j < nj; j++) K[j] = Kt[j] * std::pow(delta, 1.0 - 2.0 * j);
+}
+
+// Scaled series of R_delta: H1 = (1/delta) sum c1[m] rho^{2m}, H2 = (1/delta^3) sum c2[m] rho^{2m},
+// rho = r/delta.  From the radial Fourier integral of the modified blob:
+// H1 = 1/(2pi^2) int phihat k^2/(k^2+a^2) [j0 - j1/z](kr) dk,
+// H2 = 1/(2pi^2) int phihat k^4/(k^2+a^2) [j2/z^2](kr) dk.
+static void scaled_series(double b, int nterms, double* c1, double* c2)
+{
+    std::vector<double> Kt(nterms + 2);
+    scaled_moments(b, nterms + 2, Kt.data());
+    double f1 = 4.0 / 6.0;  // 4(m+1)^2/(2m+3)! at m = 0
+    double f2 = 1.0 / 15.0; // 1/(2^m m! (2m+5)!!) at m = 0
+    for (int m = 0; m < nterms; m++) {
+        double sg = (m & 1) ? -1.0 : 1.0;
+        c1[m] = sg * f1 * Kt[m + 1] / (2 * kPi * kPi);
+        c2[m] = sg * f2 * Kt[m + 2] / (2 * kPi * kPi);
+        f1 *= (m + 2.0) * (m + 2.0) / ((m + 1.0) * (m + 1.0) * (2 * m + 4.0) * (2 * m + 5.0));
+        f2 *= 1.0 / (2.0 * (m + 1.0) * (2 * m + 7.0));
+    }
+}
+
+void regularized_series(double a, double delta, int nterms, double* s1, double* s2)
+{
+    std::vector<double> c1(nterms), c2(nterms);
+    scaled_series(a * delta, nterms, c1.data(), c2.data());
+    for (int m = 0; m < nterms; m++) {
+        s1[m] = c1[m] / std::pow(delta, 2.0 * m + 1);
+        s2[m] = c2[m] / std::pow(delta, 2.0 * m + 3);
+    }
+}
+
+void scaled_diffH(double r, double a, double delta, const double* ser1, const double* ser2, int nser,
+                  double* T1, double* T2)
+{
+    if (r == 0) {
+        *T1 = 1.0 / (8 * kPi);
+        *T2 = 1.0 / (8 * kPi);
+        return;
+    }
+    if (r < delta) {
+        // S - R_delta with R_delta from its series (no 1/r^3 cancellation)
+        double rs1, r3s2;
+        scaled_singular(r, a, &rs1, &r3s2);
+        double r2 = r * r, R1 = 0, R2 = 0, p = 1;
+        for (int m = 0; m < nser; m++) {
+            R1 += ser1[m] * p;
+            R2 += ser2[m] * p;
+            p *= r2;
+        }
+        *T1 = rs1 - r * R1;
+        *T2 = r3s2 - r * r2 * R2;
+        return;
+    }
+    double h1, h2;
+    diffH_closed(r, a, delta, &h1, &h2);
+    *T1 = r * h1;
+    *T2 = r * r * r * h2;
+}
+
+std::vector<double> fit_monomial(const std::function<double(double)>& f, double lo, double hi, int nodes,
+                                 double rel_tol, int max_terms)
+{
+    std::vector<double> v(nodes), c(nodes);
+    for (int k = 0; k < nodes; k++) {
+        double t = std::cos(kPi * (k + 0.5) / nodes);
+        v[k] = f(lo + (hi - lo) * (t + 1) / 2);
+    }
+    double cmax = 0;
+    for (int j = 0; j < nodes; j++) {
+        double s = 0;
+        for (int k = 0; k < nodes; k++) s += v[k] * std::cos(kPi * j * (k + 0.5) / nodes);
+        c[j] = s * 2.0 / nodes;
+        cmax = std::max(cmax, std::fabs(c[j]));
+    }
+    c[0] *= 0.5;
+    int n = 1;
+    for (int j = 0; j < nodes; j++)
+        if (std::fabs(c[j]) > rel_tol * cmax) n = j + 1;
+    n = std::min(n, max_terms);
+    // Chebyshev -> monomial in t: T_{j+1} = 2 t T_j - T_{j-1}
+    std::vector<double> a(n, 0.0), Tm1(n, 0.0), T0(n, 0.0), T1(n, 0.0);
+    T0[0] = 1;
+    if (n > 1) T1[1] = 1;
+    for (int j = 0; j < n; j++) {
+        const std::vector<double>& Tj = (j == 0) ? T0 : T1;
+        for (int q = 0; q < n; q++) a[q] += c[j] * Tj[q];
+        if (j >= 1) {
+            std::vector<double> Tn(n, 0.0);
+            for (int q = 0; q + 1 < n; q++) Tn[q + 1] += 2 * T1[q];
+            for (int q = 0; q < n; q++) Tn[q] -= T0[q];
+            T0 = T1;
+            T1 = Tn;
+        }
+    }
+    return a;
+}
+
+int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t)
+{
+    if (!(a > 0) || !(d > 0) || !(rc > 0) || eps < 0) return -1;
+    std::memset(t, 0, sizeof(PbTables));
+    const int nser = 40;
+    std::vector<double> sd1(nser), sd2(nser), se1(nser), se2(nser);
+    regularized_series(a, d, nser, sd1.data(), sd2.data());
+    const int nodes = 40;
+    auto Td1 = [&](double r) { double x, y; scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &x, &y); return x; };
+    auto Td2 = [&](double r) { double x, y; scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &x, &y); return y; };
+    std::vector<double> p1 = fit_monomial(Td1, 0, rc, nodes, poly_tol, kMaxPoly);
+    std::vector<double> p2 = fit_monomial(Td2, 0, rc, nodes, poly_tol, kMaxPoly);
+    int nd = (int)std::max(p1.size(), p2.size());
+    p1.resize(nd, 0.0);
+    p2.resize(nd, 0.0);
+    for (int k = 0; k < nd; k++) {
+        t->pd1[k] = (float)p1[k];
+        t->pd2[k] = (float)p2[k];
+    }
+    t->nd = nd;
+    t->td_scale = (float)(2.0 / rc);
+    t->td_off = -1.0f;
+    t->rc2 = (float)(rc * rc);
+    if (eps > 0) {
+        regularized_series(a, eps, nser, se1.data(), se2.data());
+        double rs = std::min(5.6 * eps, rc);
+        auto Te1 = [&](double r) { double x, y; scaled_diffH(r, a, eps, se1.data(), se2.data(), nser, &x, &y); return x; };
+        auto Te2 = [&](double r) { double x, y; scaled_diffH(r, a, eps, se1.data(), se2.data(), nser, &x, &y); return y; };
+        std::vector<double> q1 = fit_monomial(Te1, 0, rs, nodes, poly_tol, kMaxPoly);
+        std::vector<double> q2 = fit_monomial(Te2, 0, rs, nodes, poly_tol, kMaxPoly);
+        int ne = (int)std::max(q1.size(), q2.size());
+        q1.resize(ne, 0.0);
+        q2.resize(ne, 0.0);
+        for (int k = 0; k < ne; k++) {
+            t->pe1[k] = (float)q1[k];
+            t->pe2[k] = (float)q2[k];
+        }
+        t->ne = ne;
+        t->te_scale = (float)(2.0 / rs);
+        t->te_off = -1.0f;
+        t->rs2 = (float)(rs * rs);
+        t->blob = 1;
+        double rt = 0.8 * eps;
+        t->rtiny2 = rt * rt;
+        t->rtiny2f = (float)(rt * rt);
+        for (int m = 0; m < kNumSeries; m++) {
+            t->ser1[m] = se1[m] - sd1[m];
+            t->ser2[m] = se2[m] - sd2[m];
+        }
+        t->self1 = t->ser1[0];
+    } else {
+        t->ne = 0;
+        t->rs2 = 0;
+        t->blob = 0;
+        t->rtiny2 = 0;
+        t->rtiny2f = 0;
+        t->self1 = -sd1[0];  // -R_d(0): the reference's r -> 0 limit of diffH(d)
+    }
+    return 0;
+}
+
+}  // namespace pb

@@ -1,0 +1,80 @@
+// Launch wrappers for the CUDA kernels of the evaluator (host-callable).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pb_types.h"
+
+namespace pb {
+
+// ---- binning and sorting (pb_sort.cu) ----
+// cell_of[p] = global cell index of particle p (instance cell_off + local cell),
+// counts[cell] += 1.  pos: AoS doubles of all instances, offsets: ninst+1 prefix.
+void launch_bin(const double* pos, int ntot, const int* offsets, const PbInst* inst, int ninst,
+                int* cell_of, int* counts, cudaStream_t s);
+// Exclusive scan of n ints into out (out has n+1 entries; out[n] = total).
+// tmp must hold scan_tmp_ints(n) ints.
+size_t scan_tmp_ints(int n);
+void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s);
+// perm[start[c] + k] = particle, fill must be zeroed.
+void launch_scatter(const int* cell_of, int ntot, const int* start, int* fill, int* perm, cudaStream_t s);
+// Sort each cell's perm entries ascending (deterministic order).
+void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell, cudaStream_t s);
+// Sorted particle records.  Mixed: pos_hi (x,y,z, w = instance bits), pos_lo, frc.
+void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ntot, const int* offsets,
+                          const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out,
+                          cudaStream_t s);
+void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ntot, const int* offsets,
+                         const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, cudaStream_t s);
+// Work items: one per (target cell, chunk of <= 32 targets): int4 {inst, cell, first, count}.
+void launch_count_chunks(const int* start, int ncell_tot, int* chunks, cudaStream_t s);
+void launch_emit_items(const int* start, const int* chunk_start, int ncell_tot, const int* cell_offsets,
+                       int ninst, int4* items, cudaStream_t s);
+
+// ---- real space (pb_real.cu) ----
+// Mixed precision: FP32 polynomial kernel, hi/lo displacements, Kahan sums.
+void launch_real_mixed(int npoly, const PbInst* inst, const PbTables* tab, const int4* items, const int* nitems_ptr,
+                       int nitems_max,
+                       const float4* spos_hi, const float4* spos_lo, const float4* sfrc, const int* src_start,
+                       const float4* tpos_hi, const float4* tpos_lo, float* u_s, float* u_c, double* u_near,
+                       int* counter, int nsm, cudaStream_t s);
+// FP64: closed forms of the reference with the FP64 series below r_tiny.
+void launch_real_fp64(const PbInst* inst, const PbTables* tab, const int4* items, const int* nitems_ptr,
+                      int nitems_max, const Dbl4* spos, const Dbl4* sfrc, const int* src_start,
+                      const Dbl4* tpos, double* u, int* counter, int nsm, cudaStream_t s);
+
+// ---- k space (pb_kspace.cu) ----
+template <class T>
+void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int ntot, const void* pos_a,
+                   const void* pos_b, const void* frc, T* grid, cudaStream_t s);
+template <class T>
+void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int ntot, const void* pos_a,
+                   const void* pos_b, const T* grid, T* u_k, cudaStream_t s);
+// Batched 3D R2C -> Green multiply -> C2R over `nvol` volumes of equal size
+// (3 components per instance, instances contiguous).
+template <class T>
+void launch_kspace_fft(const PbInst* inst_dev, const int* bucket_inst, int ninst_bucket, long long base_off,
+                       const int* M, T* grid, void* spec, const void* twiddles, cudaStream_t s);
+size_t twiddle_bytes(const int* M, bool fp64);
+void fill_twiddles(const int* M, bool fp64, void* host_buf);
+
+// Gather the packed target list: instance q's targets come from y (its own
+// targets) or from x (targets are its sources).
+void launch_pack_targets(const double* x, const double* y, int ntot, const int* tgt_off, const int* src_off,
+                         const int* y_off, int ninst, double* out, cudaStream_t s);
+
+// ---- final combine ----
+void launch_combine_mixed(const PbInst* inst, int ninst, const int* tgt_offsets, int ntot, const int* tperm,
+                          const float* u_s, const float* u_c, const double* u_near, const float* u_k, int use_real,
+                          int use_k, const double* fsum, double* U, cudaStream_t s);
+void launch_combine_fp64(const PbInst* inst, int ninst, const int* tgt_offsets, int ntot, const int* tperm,
+                         const double* u_real, const double* u_k, int use_real, int use_k, const double* fsum,
+                         double* U, cudaStream_t s);
+// Per-instance force sums (for the optional k = 0 mode): out[3*q + c] = sum f.
+void launch_force_sums(const double* frc, const int* offsets, int ninst, double* out, cudaStream_t s);
+
+// ---- dense mobility matrix (pb_dense.cu) ----
+int launch_dense_matrix(double* dA, const double* dx, int m, const double* dx0, int n, double a, double d, double e,
+                        const int* Mx, const int* Nx, const double* L, int tau_scaled, cudaStream_t s);
+
+}  // namespace pb

@@ -1,0 +1,281 @@
+// Cell binning, counting sort and work-item construction for the real-space
+// sum (device-built cell list over all instances of a batch).
+#include "pb_device.cuh"
+#include "pb_kernels.h"
+
+namespace pb {
+
+__global__ void k_bin(const double* __restrict__ pos, int ntot, const int* __restrict__ offsets,
+                      const PbInst* __restrict__ inst, int ninst, int* __restrict__ cell_of, int* __restrict__ counts)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ntot) return;
+    int q = find_instance(offsets, ninst, p);
+    const PbInst& I = inst[q];
+    int c[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        double w = wrap_coord(pos[3 * (size_t)p + a], I.L[a]);
+        int ci = (int)(w / I.h[a]);
+        c[a] = ci >= I.nc[a] ? I.nc[a] - 1 : ci;
+    }
+    int g = I.cell_off + (c[0] * I.nc[1] + c[1]) * I.nc[2] + c[2];
+    cell_of[p] = g;
+    atomicAdd(&counts[g], 1);
+}
+
+void launch_bin(const double* pos, int ntot, const int* offsets, const PbInst* inst, int ninst, int* cell_of,
+                int* counts, cudaStream_t s)
+{
+    if (ntot <= 0) return;
+    k_bin<<<(ntot + 255) / 256, 256, 0, s>>>(pos, ntot, offsets, inst, ninst, cell_of, counts);
+}
+
+// ---- exclusive scan (reduce-then-scan, recursive over block sums) ----
+constexpr int kScanBlock = 1024;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums)
+{
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = (lane < (int)(blockDim.x >> 5)) ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(kFull, w, o);
+            if (lane >= o) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    int base = wid > 0 ? warp_sums[wid - 1] : 0;
+    return base + x - v;
+}
+
+__global__ void k_scan_blocks(const int* __restrict__ in, int* __restrict__ out, int n, int* __restrict__ block_sums)
+{
+    __shared__ int ws[32];
+    int i = blockIdx.x * kScanBlock + threadIdx.x;
+    int v = i < n ? in[i] : 0;
+    int ex = block_exclusive_scan(v, ws);
+    if (i < n) out[i] = ex;
+    if (threadIdx.x == blockDim.x - 1) block_sums[blockIdx.x] = ex + v;
+}
+
+__global__ void k_scan_add(int* __restrict__ out, int n, const int* __restrict__ block_offsets)
+{
+    int i = blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n) out[i] += block_offsets[blockIdx.x];
+}
+
+__global__ void k_set_total(int* out, int n, const int* in)
+{
+    // out[n] = out[n-1] + in[n-1]
+    out[n] = (n > 0) ? out[n - 1] + in[n - 1] : 0;
+}
+
+size_t scan_tmp_ints(int n)
+{
+    size_t total = 0;
+    int m = n;
+    while (m > 1) {
+        int nb = (m + kScanBlock - 1) / kScanBlock;
+        total += 2 * (size_t)nb + 2;
+        m = nb;
+    }
+    return total + 4;
+}
+
+static void scan_rec(const int* in, int* out, int n, int* tmp, cudaStream_t s)
+{
+    int nb = (n + kScanBlock - 1) / kScanBlock;
+    int* sums = tmp;
+    int* sums_scan = tmp + nb + 1;
+    k_scan_blocks<<<nb, kScanBlock, 0, s>>>(in, out, n, sums);
+    if (nb > 1) {
+        scan_rec(sums, sums_scan, nb, tmp + 2 * (size_t)nb + 2, s);
+        k_scan_add<<<nb, kScanBlock, 0, s>>>(out, n, sums_scan);
+    }
+}
+
+void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s)
+{
+    if (n <= 0) {
+        cudaMemsetAsync(out, 0, sizeof(int), s);
+        return;
+    }
+    scan_rec(in, out, n, tmp, s);
+    k_set_total<<<1, 1, 0, s>>>(out, n, in);
+}
+
+__global__ void k_scatter(const int* __restrict__ cell_of, int ntot, const int* __restrict__ start,
+                          int* __restrict__ fill, int* __restrict__ perm)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ntot) return;
+    int c = cell_of[p];
+    int slot = start[c] + atomicAdd(&fill[c], 1);
+    perm[slot] = p;
+}
+
+void launch_scatter(const int* cell_of, int ntot, const int* start, int* fill, int* perm, cudaStream_t s)
+{
+    if (ntot <= 0) return;
+    k_scatter<<<(ntot + 255) / 256, 256, 0, s>>>(cell_of, ntot, start, fill, perm);
+}
+
+// Rank sort of each cell's entries (warp per cell): entry v goes to slot
+// start + #{u in cell : u < v}.  Entries are distinct particle indices.
+__global__ void k_sort_cells(const int* __restrict__ perm_in, int* __restrict__ perm_out,
+                             const int* __restrict__ start, int ncell)
+{
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= ncell) return;
+    int b = start[warp], e = start[warp + 1], n = e - b;
+    if (n <= 1) {
+        if (n == 1 && lane == 0) perm_out[b] = perm_in[b];
+        return;
+    }
+    if (n > 4096) {  // very large cells keep the scatter order
+        for (int i = lane; i < n; i += 32) perm_out[b + i] = perm_in[b + i];
+        return;
+    }
+    for (int i = lane; i < n; i += 32) {
+        int v = perm_in[b + i], rank = 0;
+        for (int j = 0; j < n; j++) rank += (perm_in[b + j] < v);
+        perm_out[b + rank] = v;
+    }
+}
+
+void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell, cudaStream_t s)
+{
+    if (ncell <= 0) return;
+    long long threads = (long long)ncell * 32;
+    int blocks = (int)((threads + 255) / 256);
+    k_sort_cells<<<blocks, 256, 0, s>>>(perm, perm_tmp, start, ncell);
+}
+
+__global__ void k_prepare_mixed(const double* __restrict__ pos, const double* __restrict__ frc,
+                                const int* __restrict__ perm, int ntot, const int* __restrict__ offsets,
+                                const PbInst* __restrict__ inst, int ninst, float4* __restrict__ pos_hi,
+                                float4* __restrict__ pos_lo, float4* __restrict__ frc_out)
+{
+    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sidx >= ntot) return;
+    int p = perm[sidx];
+    int q = find_instance(offsets, ninst, p);
+    const PbInst& I = inst[q];
+    float hi[3], lo[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) split_double(wrap_coord(pos[3 * (size_t)p + a], I.L[a]), hi[a], lo[a]);
+    pos_hi[sidx] = make_float4(hi[0], hi[1], hi[2], __int_as_float(q));
+    pos_lo[sidx] = make_float4(lo[0], lo[1], lo[2], 0.f);
+    if (frc)
+        frc_out[sidx] = make_float4((float)frc[3 * (size_t)p], (float)frc[3 * (size_t)p + 1],
+                                    (float)frc[3 * (size_t)p + 2], 0.f);
+}
+
+void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ntot, const int* offsets,
+                          const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out,
+                          cudaStream_t s)
+{
+    if (ntot <= 0) return;
+    k_prepare_mixed<<<(ntot + 255) / 256, 256, 0, s>>>(pos, frc, perm, ntot, offsets, inst, ninst, pos_hi, pos_lo,
+                                                        frc_out);
+}
+
+__global__ void k_prepare_fp64(const double* __restrict__ pos, const double* __restrict__ frc,
+                               const int* __restrict__ perm, int ntot, const int* __restrict__ offsets,
+                               const PbInst* __restrict__ inst, int ninst, Dbl4* __restrict__ pos_out,
+                               Dbl4* __restrict__ frc_out)
+{
+    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sidx >= ntot) return;
+    int p = perm[sidx];
+    int q = find_instance(offsets, ninst, p);
+    const PbInst& I = inst[q];
+    double w[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) w[a] = wrap_coord(pos[3 * (size_t)p + a], I.L[a]);
+    pos_out[sidx] = make_dbl4(w[0], w[1], w[2], (double)q);
+    if (frc) frc_out[sidx] = make_dbl4(frc[3 * (size_t)p], frc[3 * (size_t)p + 1], frc[3 * (size_t)p + 2], 0.0);
+}
+
+void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ntot, const int* offsets,
+                         const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, cudaStream_t s)
+{
+    if (ntot <= 0) return;
+    k_prepare_fp64<<<(ntot + 255) / 256, 256, 0, s>>>(pos, frc, perm, ntot, offsets, inst, ninst, pos_out,
+                                                       frc_out);
+}
+
+__global__ void k_count_chunks(const int* __restrict__ start, int ncell, int* __restrict__ chunks)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    int n = start[c + 1] - start[c];
+    chunks[c] = (n + 31) >> 5;
+}
+
+void launch_count_chunks(const int* start, int ncell_tot, int* chunks, cudaStream_t s)
+{
+    if (ncell_tot <= 0) return;
+    k_count_chunks<<<(ncell_tot + 255) / 256, 256, 0, s>>>(start, ncell_tot, chunks);
+}
+
+__global__ void k_emit_items(const int* __restrict__ start, const int* __restrict__ chunk_start, int ncell,
+                             const int* __restrict__ cell_offsets, int ninst, int4* __restrict__ items)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    int b = start[c], n = start[c + 1] - b;
+    if (n == 0) return;
+    int q = find_instance(cell_offsets, ninst, c);
+    int k0 = chunk_start[c];
+    for (int k = 0; k * 32 < n; k++) {
+        int cnt = min(32, n - 32 * k);
+        items[k0 + k] = make_int4(q, c, b + 32 * k, cnt);
+    }
+}
+
+void launch_emit_items(const int* start, const int* chunk_start, int ncell_tot, const int* cell_offsets, int ninst,
+                       int4* items, cudaStream_t s)
+{
+    if (ncell_tot <= 0) return;
+    k_emit_items<<<(ncell_tot + 255) / 256, 256, 0, s>>>(start, chunk_start, ncell_tot, cell_offsets, ninst, items);
+}
+
+}  // namespace pb
+
+namespace pb {
+
+__global__ void k_pack_targets(const double* __restrict__ x, const double* __restrict__ y, int ntot,
+                               const int* __restrict__ tgt_off, const int* __restrict__ src_off,
+                               const int* __restrict__ y_off, int ninst, double* __restrict__ out)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ntot) return;
+    int q = find_instance(tgt_off, ninst, p);
+    int local = p - tgt_off[q];
+    const double* src = (y_off[q] >= 0) ? (y + 3 * (size_t)(y_off[q] + local)) : (x + 3 * (size_t)(src_off[q] + local));
+    out[3 * (size_t)p] = src[0];
+    out[3 * (size_t)p + 1] = src[1];
+    out[3 * (size_t)p + 2] = src[2];
+}
+
+void launch_pack_targets(const double* x, const double* y, int ntot, const int* tgt_off, const int* src_off,
+                         const int* y_off, int ninst, double* out, cudaStream_t s)
+{
+    if (ntot <= 0) return;
+    k_pack_targets<<<(ntot + 255) / 256, 256, 0, s>>>(x, y, ntot, tgt_off, src_off, y_off, ninst, out);
+}
+
+}  // namespace pb
