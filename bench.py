@@ -171,6 +171,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="run the workload's plan twice (eager, then capture+replay) and exit: for ncu")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -198,6 +200,13 @@ def main():
     xd = torch.from_numpy(x).cuda()
     fd = torch.from_numpy(f).cuda()
     Ud = torch.empty_like(xd)
+    if args.profile:
+        plan.execute(xd, fd, U=Ud)
+        plan.execute(xd, fd, U=Ud)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": w["name"], "info": info, "kernels_per_solve": plan.kernel_count}))
+        plan.close()
+        return
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     stream = torch.cuda.current_stream()
     for _ in range(max(args.warmup, 3)):

@@ -61,7 +61,7 @@ typedef struct pb_solve_params {
     int flags;     /* PB_REAL_SPACE | PB_KSPACE | PB_ZERO_MODE; 0 = default */
 } pb_solve_params;
 
-/* Resolved parameters of one instance of a plan. */
+/* Resolved parameters of one instance (d, rc, grid, support, cells). */
 typedef struct pb_instance_info {
     double d, rc, eta, m_std;
     int M[3];
@@ -125,6 +125,8 @@ int pb_plan_create(const pb_solve_params* p, int count, pb_plan* out);
 int pb_plan_execute(pb_plan plan, const double* x, const double* f, const double* y, double* U, int where,
                     void* stream);
 int pb_plan_instance_info(pb_plan plan, int i, pb_instance_info* info);
+/* The autotuner's choice for one parameter block, on the host (no GPU). */
+int pb_resolve(const pb_solve_params* p, pb_instance_info* info);
 /* Device bytes held by the plan. */
 long long pb_plan_device_bytes(pb_plan plan);
 /* CUDA kernels one execution launches (kernel nodes of the captured graph;

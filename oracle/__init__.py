@@ -175,7 +175,7 @@ def choose_split(n: int, m: int, L) -> float:
     The total is independent of this choice; it only sets the oracle's run
     time (real space ~ m*n*(6d)^3/tau closed-form pairs, k space ~
     (n+m)*tau/d^3 structure-factor terms)."""
-    L = np.asarray(L, dtype=np.float64)
+    L = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
     tau = float(np.prod(L))
     c_r, c_k = 60e-9, 1.5e-9
     real_coef = m * n * (4 * np.pi / 3) * 216.0 / tau * c_r
@@ -197,7 +197,8 @@ def ewald_velocity(y, x, f, L, alpha, eps, d=None, rc=0.0, kc=0.0, real=True, ks
         d = choose_split(n, m, L)
     U = np.zeros((m, 3))
     flags = (REAL if real else 0) | (KSPACE if kspace else 0) | (ZERO_MODE if zero_mode else 0)
-    rcode = lib().pbo_ewald_velocity(_p(U), _p(y), m, _p(x), _p(f), n, _p(_c64(L)), float(alpha), float(eps),
+    Lv = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), (3,)))
+    rcode = lib().pbo_ewald_velocity(_p(U), _p(y), m, _p(x), _p(f), n, _p(Lv), float(alpha), float(eps),
                                      float(d), float(rc), float(kc), flags)
     if rcode != 0:
         raise ValueError("oracle: bad input")

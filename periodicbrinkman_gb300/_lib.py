@@ -113,6 +113,7 @@ def lib():
     L.pb_plan_create.argtypes = [C.POINTER(SolveParams), C.c_int, C.POINTER(vp)]
     L.pb_plan_execute.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp]
     L.pb_plan_instance_info.argtypes = [vp, C.c_int, C.POINTER(InstanceInfo)]
+    L.pb_resolve.argtypes = [C.POINTER(SolveParams), C.POINTER(InstanceInfo)]
     L.pb_plan_device_bytes.restype = C.c_longlong
     L.pb_plan_device_bytes.argtypes = [vp]
     L.pb_plan_kernel_count.argtypes = [vp]

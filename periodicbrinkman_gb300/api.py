@@ -146,6 +146,14 @@ class Plan:
         self.close()
 
 
+def resolve(params: SolveParams) -> dict:
+    """The autotuner's resolved parameters for one instance (host only)."""
+    inf = InstanceInfo()
+    check(lib().pb_resolve(C.byref(params), C.byref(inf)))
+    return {"d": inf.d, "rc": inf.rc, "eta": inf.eta, "m_std": inf.m_std, "M": list(inf.M), "P": inf.P,
+            "ncell": list(inf.ncell), "npoly": inf.npoly, "pairs_est": int(inf.pairs_est)}
+
+
 def estimate_bytes(params: SolveParams | Iterable[SolveParams]) -> int:
     if isinstance(params, SolveParams):
         params = [params]

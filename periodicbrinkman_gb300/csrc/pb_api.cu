@@ -235,6 +235,15 @@ struct pb_plan_s {
     double *u_near = nullptr, *u_real = nullptr, *fsum = nullptr;
     void *u_k = nullptr, *grid = nullptr, *spec = nullptr;
 
+    // binding: a plan is a capacity; pb_plan_bind places actual instances in it
+    int npoly_cap = 0;        // polynomial terms compiled into the captured real-space kernel
+    int bound = 0;            // instances bound (<= count)
+    int act_src = 0, act_tgt = 0, act_y = 0;
+    bool upload_pending = false;
+    char* staging = nullptr;  // pinned host copy of instances, tables and offsets
+    size_t staging_bytes = 0;
+    cudaEvent_t ev_upload = nullptr;
+
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -496,6 +505,11 @@ int build_plan_host(const pb_solve_params* p, int count, pb_plan_s* P)
         npoly = std::max(npoly, P->htab[q].nd);
     }
     P->npoly = npoly;
+    P->npoly_cap = npoly;
+    P->bound = count;
+    P->act_src = P->n_src;
+    P->act_tgt = P->n_tgt;
+    P->act_y = P->n_y;
     return PB_OK;
 }
 
@@ -504,6 +518,8 @@ void plan_free(pb_plan_s* P)
     if (!P) return;
     if (P->gexec) cudaGraphExecDestroy(P->gexec);
     if (P->arena) cudaFree(P->arena);
+    if (P->staging) cudaFreeHost(P->staging);
+    if (P->ev_upload) cudaEventDestroy(P->ev_upload);
     if (P->ev_in) cudaEventDestroy(P->ev_in);
     if (P->ev_out) cudaEventDestroy(P->ev_out);
     for (auto& e : P->tev)
@@ -525,6 +541,9 @@ int plan_alloc(pb_plan_s* P)
     }
     plan_layout(P, true);
     PB_CK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+    P->staging_bytes = (sizeof(PbInst) + sizeof(PbTables)) * (size_t)P->count + 4 * sizeof(int) * (P->count + 1);
+    PB_CK(cudaMallocHost(&P->staging, P->staging_bytes));
+    PB_CK(cudaEventCreateWithFlags(&P->ev_upload, cudaEventDisableTiming));
     PB_CK(cudaEventCreateWithFlags(&P->ev_in, cudaEventDisableTiming));
     PB_CK(cudaEventCreateWithFlags(&P->ev_out, cudaEventDisableTiming));
     for (auto& ev : P->tev) PB_CK(cudaEventCreate(&ev));
@@ -552,7 +571,7 @@ void bin_and_sort(pb_plan_s* P, const double* pos, int n, const int* d_off, int*
     cudaMemsetAsync(fill, 0, sizeof(int) * (P->ncell + 1), s);
     launch_bin(pos, n, d_off, P->d_inst, P->count, cell_of, cnt, s);
     launch_exclusive_scan(cnt, start, P->ncell, P->scan_tmp, s);
-    launch_scatter(cell_of, n, start, fill, perm_tmp, s);
+    launch_scatter(cell_of, n, d_off + P->count, start, fill, perm_tmp, s);
     launch_sort_cells(perm_tmp, perm, start, P->ncell, s);
 }
 
@@ -636,10 +655,12 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
     if (P->any_zero) launch_force_sums(P->f, P->d_src_off, P->count, P->fsum, s);
     if (mixed)
         launch_combine_mixed(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->perm_t, P->u_s, P->u_c, P->u_near,
-                             (const float*)P->u_k, P->any_real, P->any_k, P->fsum, P->U, s);
+                             (const float*)P->u_k, P->any_real, P->any_k, P->fsum, P->d_tab, P->f, P->d_src_off, P->U,
+                             s);
     else
         launch_combine_fp64(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->perm_t, P->u_real,
-                            (const double*)P->u_k, P->any_real, P->any_k, P->fsum, P->U, s);
+                            (const double*)P->u_k, P->any_real, P->any_k, P->fsum, P->d_tab, P->f, P->d_src_off, P->U,
+                            s);
     record(P, 6, s);
 }
 
@@ -668,6 +689,28 @@ long long pb_plan_estimate_bytes(const pb_solve_params* p, int count)
     int rc = build_plan_host(p, count, &tmp);
     if (rc) return rc;
     return (long long)plan_layout(&tmp, false);
+}
+
+int pb_resolve(const pb_solve_params* p, pb_instance_info* info)
+{
+    if (!p || !info) return fail(PB_ERR_INVALID, "bad arguments");
+    Resolved R;
+    int rc = resolve(*p, R);
+    if (rc) return rc;
+    PbTables T;
+    if (build_tables(p->alpha, R.d, p->eps, R.rc, 1e-9, &T)) return fail(PB_ERR_INVALID, "table construction failed");
+    info->d = R.d;
+    info->rc = R.rc;
+    info->eta = R.eta;
+    info->m_std = R.m;
+    for (int a = 0; a < 3; a++) {
+        info->M[a] = R.M[a];
+        info->ncell[a] = R.nc[a];
+    }
+    info->P = R.P;
+    info->npoly = T.nd;
+    info->pairs_est = R.pairs_est;
+    return PB_OK;
 }
 
 int pb_plan_create(const pb_solve_params* p, int count, pb_plan* out)
@@ -735,27 +778,40 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
                     void* stream_v)
 {
     if (!P) return fail(PB_ERR_INVALID, "null plan");
-    if ((P->n_src > 0 && (!x || !f)) || (P->n_tgt > 0 && !U) || (!P->all_same && P->n_y > 0 && !y))
+    if ((P->act_src > 0 && (!x || !f)) || (P->act_tgt > 0 && !U) || (!P->all_same && P->act_y > 0 && !y))
         return fail(PB_ERR_INVALID, "null buffer");
     if (where != PB_HOST && where != PB_DEVICE) return fail(PB_ERR_INVALID, "bad memory location");
     cudaStream_t us = (cudaStream_t)stream_v;
     cudaStream_t s = P->stream;
     if (where == PB_HOST) {
-        for (size_t i = 0; i < 3 * (size_t)P->n_src; i++)
+        for (size_t i = 0; i < 3 * (size_t)P->act_src; i++)
             if (!std::isfinite(x[i]) || !std::isfinite(f[i])) return fail(PB_ERR_INVALID, "non-finite input");
         if (!P->all_same)
-            for (size_t i = 0; i < 3 * (size_t)P->n_y; i++)
+            for (size_t i = 0; i < 3 * (size_t)P->act_y; i++)
                 if (!std::isfinite(y[i])) return fail(PB_ERR_INVALID, "non-finite target");
     }
     PB_CK(cudaEventRecord(P->ev_in, us));
     PB_CK(cudaStreamWaitEvent(s, P->ev_in, 0));
-    cudaMemcpyKind kin = where == PB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-    if (P->n_src > 0) {
-        PB_CK(cudaMemcpyAsync(P->x, x, sizeof(double) * 3 * P->n_src, kin, s));
-        PB_CK(cudaMemcpyAsync(P->f, f, sizeof(double) * 3 * P->n_src, kin, s));
+    if (P->upload_pending) {
+        char* st = P->staging;
+        size_t oi = 0, ot = oi + sizeof(PbInst) * P->count, oo = ot + sizeof(PbTables) * P->count;
+        size_t ob = sizeof(int) * (P->count + 1);
+        PB_CK(cudaMemcpyAsync(P->d_inst, st + oi, sizeof(PbInst) * P->count, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_tab, st + ot, sizeof(PbTables) * P->count, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_src_off, st + oo, ob, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_tgt_off, st + oo + ob, ob, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_cell_off, st + oo + 2 * ob, ob, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_y_off, st + oo + 3 * ob, ob, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaEventRecord(P->ev_upload, s));
+        P->upload_pending = false;
     }
-    if (!P->all_same && P->n_y > 0) PB_CK(cudaMemcpyAsync(P->y, y, sizeof(double) * 3 * P->n_y, kin, s));
-    if (P->n_tgt > 0) {
+    cudaMemcpyKind kin = where == PB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if (P->act_src > 0) {
+        PB_CK(cudaMemcpyAsync(P->x, x, sizeof(double) * 3 * P->act_src, kin, s));
+        PB_CK(cudaMemcpyAsync(P->f, f, sizeof(double) * 3 * P->act_src, kin, s));
+    }
+    if (!P->all_same && P->act_y > 0) PB_CK(cudaMemcpyAsync(P->y, y, sizeof(double) * 3 * P->act_y, kin, s));
+    if (P->n_tgt > 0 && P->act_tgt > 0) {
         if (P->timing || P->exec_count < 1) {
             run_compute(P, s);
         } else {
@@ -782,7 +838,7 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
         }
         PB_CK(cudaGetLastError());
         cudaMemcpyKind kout = where == PB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-        PB_CK(cudaMemcpyAsync(U, P->U, sizeof(double) * 3 * P->n_tgt, kout, s));
+        PB_CK(cudaMemcpyAsync(U, P->U, sizeof(double) * 3 * P->act_tgt, kout, s));
     }
     P->exec_count++;
     PB_CK(cudaEventRecord(P->ev_out, s));

@@ -204,9 +204,11 @@ std::vector<double> fit_monomial(const std::function<double(double)>& f, double 
         v[k] = f(lo + (hi - lo) * (t + 1) / 2);
     }
     double cmax = 0;
+    std::vector<double> ct(2 * nodes * 2);
+    for (int q = 0; q < 4 * nodes; q++) ct[q] = std::cos(kPi * q / (2.0 * nodes));  // cos(pi q / (2 nodes))
     for (int j = 0; j < nodes; j++) {
         double s = 0;
-        for (int k = 0; k < nodes; k++) s += v[k] * std::cos(kPi * j * (k + 0.5) / nodes);
+        for (int k = 0; k < nodes; k++) s += v[k] * ct[(j * (2 * k + 1)) % (4 * nodes)];
         c[j] = s * 2.0 / nodes;
         cmax = std::max(cmax, std::fabs(c[j]));
     }
@@ -233,8 +235,9 @@ std::vector<double> fit_monomial(const std::function<double(double)>& f, double 
     return a;
 }
 
-int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t)
+int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t, int max_terms)
 {
+    if (max_terms <= 0 || max_terms > kMaxPoly) max_terms = kMaxPoly;
     if (!(a > 0) || !(d > 0) || !(rc > 0) || eps < 0) return -1;
     std::memset(t, 0, sizeof(PbTables));
     const int nser = 40;
@@ -243,8 +246,8 @@ int build_tables(double a, double d, double eps, double rc, double poly_tol, PbT
     const int nodes = 40;
     auto Td1 = [&](double r) { double x, y; scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &x, &y); return x; };
     auto Td2 = [&](double r) { double x, y; scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &x, &y); return y; };
-    std::vector<double> p1 = fit_monomial(Td1, 0, rc, nodes, poly_tol, kMaxPoly);
-    std::vector<double> p2 = fit_monomial(Td2, 0, rc, nodes, poly_tol, kMaxPoly);
+    std::vector<double> p1 = fit_monomial(Td1, 0, rc, nodes, poly_tol, max_terms);
+    std::vector<double> p2 = fit_monomial(Td2, 0, rc, nodes, poly_tol, max_terms);
     int nd = (int)std::max(p1.size(), p2.size());
     p1.resize(nd, 0.0);
     p2.resize(nd, 0.0);

@@ -42,7 +42,8 @@ std::vector<double> fit_monomial(const std::function<double(double)>& f, double 
                                  double rel_tol, int max_terms);
 
 // Fill the per-instance real-space tables.  poly_tol: relative truncation of
-// the Chebyshev series (1e-9 keeps ~20 terms).  Returns 0 or an error code.
-int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t);
+// the Chebyshev series (1e-9 keeps ~20 terms); max_terms caps the screened
+// polynomial (<= 0: kMaxPoly).  Returns 0 or an error code.
+int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t, int max_terms = 0);
 
 }  // namespace pb

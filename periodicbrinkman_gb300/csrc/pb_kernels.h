@@ -8,23 +8,27 @@
 namespace pb {
 
 // ---- binning and sorting (pb_sort.cu) ----
+// Every particle kernel is launched for a capacity `ncap` and reads the actual
+// count from device memory (offsets[ninst]), so one captured graph serves any
+// set of instances that fits the capacity.
 // cell_of[p] = global cell index of particle p (instance cell_off + local cell),
 // counts[cell] += 1.  pos: AoS doubles of all instances, offsets: ninst+1 prefix.
-void launch_bin(const double* pos, int ntot, const int* offsets, const PbInst* inst, int ninst,
+void launch_bin(const double* pos, int ncap, const int* offsets, const PbInst* inst, int ninst,
                 int* cell_of, int* counts, cudaStream_t s);
 // Exclusive scan of n ints into out (out has n+1 entries; out[n] = total).
 // tmp must hold scan_tmp_ints(n) ints.
 size_t scan_tmp_ints(int n);
 void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s);
 // perm[start[c] + k] = particle, fill must be zeroed.
-void launch_scatter(const int* cell_of, int ntot, const int* start, int* fill, int* perm, cudaStream_t s);
+void launch_scatter(const int* cell_of, int ncap, const int* ntot, const int* start, int* fill, int* perm,
+                    cudaStream_t s);
 // Sort each cell's perm entries ascending (deterministic order).
 void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell, cudaStream_t s);
 // Sorted particle records.  Mixed: pos_hi (x,y,z, w = instance bits), pos_lo, frc.
-void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ntot, const int* offsets,
+void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                           const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out,
                           cudaStream_t s);
-void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ntot, const int* offsets,
+void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                          const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, cudaStream_t s);
 // Work items: one per (target cell, chunk of <= 32 targets): int4 {inst, cell, first, count}.
 void launch_count_chunks(const int* start, int ncell_tot, int* chunks, cudaStream_t s);
@@ -45,10 +49,10 @@ void launch_real_fp64(const PbInst* inst, const PbTables* tab, const int4* items
 
 // ---- k space (pb_kspace.cu) ----
 template <class T>
-void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int ntot, const void* pos_a,
+void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int ncap, const void* pos_a,
                    const void* pos_b, const void* frc, T* grid, cudaStream_t s);
 template <class T>
-void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int ntot, const void* pos_a,
+void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const void* pos_a,
                    const void* pos_b, const T* grid, T* u_k, cudaStream_t s);
 // Batched 3D R2C -> Green multiply -> C2R over `nvol` volumes of equal size
 // (3 components per instance, instances contiguous).
@@ -60,16 +64,17 @@ void fill_twiddles(const int* M, bool fp64, void* host_buf);
 
 // Gather the packed target list: instance q's targets come from y (its own
 // targets) or from x (targets are its sources).
-void launch_pack_targets(const double* x, const double* y, int ntot, const int* tgt_off, const int* src_off,
+void launch_pack_targets(const double* x, const double* y, int ncap, const int* tgt_off, const int* src_off,
                          const int* y_off, int ninst, double* out, cudaStream_t s);
 
 // ---- final combine ----
-void launch_combine_mixed(const PbInst* inst, int ninst, const int* tgt_offsets, int ntot, const int* tperm,
+void launch_combine_mixed(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const int* tperm,
                           const float* u_s, const float* u_c, const double* u_near, const float* u_k, int use_real,
-                          int use_k, const double* fsum, double* U, cudaStream_t s);
-void launch_combine_fp64(const PbInst* inst, int ninst, const int* tgt_offsets, int ntot, const int* tperm,
+                          int use_k, const double* fsum, const PbTables* tab, const double* frc,
+                          const int* src_offsets, double* U, cudaStream_t s);
+void launch_combine_fp64(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const int* tperm,
                          const double* u_real, const double* u_k, int use_real, int use_k, const double* fsum,
-                         double* U, cudaStream_t s);
+                         const PbTables* tab, const double* frc, const int* src_offsets, double* U, cudaStream_t s);
 // Per-instance force sums (for the optional k = 0 mode): out[3*q + c] = sum f.
 void launch_force_sums(const double* frc, const int* offsets, int ninst, double* out, cudaStream_t s);
 

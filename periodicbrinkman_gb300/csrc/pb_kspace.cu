@@ -97,9 +97,10 @@ __device__ __forceinline__ void window(const PbInst& I, const double* x, int lan
 
 template <class T, class PV, class FV>
 __global__ void __launch_bounds__(kSpreadWarps * 32)
-    k_spread(const PbInst* __restrict__ inst, int ntot, const PV* __restrict__ pa, const PV* __restrict__ pb,
-             const FV* __restrict__ frc, T* __restrict__ grid)
+    k_spread(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const PV* __restrict__ pa,
+             const PV* __restrict__ pb, const FV* __restrict__ frc, T* __restrict__ grid)
 {
+    const int ntot = *ntot_p;
     __shared__ T wgt[kSpreadWarps][3][kMaxP];
     __shared__ int gidx[kSpreadWarps][3][kMaxP];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -128,9 +129,10 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
 
 template <class T, class PV>
 __global__ void __launch_bounds__(kSpreadWarps * 32)
-    k_gather(const PbInst* __restrict__ inst, int ntot, const PV* __restrict__ pa, const PV* __restrict__ pb,
-             const T* __restrict__ grid, T* __restrict__ u_k)
+    k_gather(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const PV* __restrict__ pa,
+             const PV* __restrict__ pb, const T* __restrict__ grid, T* __restrict__ u_k)
 {
+    const int ntot = *ntot_p;
     __shared__ T wgt[kSpreadWarps][3][kMaxP];
     __shared__ int gidx[kSpreadWarps][3][kMaxP];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -181,11 +183,12 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
 }
 
 template <class T>
-void launch_spread(const PbInst* inst, int /*ninst*/, const int* /*src_offsets*/, int ntot, const void* pos_a,
+void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int ncap, const void* pos_a,
                    const void* pos_b, const void* frc, T* grid, cudaStream_t s)
 {
-    if (ntot <= 0) return;
-    int blocks = (ntot + kSpreadWarps - 1) / kSpreadWarps;
+    if (ncap <= 0) return;
+    int blocks = (ncap + kSpreadWarps - 1) / kSpreadWarps;
+    const int* ntot = src_offsets + ninst;
     if (sizeof(T) == 4)
         k_spread<T, float4, float4><<<blocks, kSpreadWarps * 32, 0, s>>>(
             inst, ntot, (const float4*)pos_a, (const float4*)pos_b, (const float4*)frc, grid);
@@ -195,11 +198,12 @@ void launch_spread(const PbInst* inst, int /*ninst*/, const int* /*src_offsets*/
 }
 
 template <class T>
-void launch_gather(const PbInst* inst, int /*ninst*/, const int* /*tgt_offsets*/, int ntot, const void* pos_a,
+void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const void* pos_a,
                    const void* pos_b, const T* grid, T* u_k, cudaStream_t s)
 {
-    if (ntot <= 0) return;
-    int blocks = (ntot + kSpreadWarps - 1) / kSpreadWarps;
+    if (ncap <= 0) return;
+    int blocks = (ncap + kSpreadWarps - 1) / kSpreadWarps;
+    const int* ntot = tgt_offsets + ninst;
     if (sizeof(T) == 4)
         k_gather<T, float4><<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const float4*)pos_a,
                                                                    (const float4*)pos_b, grid, u_k);
@@ -543,64 +547,75 @@ template void launch_kspace_fft<double>(const PbInst*, const int*, int, long lon
 // Final FP64 combine and force sums
 // ---------------------------------------------------------------------------
 __global__ void k_combine_mixed(const PbInst* __restrict__ inst, int ninst, const int* __restrict__ tgt_offsets,
-                                int ntot, const int* __restrict__ tperm, const float* __restrict__ u_s,
+                                const int* __restrict__ tperm, const float* __restrict__ u_s,
                                 const float* __restrict__ u_c, const double* __restrict__ u_near,
                                 const float* __restrict__ u_k, int use_real, int use_k, const double* __restrict__ fsum,
-                                double* __restrict__ U)
+                                const PbTables* __restrict__ tab, const double* __restrict__ frc,
+                                const int* __restrict__ src_offsets, double* __restrict__ U)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntot) return;
+    if (t >= tgt_offsets[ninst]) return;
     int p = tperm[t];
     int q = find_instance(tgt_offsets, ninst, p);
     const PbInst& I = inst[q];
     double tau = I.L[0] * I.L[1] * I.L[2];
+    // self pair (targets are the sources): (R_eps(0) - R_d(0)) f_i in FP64
+    const bool self = use_real && I.same && (I.flags & 1);
+    const size_t ps = (size_t)(p - tgt_offsets[q] + src_offsets[q]);
     for (int c = 0; c < 3; c++) {
         double v = 0;
         size_t o = 3 * (size_t)t + c;
-        if (use_real) v += ((double)u_s[o] - (double)u_c[o]) + u_near[o];
-        if (use_k) v += (double)u_k[o];
+        if (self) v += tab[q].self1 * frc[3 * ps + c];
+        if (use_real && (I.flags & 1)) v += ((double)u_s[o] - (double)u_c[o]) + u_near[o];
+        if (use_k && (I.flags & 2)) v += (double)u_k[o];
         if (I.flags & 4) v += fsum[3 * q + c] / (I.alpha * I.alpha * tau);
         U[3 * (size_t)p + c] = v;
     }
 }
 
 __global__ void k_combine_fp64(const PbInst* __restrict__ inst, int ninst, const int* __restrict__ tgt_offsets,
-                               int ntot, const int* __restrict__ tperm, const double* __restrict__ u_real,
+                               const int* __restrict__ tperm, const double* __restrict__ u_real,
                                const double* __restrict__ u_k, int use_real, int use_k,
-                               const double* __restrict__ fsum, double* __restrict__ U)
+                               const double* __restrict__ fsum, const PbTables* __restrict__ tab,
+                               const double* __restrict__ frc, const int* __restrict__ src_offsets,
+                               double* __restrict__ U)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntot) return;
+    if (t >= tgt_offsets[ninst]) return;
     int p = tperm[t];
     int q = find_instance(tgt_offsets, ninst, p);
     const PbInst& I = inst[q];
     double tau = I.L[0] * I.L[1] * I.L[2];
+    const bool self = use_real && I.same && (I.flags & 1);
+    const size_t ps = (size_t)(p - tgt_offsets[q] + src_offsets[q]);
     for (int c = 0; c < 3; c++) {
         double v = 0;
         size_t o = 3 * (size_t)t + c;
-        if (use_real) v += u_real[o];
-        if (use_k) v += u_k[o];
+        if (self) v += tab[q].self1 * frc[3 * ps + c];
+        if (use_real && (I.flags & 1)) v += u_real[o];
+        if (use_k && (I.flags & 2)) v += u_k[o];
         if (I.flags & 4) v += fsum[3 * q + c] / (I.alpha * I.alpha * tau);
         U[3 * (size_t)p + c] = v;
     }
 }
 
-void launch_combine_mixed(const PbInst* inst, int ninst, const int* tgt_offsets, int ntot, const int* tperm,
+void launch_combine_mixed(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const int* tperm,
                           const float* u_s, const float* u_c, const double* u_near, const float* u_k, int use_real,
-                          int use_k, const double* fsum, double* U, cudaStream_t s)
+                          int use_k, const double* fsum, const PbTables* tab, const double* frc,
+                          const int* src_offsets, double* U, cudaStream_t s)
 {
-    if (ntot <= 0) return;
-    k_combine_mixed<<<(ntot + 255) / 256, 256, 0, s>>>(inst, ninst, tgt_offsets, ntot, tperm, u_s, u_c, u_near, u_k,
-                                                        use_real, use_k, fsum, U);
+    if (ncap <= 0) return;
+    k_combine_mixed<<<(ncap + 255) / 256, 256, 0, s>>>(inst, ninst, tgt_offsets, tperm, u_s, u_c, u_near, u_k,
+                                                        use_real, use_k, fsum, tab, frc, src_offsets, U);
 }
 
-void launch_combine_fp64(const PbInst* inst, int ninst, const int* tgt_offsets, int ntot, const int* tperm,
-                         const double* u_real, const double* u_k, int use_real, int use_k, const double* fsum, double* U,
-                         cudaStream_t s)
+void launch_combine_fp64(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const int* tperm,
+                         const double* u_real, const double* u_k, int use_real, int use_k, const double* fsum,
+                         const PbTables* tab, const double* frc, const int* src_offsets, double* U, cudaStream_t s)
 {
-    if (ntot <= 0) return;
-    k_combine_fp64<<<(ntot + 255) / 256, 256, 0, s>>>(inst, ninst, tgt_offsets, ntot, tperm, u_real, u_k, use_real,
-                                                       use_k, fsum, U);
+    if (ncap <= 0) return;
+    k_combine_fp64<<<(ncap + 255) / 256, 256, 0, s>>>(inst, ninst, tgt_offsets, tperm, u_real, u_k, use_real,
+                                                       use_k, fsum, tab, frc, src_offsets, U);
 }
 
 __global__ void k_force_sums(const double* __restrict__ frc, const int* __restrict__ offsets, int ninst,

@@ -11,8 +11,9 @@
 // in the frame of the target cell (error-free TwoSum), so displacements carry
 // FP32 relative accuracy even at r << cell size; the pair kernel is the FP32
 // polynomial T(r) of the instance tables (FMA only); per-chunk partial sums are
-// Kahan-accumulated; pairs below r_tiny (including the self pair) use the FP64
-// series and an FP64 accumulator.
+// Kahan-accumulated; pairs below r_tiny use the FP64 series and an FP64
+// accumulator.  The self pair of targets that are the sources is skipped here
+// and added in FP64 by the combine kernel (R_eps(0) - R_d(0)) f_i.
 //
 // FP64 (k_real_fp64): the reference's closed forms (cuda/periodicBrinkman.h:85-176)
 // in double precision, FP64 series below r_tiny.
@@ -104,6 +105,8 @@ __global__ void __launch_bounds__(kRealWarps * 32)
         item_frame(I, it, F);
         const bool active = lane < it.w;
         const int tidx = it.z + (active ? lane : 0);
+        // sorted index of this target among the sources when targets are the sources
+        const int self_src = I.same ? tidx - I.tgt_off + I.src_off : -1;
         // target in the cell frame, hi + lo
         float th[3], tl[3];
         {
@@ -139,6 +142,7 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                     double sh2 = (double)((g2 - w2) / I.nc[2]) * I.L[2];
                     int b = src_start[row + w2], e = src_start[row + w2 + run];
                     g2 += run;
+                    const bool zero_shift = (sh0 == 0.0) && (sh1 == 0.0) && (sh2 == 0.0);
                     float qh[3], ql[3];
                     split_double(F.O[0] - sh0, qh[0], ql[0]);
                     split_double(F.O[1] - sh1, qh[1], ql[1]);
@@ -170,6 +174,10 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                 float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                                 mask |= (r2 < rc2 ? 1u : 0u) << jj;
                             }
+                            // the self pair (targets are the sources, same particle, no shift)
+                            // is added in FP64 by the combine kernel
+                            if (self_src >= base && self_src < base + ncand && zero_shift)
+                                mask &= ~(1u << (self_src - base));
                         }
                         float a0 = 0, a1 = 0, a2 = 0;
                         while (__any_sync(kFull, mask)) {
@@ -292,6 +300,7 @@ __global__ void __launch_bounds__(kRealWarps * 32)
         item_frame(I, it, F);
         const bool active = lane < it.w;
         const int tidx = it.z + (active ? lane : 0);
+        const int self_src = I.same ? tidx - I.tgt_off + I.src_off : -1;
         Dbl4 tp = tpos[tidx];
         double v0 = 0, v1 = 0, v2 = 0;
         for (int o0 = -I.S[0]; o0 <= I.S[0]; o0++) {
@@ -311,6 +320,7 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                     double sh2 = (double)((g2 - w2) / I.nc[2]) * I.L[2];
                     int b = src_start[row + w2], e = src_start[row + w2 + run];
                     g2 += run;
+                    const bool zero_shift = (sh0 == 0.0) && (sh1 == 0.0) && (sh2 == 0.0);
                     for (int base = b; base < e; base += 32) {
                         int j = base + lane;
                         if (j < e) {
@@ -328,6 +338,8 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                 double r2 = dx * dx + dy * dy + dz * dz;
                                 mask |= (r2 < rc2 ? 1u : 0u) << jj;
                             }
+                            if (self_src >= base && self_src < base + ncand && zero_shift)
+                                mask &= ~(1u << (self_src - base));
                         }
                         while (__any_sync(kFull, mask)) {
                             if (mask) {

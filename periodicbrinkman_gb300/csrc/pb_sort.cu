@@ -5,11 +5,11 @@
 
 namespace pb {
 
-__global__ void k_bin(const double* __restrict__ pos, int ntot, const int* __restrict__ offsets,
+__global__ void k_bin(const double* __restrict__ pos, const int* __restrict__ offsets,
                       const PbInst* __restrict__ inst, int ninst, int* __restrict__ cell_of, int* __restrict__ counts)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= ntot) return;
+    if (p >= offsets[ninst]) return;
     int q = find_instance(offsets, ninst, p);
     const PbInst& I = inst[q];
     int c[3];
@@ -24,11 +24,11 @@ __global__ void k_bin(const double* __restrict__ pos, int ntot, const int* __res
     atomicAdd(&counts[g], 1);
 }
 
-void launch_bin(const double* pos, int ntot, const int* offsets, const PbInst* inst, int ninst, int* cell_of,
+void launch_bin(const double* pos, int ncap, const int* offsets, const PbInst* inst, int ninst, int* cell_of,
                 int* counts, cudaStream_t s)
 {
-    if (ntot <= 0) return;
-    k_bin<<<(ntot + 255) / 256, 256, 0, s>>>(pos, ntot, offsets, inst, ninst, cell_of, counts);
+    if (ncap <= 0) return;
+    k_bin<<<(ncap + 255) / 256, 256, 0, s>>>(pos, offsets, inst, ninst, cell_of, counts);
 }
 
 // ---- exclusive scan (reduce-then-scan, recursive over block sums) ----
@@ -115,20 +115,21 @@ void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_
     k_set_total<<<1, 1, 0, s>>>(out, n, in);
 }
 
-__global__ void k_scatter(const int* __restrict__ cell_of, int ntot, const int* __restrict__ start,
+__global__ void k_scatter(const int* __restrict__ cell_of, const int* __restrict__ ntot, const int* __restrict__ start,
                           int* __restrict__ fill, int* __restrict__ perm)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= ntot) return;
+    if (p >= *ntot) return;
     int c = cell_of[p];
     int slot = start[c] + atomicAdd(&fill[c], 1);
     perm[slot] = p;
 }
 
-void launch_scatter(const int* cell_of, int ntot, const int* start, int* fill, int* perm, cudaStream_t s)
+void launch_scatter(const int* cell_of, int ncap, const int* ntot, const int* start, int* fill, int* perm,
+                    cudaStream_t s)
 {
-    if (ntot <= 0) return;
-    k_scatter<<<(ntot + 255) / 256, 256, 0, s>>>(cell_of, ntot, start, fill, perm);
+    if (ncap <= 0) return;
+    k_scatter<<<(ncap + 255) / 256, 256, 0, s>>>(cell_of, ntot, start, fill, perm);
 }
 
 // Rank sort of each cell's entries (warp per cell): entry v goes to slot
@@ -164,12 +165,12 @@ void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell, cu
 }
 
 __global__ void k_prepare_mixed(const double* __restrict__ pos, const double* __restrict__ frc,
-                                const int* __restrict__ perm, int ntot, const int* __restrict__ offsets,
+                                const int* __restrict__ perm, const int* __restrict__ offsets,
                                 const PbInst* __restrict__ inst, int ninst, float4* __restrict__ pos_hi,
                                 float4* __restrict__ pos_lo, float4* __restrict__ frc_out)
 {
     int sidx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sidx >= ntot) return;
+    if (sidx >= offsets[ninst]) return;
     int p = perm[sidx];
     int q = find_instance(offsets, ninst, p);
     const PbInst& I = inst[q];
@@ -183,22 +184,22 @@ __global__ void k_prepare_mixed(const double* __restrict__ pos, const double* __
                                     (float)frc[3 * (size_t)p + 2], 0.f);
 }
 
-void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ntot, const int* offsets,
+void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                           const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out,
                           cudaStream_t s)
 {
-    if (ntot <= 0) return;
-    k_prepare_mixed<<<(ntot + 255) / 256, 256, 0, s>>>(pos, frc, perm, ntot, offsets, inst, ninst, pos_hi, pos_lo,
+    if (ncap <= 0) return;
+    k_prepare_mixed<<<(ncap + 255) / 256, 256, 0, s>>>(pos, frc, perm, offsets, inst, ninst, pos_hi, pos_lo,
                                                         frc_out);
 }
 
 __global__ void k_prepare_fp64(const double* __restrict__ pos, const double* __restrict__ frc,
-                               const int* __restrict__ perm, int ntot, const int* __restrict__ offsets,
+                               const int* __restrict__ perm, const int* __restrict__ offsets,
                                const PbInst* __restrict__ inst, int ninst, Dbl4* __restrict__ pos_out,
                                Dbl4* __restrict__ frc_out)
 {
     int sidx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sidx >= ntot) return;
+    if (sidx >= offsets[ninst]) return;
     int p = perm[sidx];
     int q = find_instance(offsets, ninst, p);
     const PbInst& I = inst[q];
@@ -209,12 +210,11 @@ __global__ void k_prepare_fp64(const double* __restrict__ pos, const double* __r
     if (frc) frc_out[sidx] = make_dbl4(frc[3 * (size_t)p], frc[3 * (size_t)p + 1], frc[3 * (size_t)p + 2], 0.0);
 }
 
-void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ntot, const int* offsets,
+void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                          const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, cudaStream_t s)
 {
-    if (ntot <= 0) return;
-    k_prepare_fp64<<<(ntot + 255) / 256, 256, 0, s>>>(pos, frc, perm, ntot, offsets, inst, ninst, pos_out,
-                                                       frc_out);
+    if (ncap <= 0) return;
+    k_prepare_fp64<<<(ncap + 255) / 256, 256, 0, s>>>(pos, frc, perm, offsets, inst, ninst, pos_out, frc_out);
 }
 
 __global__ void k_count_chunks(const int* __restrict__ start, int ncell, int* __restrict__ chunks)
@@ -257,12 +257,12 @@ void launch_emit_items(const int* start, const int* chunk_start, int ncell_tot, 
 
 namespace pb {
 
-__global__ void k_pack_targets(const double* __restrict__ x, const double* __restrict__ y, int ntot,
+__global__ void k_pack_targets(const double* __restrict__ x, const double* __restrict__ y,
                                const int* __restrict__ tgt_off, const int* __restrict__ src_off,
                                const int* __restrict__ y_off, int ninst, double* __restrict__ out)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= ntot) return;
+    if (p >= tgt_off[ninst]) return;
     int q = find_instance(tgt_off, ninst, p);
     int local = p - tgt_off[q];
     const double* src = (y_off[q] >= 0) ? (y + 3 * (size_t)(y_off[q] + local)) : (x + 3 * (size_t)(src_off[q] + local));
@@ -271,11 +271,11 @@ __global__ void k_pack_targets(const double* __restrict__ x, const double* __res
     out[3 * (size_t)p + 2] = src[2];
 }
 
-void launch_pack_targets(const double* x, const double* y, int ntot, const int* tgt_off, const int* src_off,
+void launch_pack_targets(const double* x, const double* y, int ncap, const int* tgt_off, const int* src_off,
                          const int* y_off, int ninst, double* out, cudaStream_t s)
 {
-    if (ntot <= 0) return;
-    k_pack_targets<<<(ntot + 255) / 256, 256, 0, s>>>(x, y, ntot, tgt_off, src_off, y_off, ninst, out);
+    if (ncap <= 0) return;
+    k_pack_targets<<<(ncap + 255) / 256, 256, 0, s>>>(x, y, tgt_off, src_off, y_off, ninst, out);
 }
 
 }  // namespace pb
