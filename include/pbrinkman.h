@@ -38,8 +38,9 @@ extern "C" {
 #define PB_FLAGS_DEFAULT (PB_REAL_SPACE | PB_KSPACE)
 
 /* memory location of user buffers */
-#define PB_HOST 0
-#define PB_DEVICE 1
+#define PB_HOST 0        /* host memory; the call returns when U is written */
+#define PB_DEVICE 1      /* device memory; ordered on the given stream */
+#define PB_HOST_PINNED 2 /* page-locked host memory; ordered on the given stream, no wait */
 
 /* One solve: velocities at n_tgt targets induced by n_src point forces in the
  * periodic box L with Brinkman alpha (inverse permeability length) and blob
@@ -70,6 +71,17 @@ typedef struct pb_instance_info {
     int npoly;            /* polynomial terms of the FP32 pair kernel */
     long long pairs_est;  /* estimated real-space pairs inside rc */
 } pb_instance_info;
+
+/* Capacity of a serving slot: a plan whose instances are bound per use. */
+typedef struct pb_slot_config {
+    int M[3];          /* FFT grid of every instance bound to the slot */
+    int max_instances; /* instances per execution */
+    int max_src;       /* total sources over the bound instances */
+    int max_tgt;       /* total targets (an instance whose targets are its sources counts n_src) */
+    int max_cells;     /* total real-space cells over the bound instances */
+    int precision;     /* PB_PREC_FP64 or PB_PREC_MIXED */
+    int npoly;         /* polynomial terms of the FP32 pair kernel (16..28; 0 = 24) */
+} pb_slot_config;
 
 typedef struct pb_plan_s* pb_plan;
 
@@ -125,6 +137,15 @@ int pb_plan_create(const pb_solve_params* p, int count, pb_plan* out);
 int pb_plan_execute(pb_plan plan, const double* x, const double* f, const double* y, double* U, int where,
                     void* stream);
 int pb_plan_instance_info(pb_plan plan, int i, pb_instance_info* info);
+/* A capacity plan (serving slot) with no instances bound yet. */
+int pb_plan_create_slot(const pb_slot_config* cfg, pb_plan* out);
+long long pb_slot_estimate_bytes(const pb_slot_config* cfg);
+/* Bind `count` instances (<= the plan's instances) to the plan; the next
+ * pb_plan_execute solves them (packed inputs in this order).  Each instance
+ * keeps the grid of its position; the autotuner picks d and rc for it.  The
+ * captured CUDA graph is reused: kernels read the bound sizes from device
+ * memory.  PB_ERR_BUDGET if the totals exceed the capacity. */
+int pb_plan_bind(pb_plan plan, const pb_solve_params* p, int count);
 /* The autotuner's choice for one parameter block, on the host (no GPU). */
 int pb_resolve(const pb_solve_params* p, pb_instance_info* info);
 /* Device bytes held by the plan. */
@@ -140,6 +161,47 @@ long long pb_plan_estimate_bytes(const pb_solve_params* p, int count);
 int pb_plan_set_timing(pb_plan plan, int enable);
 int pb_plan_stage_ms(pb_plan plan, double* ms6);
 int pb_plan_destroy(pb_plan plan);
+
+/* ---- continuous-batching server ------------------------------------------- */
+
+typedef struct pb_server_config {
+    long long budget_bytes; /* device memory for resident slots (0: 150 GiB) */
+    int precision;          /* PB_PREC_MIXED or PB_PREC_FP64 */
+    int max_batch;          /* instances per slot execution (0: 16) */
+    int slots_per_grid;     /* concurrent slots per grid size (0: 2) */
+    int n_grids;            /* grid sizes provisioned (0: 8, 16, ..., 256) */
+    int grids[8];
+    int max_src;            /* source capacity of a slot = largest request (0: 262144) */
+    int max_tgt;            /* target capacity of a slot (0: max_src) */
+    int queue_capacity;     /* pending requests before PB_ERR_BUSY (0: unbounded) */
+} pb_server_config;
+
+typedef struct pb_server_counters {
+    long long submitted, completed, failed, rejected, batches;
+    double mean_batch;      /* instances per slot execution */
+    long long device_bytes; /* held by the slots */
+    int slots;
+} pb_server_counters;
+
+typedef struct pb_server_s* pb_server;
+
+/* Creates the resident slots within the budget and starts the scheduler. */
+int pb_server_create(const pb_server_config* cfg, pb_server* out);
+/* Queue one solve (HOST buffers the caller keeps alive until it completes;
+ * U receives 3 x n_tgt, or 3 x n_src when n_tgt = 0).  The request is
+ * autotuned here and assigned to the smallest provisioned grid that holds
+ * its k-space resolution.  PB_ERR_BUDGET: no slot can hold it. */
+int pb_server_submit(pb_server s, const pb_solve_params* p, const double* x, const double* f, const double* y,
+                     double* U, long long* ticket);
+/* state: 0 queued, 1 on the GPU, 2 done (then status and latency are set). */
+int pb_server_poll(pb_server s, long long ticket, int* state, int* status, double* latency_s);
+int pb_server_wait(pb_server s, long long ticket, double timeout_s, int* status, double* latency_s);
+/* Forget a finished request. */
+int pb_server_release(pb_server s, long long ticket);
+/* Wait until every submitted request has finished. */
+int pb_server_drain(pb_server s, double timeout_s);
+int pb_server_stats(pb_server s, pb_server_counters* out);
+int pb_server_destroy(pb_server s);
 
 /* ---- misc ----------------------------------------------------------------- */
 const char* pb_last_error(void);

@@ -25,6 +25,7 @@ PB_ZERO_MODE = 4
 PB_FLAGS_DEFAULT = PB_REAL_SPACE | PB_KSPACE
 PB_HOST = 0
 PB_DEVICE = 1
+PB_HOST_PINNED = 2
 
 _ERRNAMES = {
     PB_ERR_INVALID: "PB_ERR_INVALID",
@@ -71,6 +72,45 @@ class InstanceInfo(C.Structure):
         ("ncell", C.c_int * 3),
         ("npoly", C.c_int),
         ("pairs_est", C.c_longlong),
+    ]
+
+
+class SlotConfig(C.Structure):
+    _fields_ = [
+        ("M", C.c_int * 3),
+        ("max_instances", C.c_int),
+        ("max_src", C.c_int),
+        ("max_tgt", C.c_int),
+        ("max_cells", C.c_int),
+        ("precision", C.c_int),
+        ("npoly", C.c_int),
+    ]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [
+        ("budget_bytes", C.c_longlong),
+        ("precision", C.c_int),
+        ("max_batch", C.c_int),
+        ("slots_per_grid", C.c_int),
+        ("n_grids", C.c_int),
+        ("grids", C.c_int * 8),
+        ("max_src", C.c_int),
+        ("max_tgt", C.c_int),
+        ("queue_capacity", C.c_int),
+    ]
+
+
+class ServerCounters(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_longlong),
+        ("completed", C.c_longlong),
+        ("failed", C.c_longlong),
+        ("rejected", C.c_longlong),
+        ("batches", C.c_longlong),
+        ("mean_batch", C.c_double),
+        ("device_bytes", C.c_longlong),
+        ("slots", C.c_int),
     ]
 
 
@@ -123,6 +163,18 @@ def lib():
     L.pb_plan_stage_ms.argtypes = [vp, dp]
     L.pb_plan_destroy.argtypes = [vp]
     L.pb_debug_pair_kernel.argtypes = [C.c_double] * 4 + [C.c_int, dp, dp, dp]
+    L.pb_plan_create_slot.argtypes = [C.POINTER(SlotConfig), C.POINTER(vp)]
+    L.pb_slot_estimate_bytes.restype = C.c_longlong
+    L.pb_slot_estimate_bytes.argtypes = [C.POINTER(SlotConfig)]
+    L.pb_plan_bind.argtypes = [vp, C.POINTER(SolveParams), C.c_int]
+    L.pb_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(vp)]
+    L.pb_server_submit.argtypes = [vp, C.POINTER(SolveParams), vp, vp, vp, vp, C.POINTER(C.c_longlong)]
+    L.pb_server_poll.argtypes = [vp, C.c_longlong, ip, ip, dp]
+    L.pb_server_wait.argtypes = [vp, C.c_longlong, C.c_double, ip, dp]
+    L.pb_server_release.argtypes = [vp, C.c_longlong]
+    L.pb_server_drain.argtypes = [vp, C.c_double]
+    L.pb_server_stats.argtypes = [vp, C.POINTER(ServerCounters)]
+    L.pb_server_destroy.argtypes = [vp]
     _lib = L
     return L
 

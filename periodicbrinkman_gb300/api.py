@@ -16,6 +16,9 @@ from ._lib import (
     PB_PREC_FP64,
     PB_PREC_MIXED,
     InstanceInfo,
+    ServerConfig,
+    ServerCounters,
+    SlotConfig,
     SolveParams,
     check,
     lib,
@@ -144,6 +147,112 @@ class Plan:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def make_slot(M: int, max_instances: int, max_src: int, max_tgt: int, max_cells: int = 1 << 20,
+              precision: str | int = "mixed", npoly: int = 24) -> "Plan":
+    """A capacity plan (serving slot) for instances on an M^3 grid."""
+    c = SlotConfig()
+    for a in range(3):
+        c.M[a] = int(M)
+    c.max_instances, c.max_src, c.max_tgt, c.max_cells = int(max_instances), int(max_src), int(max_tgt), int(max_cells)
+    c.precision = {"mixed": PB_PREC_MIXED, "fp64": PB_PREC_FP64}.get(precision, precision)
+    c.npoly = int(npoly)
+    h = C.c_void_p()
+    check(lib().pb_plan_create_slot(C.byref(c), C.byref(h)))
+    plan = Plan.__new__(Plan)
+    plan._h = h
+    plan.params = []
+    plan.n_src = plan.n_tgt = plan.n_y = 0
+    return plan
+
+
+def bind(plan: "Plan", params) -> None:
+    """Bind instances to a plan (see pb_plan_bind); sets the packed sizes."""
+    params = list(params)
+    arr = (SolveParams * max(len(params), 1))(*params)
+    check(lib().pb_plan_bind(plan._h, arr, len(params)))
+    plan.params = params
+    plan.n_src = sum(p.n_src for p in params)
+    plan.n_tgt = sum(p.n_tgt if p.n_tgt > 0 else p.n_src for p in params)
+    plan.n_y = sum(p.n_tgt for p in params)
+
+
+class Server:
+    """Continuous-batching server (pb_server_*): submit host requests, wait."""
+
+    def __init__(self, precision: str | int = "mixed", budget_bytes: int = 150 << 30, max_batch: int = 16,
+                 slots_per_grid: int = 2, grids=(8, 16, 32, 64, 128, 256), max_src: int = 1 << 18,
+                 max_tgt: int = 0, queue_capacity: int = 0):
+        c = ServerConfig()
+        c.budget_bytes = int(budget_bytes)
+        c.precision = {"mixed": PB_PREC_MIXED, "fp64": PB_PREC_FP64}.get(precision, precision)
+        c.max_batch = int(max_batch)
+        c.slots_per_grid = int(slots_per_grid)
+        c.n_grids = len(grids)
+        for i, g in enumerate(grids):
+            c.grids[i] = int(g)
+        c.max_src = int(max_src)
+        c.max_tgt = int(max_tgt)
+        c.queue_capacity = int(queue_capacity)
+        self.precision = c.precision
+        h = C.c_void_p()
+        check(lib().pb_server_create(C.byref(c), C.byref(h)))
+        self._h = h
+        self._live = {}
+
+    def submit(self, x, f, L, alpha, eps, y=None, **kw) -> int:
+        """Queue one solve; returns a ticket.  Buffers are kept until done."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        y = None if y is None else np.ascontiguousarray(y, dtype=np.float64)
+        m = 0 if y is None else y.shape[0]
+        p = make_params(x.shape[0], L, alpha, eps, n_tgt=m, precision=self.precision, **kw)
+        U = np.empty((m if m else x.shape[0], 3))
+        t = C.c_longlong()
+        check(lib().pb_server_submit(self._h, C.byref(p), x.ctypes.data, f.ctypes.data,
+                                     None if y is None else y.ctypes.data, U.ctypes.data, C.byref(t)))
+        self._live[t.value] = (x, f, y, U)
+        return t.value
+
+    def poll(self, ticket: int):
+        st, status, lat = C.c_int(), C.c_int(), C.c_double()
+        check(lib().pb_server_poll(self._h, ticket, C.byref(st), C.byref(status), C.byref(lat)))
+        return st.value, status.value, lat.value
+
+    def result(self, ticket: int, timeout: float = 60.0):
+        """Wait for a request; returns (U, latency_s) and forgets it."""
+        status, lat = C.c_int(), C.c_double()
+        check(lib().pb_server_wait(self._h, ticket, float(timeout), C.byref(status), C.byref(lat)))
+        check(status.value)
+        U = self._live.pop(ticket)[3]
+        lib().pb_server_release(self._h, ticket)
+        return U, lat.value
+
+    def drain(self, timeout: float = 600.0) -> None:
+        check(lib().pb_server_drain(self._h, float(timeout)))
+
+    def stats(self) -> dict:
+        c = ServerCounters()
+        check(lib().pb_server_stats(self._h, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in c._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().pb_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def resolve(params: SolveParams) -> dict:

@@ -52,6 +52,7 @@ struct Resolved {
     double d, rc, eta, m, tol;
     int M[3];
     int P;
+    int Pa[3];
     int nc[3], S[3];
     double h[3];
     int n_src, n_tgt;  // n_tgt: effective targets (n_src when targets are the sources)
@@ -93,18 +94,21 @@ int validate(const pb_solve_params& p)
 }
 
 // Choose the grid for splitting width d (tuning fields the user left at 0).
-void grid_for(const pb_solve_params& p, double d, double m, int P, double kconst, int* M)
+// s = eta / h^2 is the Gaussian width in grid units (fixed by the support).
+void grid_for(const pb_solve_params& p, double d, double s, double kconst, int* M)
 {
     for (int a = 0; a < 3; a++) {
         if (p.M[a] > 0) {
             M[a] = p.M[a];
             continue;
         }
-        // k-space truncation exp(-kmax^2 d^2/4) <= tol with kmax = 2 pi (M/2 - 1)/L,
-        // and Gaussian deconvolution eta < d^2/2  <=>  P L/(M m) < d.
+        // k-space truncation exp(-kmax^2 d^2/4) <= tol with kmax = 2 pi (M/2 - 1)/L
+        // (Nyquist planes are zeroed), and Gaussian deconvolution: the spreading
+        // width eta = s h^2 must stay below d^2/2 (with margin) so that
+        // exp(-k^2 (d^2/4 - eta/2)) still decays.
         double nk = 2.0 * std::sqrt(kconst) / d * p.L[a] / (2 * M_PI) + 1.0;
         double mk = 2.0 * nk + 2.0;
-        double md = 1.15 * P * p.L[a] / (m * d);
+        double md = p.L[a] * std::sqrt(2.6 * s) / d;
         M[a] = pow2ceil((int)std::ceil(std::max(mk, md)));
     }
 }
@@ -119,16 +123,28 @@ int resolve(const pb_solve_params& p, Resolved& R)
     R.n_src = p.n_src;
     R.same = (p.n_tgt == 0);
     R.n_tgt = R.same ? p.n_src : p.n_tgt;
-    const double kconst = std::log(10.0 / tol);
+    const double kconst = std::log(10.0 / tol);      // k-space truncation exponent
+    const double ksup = std::log(1.0 / tol) + 1.0;   // Gaussian truncation and aliasing exponent
     const double zeta = std::sqrt(std::log(1.0 / tol)) + 0.35;
-    R.m = p.m_std > 0 ? p.m_std : std::sqrt(2.0 * kconst);
+    // Gaussian support: a window of P points reaches (P/2 - 1) h from the
+    // particle on the near side; with eta = s h^2 the truncation error is
+    // exp(-(P/2-1)^2 / s) and the grid aliasing error exp(-pi^2 s).  Given P,
+    // s = (P/2 - 1)/pi balances both at exp(-pi (P/2 - 1)); given the
+    // reference's m (support half-width in standard deviations), s = P^2/(2 m^2).
     int P = p.P;
     if (P == 0) {
-        P = (int)std::ceil(R.m * std::sqrt(2.0 * kconst) / M_PI) + 1;
-        P += (P & 1);
+        P = 2 * (int)std::ceil(ksup / M_PI + 1.0);
         P = std::max(4, std::min(32, P));
     }
     R.P = P;
+    double s;
+    if (p.m_std > 0) {
+        s = (double)P * P / (2.0 * p.m_std * p.m_std);
+        R.m = p.m_std;
+    } else {
+        s = std::max(0.25, (P / 2.0 - 1.0) / M_PI);
+        R.m = P / std::sqrt(2.0 * s);
+    }
     const double tau = p.L[0] * p.L[1] * p.L[2];
     const double Lmin = std::min(p.L[0], std::min(p.L[1], p.L[2]));
     const CostModel C = cost_model(p.precision);
@@ -145,14 +161,14 @@ int resolve(const pb_solve_params& p, Resolved& R)
             double dd = Lmin * std::pow(2.0, -1.0 - k * 0.0625);
             if (dd < 1e-6) break;
             int M[3];
-            grid_for(p, dd, R.m, P, kconst, M);
+            grid_for(p, dd, s, kconst, M);
             bool ok = true;
             for (int a = 0; a < 3; a++) {
                 if (M[a] > 1024) ok = false;
                 if (p.M[a] > 0) {  // fixed grid: d must satisfy its k-space and deconvolution limits
                     double kmax = 2 * M_PI * (M[a] / 2 - 1) / p.L[a];
                     if (kmax * dd / 2 < std::sqrt(kconst)) ok = false;
-                    if (1.1 * P * p.L[a] / (M[a] * R.m) > dd) ok = false;
+                    if (p.L[a] / M[a] * std::sqrt(2.6 * s) > dd) ok = false;
                 }
             }
             if (!ok) continue;
@@ -171,25 +187,32 @@ int resolve(const pb_solve_params& p, Resolved& R)
     }
     R.d = d;
     R.rc = real_cut(d);
-    grid_for(p, d, R.m, P, kconst, R.M);
+    grid_for(p, d, s, kconst, R.M);
     for (int a = 0; a < 3; a++)
         if (R.M[a] > 1024)
             return fail(PB_ERR_UNSUPPORTED, "grid %d needed along axis %d exceeds 1024", R.M[a], a);
     for (int a = 0; a < 3; a++)
         if (R.P > R.M[a]) return fail(PB_ERR_UNSUPPORTED, "support P=%d exceeds grid M[%d]=%d", R.P, a, R.M[a]);
-    double h0 = p.L[0] / R.M[0];
-    R.eta = (R.P * h0) * (R.P * h0) / (2 * R.m * R.m);
-    // cell list: cells at least rc wide (capped at 128 per axis)
-    long long ncell = 1;
+    // eta from the coarsest axis (aliasing); finer axes get more support points
+    // so that every axis reaches the same truncation exponent
+    double hmax = std::max(p.L[0] / R.M[0], std::max(p.L[1] / R.M[1], p.L[2] / R.M[2]));
+    R.eta = s * hmax * hmax;
     for (int a = 0; a < 3; a++) {
-        int nc = (int)std::floor(p.L[a] / R.rc);
+        double h = p.L[a] / R.M[a];
+        int Pa = R.P;
+        if (p.m_std == 0) Pa = std::max(R.P, 2 * (int)std::ceil(std::sqrt(ksup * R.eta) / h + 1.0));
+        if (Pa > 32) return fail(PB_ERR_UNSUPPORTED, "anisotropic grid needs support %d > 32 along axis %d", Pa, a);
+        if (Pa > R.M[a]) return fail(PB_ERR_UNSUPPORTED, "support %d exceeds grid M[%d]=%d", Pa, a, R.M[a]);
+        R.Pa[a] = Pa;
+    }
+    // cell list: cells at least rc/2 wide (two-cell reach), capped at 128 per axis
+    for (int a = 0; a < 3; a++) {
+        int nc = (int)std::floor(2.0 * p.L[a] / R.rc);
         nc = std::max(1, std::min(128, nc));
         R.nc[a] = nc;
         R.h[a] = p.L[a] / nc;
         R.S[a] = (int)std::ceil(R.rc / R.h[a] - 1e-12);
-        ncell *= nc;
     }
-    (void)ncell;
     R.pairs_est = (long long)((double)R.n_tgt * p.n_src * (4 * M_PI / 3) * R.rc * R.rc * R.rc / tau);
     return PB_OK;
 }
@@ -395,6 +418,42 @@ size_t plan_layout(pb_plan_s* P, bool assign)
     return L.off;
 }
 
+// Per-instance descriptor and tables (grid_off/spec_off/bucket are kept).
+int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved& R, int src_off, int tgt_off,
+                  int cell_off, int max_terms)
+{
+    PbInst& I = P->hinst[q];
+    for (int a = 0; a < 3; a++) {
+        I.L[a] = p.L[a];
+        I.h[a] = R.h[a];
+        I.gh[a] = p.L[a] / R.M[a];
+        I.nc[a] = R.nc[a];
+        I.S[a] = R.S[a];
+        I.M[a] = R.M[a];
+        I.zero_mode[a] = 0;
+    }
+    I.alpha = p.alpha;
+    I.eps = p.eps;
+    I.d = R.d;
+    I.rc = R.rc;
+    I.eta = R.eta;
+    double Mtot = (double)R.M[0] * R.M[1] * R.M[2];
+    I.kfac = I.gh[0] * I.gh[1] * I.gh[2] / (Mtot * std::pow(M_PI * R.eta, 3.0));
+    I.P = std::max(R.Pa[0], std::max(R.Pa[1], R.Pa[2]));
+    for (int a = 0; a < 3; a++) I.Pa[a] = R.Pa[a];
+    I.n_src = R.n_src;
+    I.n_tgt = R.n_tgt;
+    I.src_off = src_off;
+    I.tgt_off = tgt_off;
+    I.cell_off = cell_off;
+    I.ncell = R.nc[0] * R.nc[1] * R.nc[2];
+    I.flags = R.flags;
+    I.same = R.same;
+    int trc = build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, &P->htab[q], max_terms);
+    if (trc) return fail(PB_ERR_INVALID, "table construction failed");
+    return PB_OK;
+}
+
 int build_plan_host(const pb_solve_params* p, int count, pb_plan_s* P)
 {
     if (count <= 0) return fail(PB_ERR_INVALID, "count must be >= 1");
@@ -473,35 +532,8 @@ int build_plan_host(const pb_solve_params* p, int count, pb_plan_s* P)
     if (!P->any_k) P->grid_elems = P->spec_elems = 0;
     int npoly = 16;
     for (int q = 0; q < count; q++) {
-        const Resolved& R = P->res[q];
-        PbInst& I = P->hinst[q];
-        for (int a = 0; a < 3; a++) {
-            I.L[a] = p[q].L[a];
-            I.h[a] = R.h[a];
-            I.gh[a] = p[q].L[a] / R.M[a];
-            I.nc[a] = R.nc[a];
-            I.S[a] = R.S[a];
-            I.M[a] = R.M[a];
-            I.zero_mode[a] = 0;
-        }
-        I.alpha = p[q].alpha;
-        I.eps = p[q].eps;
-        I.d = R.d;
-        I.rc = R.rc;
-        I.eta = R.eta;
-        double Mtot = (double)R.M[0] * R.M[1] * R.M[2];
-        I.kfac = I.gh[0] * I.gh[1] * I.gh[2] / (Mtot * std::pow(M_PI * R.eta, 3.0));
-        I.P = R.P;
-        I.n_src = R.n_src;
-        I.n_tgt = R.n_tgt;
-        I.src_off = P->src_off[q];
-        I.tgt_off = P->tgt_off[q];
-        I.cell_off = P->cell_off[q];
-        I.ncell = R.nc[0] * R.nc[1] * R.nc[2];
-        I.flags = R.flags;
-        I.same = R.same;
-        int trc = build_tables(p[q].alpha, R.d, p[q].eps, R.rc, 1e-9, &P->htab[q]);
-        if (trc) return fail(PB_ERR_INVALID, "table construction failed");
+        int trc = fill_instance(P, q, p[q], P->res[q], P->src_off[q], P->tgt_off[q], P->cell_off[q], 0);
+        if (trc) return trc;
         npoly = std::max(npoly, P->htab[q].nd);
     }
     P->npoly = npoly;
@@ -664,6 +696,176 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
     record(P, 6, s);
 }
 
+
+// Capacity plan: `cfg.max_instances` positions with one FFT grid, capacity
+// totals for sources, targets and cells; bound to actual instances by
+// pb_plan_bind before each execution (a serving slot).
+int build_slot_host(const pb_slot_config* cfg, pb_plan_s* P)
+{
+    if (!cfg || cfg->max_instances <= 0 || cfg->max_src < 0 || cfg->max_tgt < 0 || cfg->max_cells <= 0)
+        return fail(PB_ERR_INVALID, "bad slot configuration");
+    for (int a = 0; a < 3; a++)
+        if (!is_pow2(cfg->M[a]) || cfg->M[a] < 8 || cfg->M[a] > 1024)
+            return fail(PB_ERR_UNSUPPORTED, "slot grid must be powers of two in [8, 1024]");
+    if (cfg->precision != PB_PREC_FP64 && cfg->precision != PB_PREC_MIXED) return fail(PB_ERR_INVALID, "bad precision");
+    const int B = cfg->max_instances;
+    P->count = B;
+    P->prec = cfg->precision;
+    P->all_same = false;
+    P->any_real = P->any_k = P->any_zero = true;
+    P->n_src = std::max(cfg->max_src, 1);
+    P->n_tgt = std::max(cfg->max_tgt, 1);
+    P->n_y = P->n_tgt;
+    P->ncell = cfg->max_cells;
+    P->npoly = P->npoly_cap = std::max(16, std::min(kMaxPoly, cfg->npoly > 0 ? cfg->npoly : 24));
+    P->res.resize(B);
+    P->hinst.resize(B);
+    P->htab.resize(B);
+    P->par.resize(B);
+    P->src_off.assign(B + 1, 0);
+    P->tgt_off.assign(B + 1, 0);
+    P->cell_off.assign(B + 1, 0);
+    P->y_off.assign(B + 1, -1);
+    Bucket Bk;
+    std::memcpy(Bk.M, cfg->M, sizeof(Bk.M));
+    size_t gsz = (size_t)Bk.M[0] * Bk.M[1] * Bk.M[2], ssz = (size_t)Bk.M[0] * Bk.M[1] * (Bk.M[2] / 2 + 1);
+    P->grid_elems = P->spec_elems = 0;
+    // a valid, empty instance for every position
+    pb_solve_params d;
+    std::memset(&d, 0, sizeof(d));
+    d.L[0] = d.L[1] = d.L[2] = 1.0;
+    d.alpha = 1.0;
+    d.eps = 0.0;
+    d.tol = 1e-6;
+    d.d = 0.1;
+    d.rc = 0.4;
+    for (int a = 0; a < 3; a++) d.M[a] = cfg->M[a];
+    d.P = 4;
+    d.precision = cfg->precision;
+    Resolved R;
+    int rc = resolve(d, R);
+    if (rc) return rc;
+    for (int q = 0; q < B; q++) {
+        Bk.inst.push_back(q);
+        P->hinst[q].grid_off = (long long)P->grid_elems;
+        P->hinst[q].spec_off = (long long)P->spec_elems;
+        P->hinst[q].bucket = 0;
+        P->grid_elems += 3 * gsz;
+        P->spec_elems += 3 * ssz;
+        P->par[q] = d;
+        P->res[q] = R;
+        rc = fill_instance(P, q, d, R, 0, 0, 0, P->npoly_cap);
+        if (rc) return rc;
+        P->hinst[q].ncell = 0;
+    }
+    P->buckets.push_back(Bk);
+    P->bound = 0;
+    P->act_src = P->act_tgt = P->act_y = 0;
+    return PB_OK;
+}
+
+}  // namespace
+
+extern "C" int pb_plan_create_slot(const pb_slot_config* cfg, pb_plan* out)
+{
+    if (!out) return fail(PB_ERR_INVALID, "bad arguments");
+    *out = nullptr;
+    if (pb_device_count() <= 0) return fail(PB_ERR_CUDA, "no CUDA device");
+    pb_plan_s* P = new pb_plan_s();
+    int rc = build_slot_host(cfg, P);
+    if (!rc) rc = plan_alloc(P);
+    if (rc) {
+        plan_free(P);
+        return rc;
+    }
+    *out = P;
+    return PB_OK;
+}
+
+extern "C" long long pb_slot_estimate_bytes(const pb_slot_config* cfg)
+{
+    pb_plan_s tmp;
+    int rc = build_slot_host(cfg, &tmp);
+    if (rc) return rc;
+    return (long long)plan_layout(&tmp, false);
+}
+
+extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
+{
+    if (!P || (count > 0 && !p) || count < 0 || count > P->count) return fail(PB_ERR_INVALID, "bad arguments");
+    std::vector<Resolved> R(count);
+    std::vector<pb_solve_params> pp(p, p + count);
+    long long ns = 0, nt = 0, ny = 0, nc = 0;
+    for (int q = 0; q < count; q++) {
+        if (pp[q].precision != P->prec) return fail(PB_ERR_INVALID, "instance %d: precision differs from the plan", q);
+        const int* Mq = P->hinst[q].M;
+        for (int a = 0; a < 3; a++) {
+            if (pp[q].M[a] == 0) pp[q].M[a] = Mq[a];
+            if (pp[q].M[a] != Mq[a]) return fail(PB_ERR_INVALID, "instance %d: grid differs from position %d", q, q);
+        }
+        int rc = resolve(pp[q], R[q]);
+        if (rc) return rc;
+        if (P->all_same && !R[q].same) return fail(PB_ERR_INVALID, "plan holds targets-are-sources instances only");
+        ns += R[q].n_src;
+        nt += R[q].n_tgt;
+        if (!R[q].same) ny += R[q].n_tgt;
+        nc += (long long)R[q].nc[0] * R[q].nc[1] * R[q].nc[2];
+    }
+    if (ns > P->n_src || nt > P->n_tgt || (!P->all_same && ny > P->n_y) || nc > P->ncell)
+        return fail(PB_ERR_BUDGET, "bound instances exceed the plan capacity (src %lld/%d, tgt %lld/%d, cells %lld/%d)",
+                    ns, P->n_src, nt, P->n_tgt, nc, P->ncell);
+    // the previous binding's upload must have left the staging buffer
+    cudaError_t e = cudaEventSynchronize(P->ev_upload);
+    if (e != cudaSuccess) return fail(PB_ERR_CUDA, "%s", cudaGetErrorString(e));
+    int so = 0, to = 0, co = 0, yo = 0;
+    bool any_zero = false;
+    for (int q = 0; q < P->count; q++) {
+        P->src_off[q] = so;
+        P->tgt_off[q] = to;
+        P->cell_off[q] = co;
+        if (q < count) {
+            P->y_off[q] = R[q].same ? -1 : yo;
+            int rc = fill_instance(P, q, pp[q], R[q], so, to, co, P->npoly_cap);
+            if (rc) return rc;
+            P->res[q] = R[q];
+            P->par[q] = pp[q];
+            so += R[q].n_src;
+            to += R[q].n_tgt;
+            if (!R[q].same) yo += R[q].n_tgt;
+            co += R[q].nc[0] * R[q].nc[1] * R[q].nc[2];
+            if (R[q].flags & PB_ZERO_MODE) any_zero = true;
+        } else {
+            P->y_off[q] = -1;
+            PbInst& I = P->hinst[q];
+            I.n_src = I.n_tgt = 0;
+            I.src_off = so;
+            I.tgt_off = to;
+            I.cell_off = co;
+            I.ncell = 0;
+        }
+    }
+    P->src_off[P->count] = so;
+    P->tgt_off[P->count] = to;
+    P->cell_off[P->count] = co;
+    P->y_off[P->count] = -1;
+    (void)any_zero;
+    char* st = P->staging;
+    size_t ot = sizeof(PbInst) * P->count, oo = ot + sizeof(PbTables) * P->count, ob = sizeof(int) * (P->count + 1);
+    std::memcpy(st, P->hinst.data(), sizeof(PbInst) * P->count);
+    std::memcpy(st + ot, P->htab.data(), sizeof(PbTables) * P->count);
+    std::memcpy(st + oo, P->src_off.data(), ob);
+    std::memcpy(st + oo + ob, P->tgt_off.data(), ob);
+    std::memcpy(st + oo + 2 * ob, P->cell_off.data(), ob);
+    std::memcpy(st + oo + 3 * ob, P->y_off.data(), ob);
+    P->upload_pending = true;
+    P->bound = count;
+    P->act_src = (int)ns;
+    P->act_tgt = (int)nt;
+    P->act_y = (int)ny;
+    return PB_OK;
+}
+
+namespace {
 }  // namespace
 
 extern "C" {
@@ -780,10 +982,11 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
     if (!P) return fail(PB_ERR_INVALID, "null plan");
     if ((P->act_src > 0 && (!x || !f)) || (P->act_tgt > 0 && !U) || (!P->all_same && P->act_y > 0 && !y))
         return fail(PB_ERR_INVALID, "null buffer");
-    if (where != PB_HOST && where != PB_DEVICE) return fail(PB_ERR_INVALID, "bad memory location");
+    if (where != PB_HOST && where != PB_DEVICE && where != PB_HOST_PINNED)
+        return fail(PB_ERR_INVALID, "bad memory location");
     cudaStream_t us = (cudaStream_t)stream_v;
     cudaStream_t s = P->stream;
-    if (where == PB_HOST) {
+    if (where == PB_HOST || where == PB_HOST_PINNED) {
         for (size_t i = 0; i < 3 * (size_t)P->act_src; i++)
             if (!std::isfinite(x[i]) || !std::isfinite(f[i])) return fail(PB_ERR_INVALID, "non-finite input");
         if (!P->all_same)
@@ -805,7 +1008,7 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
         PB_CK(cudaEventRecord(P->ev_upload, s));
         P->upload_pending = false;
     }
-    cudaMemcpyKind kin = where == PB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    cudaMemcpyKind kin = where == PB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (P->act_src > 0) {
         PB_CK(cudaMemcpyAsync(P->x, x, sizeof(double) * 3 * P->act_src, kin, s));
         PB_CK(cudaMemcpyAsync(P->f, f, sizeof(double) * 3 * P->act_src, kin, s));
@@ -837,7 +1040,7 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
             PB_CK(cudaGraphLaunch(P->gexec, s));
         }
         PB_CK(cudaGetLastError());
-        cudaMemcpyKind kout = where == PB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        cudaMemcpyKind kout = where == PB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
         PB_CK(cudaMemcpyAsync(U, P->U, sizeof(double) * 3 * P->act_tgt, kout, s));
     }
     P->exec_count++;

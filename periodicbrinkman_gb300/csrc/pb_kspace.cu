@@ -80,10 +80,10 @@ template <class T>
 __device__ __forceinline__ void window(const PbInst& I, const double* x, int lane, T (*wgt)[kMaxP],
                                        int (*idx)[kMaxP])
 {
-    const int P = I.P;
-    if (lane < P) {
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
+    for (int a = 0; a < 3; a++) {
+        const int P = I.Pa[a];
+        if (lane < P) {
             double h = I.gh[a];
             int g0 = (int)floor(x[a] / h) - P / 2 + 1;
             double base = x[a] - (double)g0 * h;
@@ -113,12 +113,12 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const PbInst& I = inst[q];
     window<T>(I, x, lane, wgt[w], gidx[w]);
     __syncwarp();
-    const int P = I.P, P2 = P * P, P3 = P2 * P;
+    const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
     const size_t comp = (size_t)I.M[0] * I.M[1] * I.M[2];
     T* g0 = grid + I.grid_off;
     const T f0 = (T)fv[0], f1 = (T)fv[1], f2 = (T)fv[2];
     for (int id = lane; id < P3; id += 32) {
-        int px = id / P2, r = id - px * P2, py = r / P, pz = r - py * P;
+        int px = id / P2, r = id - px * P2, py = r / Pz, pz = r - py * Pz;
         T wv = wgt[w][0][px] * wgt[w][1][py] * wgt[w][2][pz];
         size_t o = ((size_t)gidx[w][0][px] * I.M[1] + gidx[w][1][py]) * I.M[2] + gidx[w][2][pz];
         atomicAdd(g0 + o, f0 * wv);
@@ -144,12 +144,12 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const PbInst& I = inst[q];
     window<T>(I, x, lane, wgt[w], gidx[w]);
     __syncwarp();
-    const int P = I.P, P2 = P * P, P3 = P2 * P;
+    const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
     const size_t comp = (size_t)I.M[0] * I.M[1] * I.M[2];
     const T* g0 = grid + I.grid_off;
     T s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0;
     for (int id = lane; id < P3; id += 32) {
-        int px = id / P2, r = id - px * P2, py = r / P, pz = r - py * P;
+        int px = id / P2, r = id - px * P2, py = r / Pz, pz = r - py * Pz;
         T wv = wgt[w][0][px] * wgt[w][1][py] * wgt[w][2][pz];
         size_t o = ((size_t)gidx[w][0][px] * I.M[1] + gidx[w][1][py]) * I.M[2] + gidx[w][2][pz];
         T v0 = wv * __ldg(g0 + o), v1 = wv * __ldg(g0 + comp + o), v2 = wv * __ldg(g0 + 2 * comp + o);

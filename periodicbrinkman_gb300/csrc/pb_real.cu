@@ -4,8 +4,12 @@
 // item, items pulled from a global counter by a persistent grid.  Each lane
 // owns one target.  The sources of the (2S+1)^3 stencil are visited as
 // contiguous z-runs of the cell-sorted source array, staged 32 at a time in
-// shared memory; a first pass builds a per-lane bit mask of the sources inside
-// the cutoff, a second pass evaluates only those pairs.
+// shared memory.  Mixed precision: each lane classifies its 32 candidate
+// pairs (inside the cutoff / inside the blob region / below r_tiny), the warp
+// compacts them into target-major queues in shared memory, and every lane then
+// evaluates one queued pair at a time, so the FMA pipe sees full warps and the
+// rare blob and series pairs never diverge the common path; per-target sums
+// of each round are formed by a segmented warp reduction (no atomics).
 //
 // Mixed precision (k_real_mixed): positions are FP32 hi/lo pairs re-expressed
 // in the frame of the target cell (error-free TwoSum), so displacements carry
@@ -58,24 +62,73 @@ __device__ __forceinline__ float horner_g(const float* __restrict__ c, int n, fl
     return h;
 }
 
+// Per-warp shared memory of the mixed-precision kernel.
+struct __align__(16) RealWarpSmem {
+    float4 s_hi[32], s_lo[32], s_f[32];  // staged sources: frame-relative hi, lo; force
+    float4 t_hi[32], t_lo[32];           // the item's targets: frame-relative hi, lo
+    float acc[3][32];                    // per-target partial sums of the current chunk
+    double acc64[3][32];                 // per-target FP64 sums of series pairs
+    unsigned short q[3][1024];           // pair queues (t << 5 | j): screened, blob region, series
+    float te1[kMaxPoly], te2[kMaxPoly];  // blob polynomials of the current instance
+};
+
+// Warp-wide exclusive prefix sum (64-bit, three packed 16-bit counters).
+__device__ __forceinline__ unsigned long long warp_excl_scan64(unsigned long long v, int lane)
+{
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+    }
+    return x - v;
+}
+
+// Segmented (by target) warp reduction of the contributions of one round of
+// a target-major queue; segment ends add into the per-target accumulators.
+__device__ __forceinline__ void segment_reduce_add(float v0, float v1, float v2, int key, int lane, float (*acc)[32])
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        float a0 = __shfl_up_sync(kFull, v0, o), a1 = __shfl_up_sync(kFull, v1, o), a2 = __shfl_up_sync(kFull, v2, o);
+        int kk = __shfl_up_sync(kFull, key, o);
+        if (lane >= o && kk == key) {
+            v0 += a0;
+            v1 += a1;
+            v2 += a2;
+        }
+    }
+    int knext = __shfl_down_sync(kFull, key, 1);
+    if (key >= 0 && (lane == 31 || knext != key)) {
+        acc[0][key] += v0;
+        acc[1][key] += v1;
+        acc[2][key] += v2;
+    }
+}
+
 template <int NP>
-__global__ void __launch_bounds__(kRealWarps * 32)
+__global__ void __launch_bounds__(kRealWarps * 32, 4)
     k_real_mixed(const PbInst* __restrict__ inst, const PbTables* __restrict__ tab, const int4* __restrict__ items,
                  const int* __restrict__ nitems_ptr, const float4* __restrict__ spos_hi, const float4* __restrict__ spos_lo,
                  const float4* __restrict__ sfrc, const int* __restrict__ src_start, const float4* __restrict__ tpos_hi,
                  const float4* __restrict__ tpos_lo, float* __restrict__ u_s, float* __restrict__ u_c,
                  double* __restrict__ u_near, int* __restrict__ counter)
 {
-    __shared__ float4 sh_hi[kRealWarps][32];
-    __shared__ float4 sh_lo[kRealWarps][32];
-    __shared__ float4 sh_f[kRealWarps][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __shared__ RealWarpSmem smem_all[kRealWarps];
+    RealWarpSmem& S = smem_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
 
     const int nitems = *nitems_ptr;
     float c1[NP], c2[NP];
     int cur_q = -1;
     float tds = 0, tdo = 0, rc2 = 0, rs2 = 0, rtiny2 = 0, tes = 0, teo = 0;
-    int ne = 0;
+    int ne = 1;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        S.acc[c][lane] = 0.f;
+        S.acc64[c][lane] = 0.0;
+    }
 
     while (true) {
         int item = 0;
@@ -99,15 +152,17 @@ __global__ void __launch_bounds__(kRealWarps * 32)
             rtiny2 = T.rtiny2f;
             tes = T.te_scale;
             teo = T.te_off;
-            ne = T.ne;
+            ne = T.ne > 0 ? T.ne : 1;
+            if (lane < kMaxPoly) {
+                S.te1[lane] = T.pe1[lane];
+                S.te2[lane] = T.pe2[lane];
+            }
         }
         ItemFrame F;
         item_frame(I, it, F);
         const bool active = lane < it.w;
         const int tidx = it.z + (active ? lane : 0);
-        // sorted index of this target among the sources when targets are the sources
         const int self_src = I.same ? tidx - I.tgt_off + I.src_off : -1;
-        // target in the cell frame, hi + lo
         float th[3], tl[3];
         {
             float4 ph = tpos_hi[tidx], pl = tpos_lo[tidx];
@@ -117,12 +172,13 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                 float oh, ol, s, e;
                 split_double(F.O[a], oh, ol);
                 two_sum(xh[a], -oh, s, e);
-                th[a] = s;
+                th[a] = active ? s : 3.0e30f;  // inactive lanes pair with nothing
                 tl[a] = e + (xl[a] - ol);
             }
         }
+        S.t_hi[lane] = make_float4(th[0], th[1], th[2], 0.f);
+        S.t_lo[lane] = make_float4(tl[0], tl[1], tl[2], 0.f);
         float s0 = 0, s1 = 0, s2 = 0, k0 = 0, k1 = 0, k2 = 0;
-        double n0 = 0, n1 = 0, n2 = 0;
 
         for (int o0 = -I.S[0]; o0 <= I.S[0]; o0++) {
             int g0 = F.c0 + o0;
@@ -148,86 +204,158 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                     split_double(F.O[1] - sh1, qh[1], ql[1]);
                     split_double(F.O[2] - sh2, qh[2], ql[2]);
                     for (int base = b; base < e; base += 32) {
-                        int j = base + lane;
-                        if (j < e) {
+                        const int j = base + lane;
+                        const int ncand = min(32, e - base);
+                        if (lane < ncand) {
                             float4 ph = spos_hi[j], pl = spos_lo[j];
                             float xh[3] = {ph.x, ph.y, ph.z}, xl[3] = {pl.x, pl.y, pl.z};
-                            float ph3[3], pl3[3];
+                            float p3[3], l3[3];
 #pragma unroll
                             for (int a = 0; a < 3; a++) {
                                 float s, er;
                                 two_sum(xh[a], -qh[a], s, er);
-                                ph3[a] = s;
-                                pl3[a] = er + (xl[a] - ql[a]);
+                                p3[a] = s;
+                                l3[a] = er + (xl[a] - ql[a]);
                             }
-                            sh_hi[w][lane] = make_float4(ph3[0], ph3[1], ph3[2], 0.f);
-                            sh_lo[w][lane] = make_float4(pl3[0], pl3[1], pl3[2], 0.f);
-                            sh_f[w][lane] = sfrc[j];
+                            S.s_hi[lane] = make_float4(p3[0], p3[1], p3[2], 0.f);
+                            S.s_lo[lane] = make_float4(l3[0], l3[1], l3[2], 0.f);
+                            S.s_f[lane] = sfrc[j];
                         }
                         __syncwarp();
-                        const int ncand = min(32, e - base);
-                        unsigned mask = 0;
-                        if (active) {
-                            for (int jj = 0; jj < ncand; jj++) {
-                                float4 p = sh_hi[w][jj];
-                                float dx = th[0] - p.x, dy = th[1] - p.y, dz = th[2] - p.z;
-                                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                                mask |= (r2 < rc2 ? 1u : 0u) << jj;
-                            }
-                            // the self pair (targets are the sources, same particle, no shift)
-                            // is added in FP64 by the combine kernel
-                            if (self_src >= base && self_src < base + ncand && zero_shift)
-                                mask &= ~(1u << (self_src - base));
+                        // classify candidate pairs of this lane's target: screened / blob region / series
+                        unsigned mn = 0, mb = 0, ms = 0;
+                        for (int jj = 0; jj < ncand; jj++) {
+                            float4 p = S.s_hi[jj];
+                            float dx = th[0] - p.x, dy = th[1] - p.y, dz = th[2] - p.z;
+                            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                            unsigned in = r2 < rc2, nb = r2 < rs2, ns = r2 < rtiny2;
+                            mn |= (in & (nb ^ 1u)) << jj;
+                            mb |= (nb & (ns ^ 1u)) << jj;
+                            ms |= ns << jj;
                         }
-                        float a0 = 0, a1 = 0, a2 = 0;
-                        while (__any_sync(kFull, mask)) {
-                            if (mask) {
-                                int jj = __ffs(mask) - 1;
-                                mask &= mask - 1;
-                                float4 p = sh_hi[w][jj], pl = sh_lo[w][jj], f = sh_f[w][jj];
-                                float dx = (th[0] - p.x) + (tl[0] - pl.x);
-                                float dy = (th[1] - p.y) + (tl[1] - pl.y);
-                                float dz = (th[2] - p.z) + (tl[2] - pl.z);
+                        if (zero_shift && self_src >= base && self_src < base + ncand)
+                            ms &= ~(1u << (self_src - base));  // self pair: added in FP64 by the combine kernel
+                        // target-major queues
+                        unsigned long long cnt = (unsigned long long)__popc(mn) |
+                                                 ((unsigned long long)__popc(mb) << 16) |
+                                                 ((unsigned long long)__popc(ms) << 32);
+                        unsigned long long ex = warp_excl_scan64(cnt, lane);
+                        unsigned long long tot = __shfl_sync(kFull, ex + cnt, 31);
+                        {
+                            int pn = (int)(ex & 0xffff), pb = (int)((ex >> 16) & 0xffff), ps = (int)(ex >> 32);
+                            unsigned short tag = (unsigned short)(lane << 5);
+                            unsigned m = mn;
+                            while (m) {
+                                int jj = __ffs(m) - 1;
+                                m &= m - 1;
+                                S.q[0][pn++] = tag | jj;
+                            }
+                            m = mb;
+                            while (m) {
+                                int jj = __ffs(m) - 1;
+                                m &= m - 1;
+                                S.q[1][pb++] = tag | jj;
+                            }
+                            m = ms;
+                            while (m) {
+                                int jj = __ffs(m) - 1;
+                                m &= m - 1;
+                                S.q[2][ps++] = tag | jj;
+                            }
+                        }
+                        __syncwarp();
+                        const int nn = (int)(tot & 0xffff), nbq = (int)((tot >> 16) & 0xffff), nsq = (int)(tot >> 32);
+                        // screened pairs: T(r) polynomial of S - R_d only
+                        for (int e0 = 0; e0 < nn; e0 += 32) {
+                            const int ei = e0 + lane;
+                            float v0 = 0, v1 = 0, v2 = 0;
+                            int key = -1 - lane;
+                            if (ei < nn) {
+                                const int qv = S.q[0][ei], t = qv >> 5, jj = qv & 31;
+                                key = t;
+                                float4 p = S.s_hi[jj], pl = S.s_lo[jj], f = S.s_f[jj];
+                                float4 a = S.t_hi[t], al = S.t_lo[t];
+                                float dx = (a.x - p.x) + (al.x - pl.x);
+                                float dy = (a.y - p.y) + (al.y - pl.y);
+                                float dz = (a.z - p.z) + (al.z - pl.z);
                                 float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                                if (r2 < rtiny2 || r2 == 0.f) {
-                                    double H1, H2;
-                                    double ddx = dx, ddy = dy, ddz = dz;
-                                    double rr = ddx * ddx + ddy * ddy + ddz * ddz;
-                                    if (T.blob) {
-                                        series_H(T, rr, H1, H2);
-                                    } else {
-                                        H1 = T.self1;
-                                        H2 = 0;
-                                    }
-                                    double fd = f.x * ddx + f.y * ddy + f.z * ddz;
-                                    n0 += H1 * f.x + H2 * fd * ddx;
-                                    n1 += H1 * f.y + H2 * fd * ddy;
-                                    n2 += H1 * f.z + H2 * fd * ddz;
-                                } else {
-                                    float ri = rsqrtf(r2);
-                                    ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
-                                    float r = r2 * ri;
-                                    float t = fmaf(r, tds, tdo);
-                                    float T1 = horner<NP>(c1, t);
-                                    float T2 = horner<NP>(c2, t);
-                                    if (r2 < rs2) {
-                                        float te = fmaf(r, tes, teo);
-                                        T1 -= horner_g(T.pe1, ne, te);
-                                        T2 -= horner_g(T.pe2, ne, te);
-                                    }
-                                    float H1 = T1 * ri;
-                                    float H2 = T2 * (ri * ri * ri);
-                                    float fd = fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
-                                    float g = H2 * fd;
-                                    a0 = fmaf(H1, f.x, fmaf(g, dx, a0));
-                                    a1 = fmaf(H1, f.y, fmaf(g, dy, a1));
-                                    a2 = fmaf(H1, f.z, fmaf(g, dz, a2));
+                                float ri = rsqrtf(r2);
+                                ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
+                                float r = r2 * ri;
+                                float tt = fmaf(r, tds, tdo);
+                                float T1 = horner<NP>(c1, tt), T2 = horner<NP>(c2, tt);
+                                float H1 = T1 * ri, H2 = T2 * (ri * ri * ri);
+                                float g = H2 * fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
+                                v0 = fmaf(H1, f.x, g * dx);
+                                v1 = fmaf(H1, f.y, g * dy);
+                                v2 = fmaf(H1, f.z, g * dz);
+                            }
+                            segment_reduce_add(v0, v1, v2, key, lane, S.acc);
+                        }
+                        // blob-region pairs: subtract the polynomial of S - R_eps
+                        for (int e0 = 0; e0 < nbq; e0 += 32) {
+                            const int ei = e0 + lane;
+                            float v0 = 0, v1 = 0, v2 = 0;
+                            int key = -1 - lane;
+                            if (ei < nbq) {
+                                const int qv = S.q[1][ei], t = qv >> 5, jj = qv & 31;
+                                key = t;
+                                float4 p = S.s_hi[jj], pl = S.s_lo[jj], f = S.s_f[jj];
+                                float4 a = S.t_hi[t], al = S.t_lo[t];
+                                float dx = (a.x - p.x) + (al.x - pl.x);
+                                float dy = (a.y - p.y) + (al.y - pl.y);
+                                float dz = (a.z - p.z) + (al.z - pl.z);
+                                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                                float ri = rsqrtf(r2);
+                                ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
+                                float r = r2 * ri;
+                                float tt = fmaf(r, tds, tdo);
+                                float T1 = horner<NP>(c1, tt), T2 = horner<NP>(c2, tt);
+                                float te = fmaf(r, tes, teo);
+                                float E1 = S.te1[ne - 1], E2 = S.te2[ne - 1];
+                                for (int k = ne - 2; k >= 0; k--) {
+                                    E1 = fmaf(E1, te, S.te1[k]);
+                                    E2 = fmaf(E2, te, S.te2[k]);
                                 }
+                                float H1 = (T1 - E1) * ri, H2 = (T2 - E2) * (ri * ri * ri);
+                                float g = H2 * fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
+                                v0 = fmaf(H1, f.x, g * dx);
+                                v1 = fmaf(H1, f.y, g * dy);
+                                v2 = fmaf(H1, f.z, g * dz);
+                            }
+                            segment_reduce_add(v0, v1, v2, key, lane, S.acc);
+                        }
+                        // series pairs (r < r_tiny): FP64 series of R_eps - R_d, FP64 sums
+                        for (int e0 = 0; e0 < nsq; e0 += 32) {
+                            const int ei = e0 + lane;
+                            if (ei < nsq) {
+                                const int qv = S.q[2][ei], t = qv >> 5, jj = qv & 31;
+                                float4 p = S.s_hi[jj], pl = S.s_lo[jj], f = S.s_f[jj];
+                                float4 a = S.t_hi[t], al = S.t_lo[t];
+                                double dx = (double)(a.x - p.x) + (double)(al.x - pl.x);
+                                double dy = (double)(a.y - p.y) + (double)(al.y - pl.y);
+                                double dz = (double)(a.z - p.z) + (double)(al.z - pl.z);
+                                double rr = dx * dx + dy * dy + dz * dz;
+                                double H1, H2;
+                                if (T.blob) {
+                                    series_H(T, rr, H1, H2);
+                                } else {
+                                    H1 = T.self1;  // coincident points, eps = 0: the reference's r -> 0 limit
+                                    H2 = 0;
+                                }
+                                double fd = f.x * dx + f.y * dy + f.z * dz;
+                                atomicAdd(&S.acc64[0][t], H1 * f.x + H2 * fd * dx);
+                                atomicAdd(&S.acc64[1][t], H1 * f.y + H2 * fd * dy);
+                                atomicAdd(&S.acc64[2][t], H1 * f.z + H2 * fd * dz);
                             }
                         }
-                        kahan_add(s0, k0, a0);
-                        kahan_add(s1, k1, a1);
-                        kahan_add(s2, k2, a2);
+                        __syncwarp();
+                        kahan_add(s0, k0, S.acc[0][lane]);
+                        kahan_add(s1, k1, S.acc[1][lane]);
+                        kahan_add(s2, k2, S.acc[2][lane]);
+                        S.acc[0][lane] = 0.f;
+                        S.acc[1][lane] = 0.f;
+                        S.acc[2][lane] = 0.f;
                         __syncwarp();
                     }
                 }
@@ -241,10 +369,14 @@ __global__ void __launch_bounds__(kRealWarps * 32)
             u_c[o] = k0;
             u_c[o + 1] = k1;
             u_c[o + 2] = k2;
-            u_near[o] = n0;
-            u_near[o + 1] = n1;
-            u_near[o + 2] = n2;
+            u_near[o] = S.acc64[0][lane];
+            u_near[o + 1] = S.acc64[1][lane];
+            u_near[o + 2] = S.acc64[2][lane];
         }
+        S.acc64[0][lane] = 0.0;
+        S.acc64[1][lane] = 0.0;
+        S.acc64[2][lane] = 0.0;
+        __syncwarp();
     }
 }
 

@@ -1,0 +1,422 @@
+// Continuous-batching request server.
+//
+// Requests of different sizes are autotuned on submission, assigned to the
+// smallest provisioned FFT grid that holds their k-space resolution, and
+// queued per grid.  A scheduler thread keeps a fixed set of resident slots
+// (capacity plans with their own stream, buffers, pinned staging and CUDA
+// graph): whenever a slot is idle it binds the next requests of its grid
+// queue that fit its capacity, stages their inputs, and launches the slot's
+// graph; slots run concurrently, so requests arriving while others are on the
+// GPU are admitted as soon as a slot frees up.  Device memory is fixed at
+// creation and bounded by the configured budget (admission by memory
+// budget); a request no slot can hold is rejected at submission.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "pbrinkman.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Req {
+    long long id;
+    pb_solve_params p;
+    int grid;
+    int n_tgt_eff;
+    const double *x, *f, *y;
+    double* U;
+    Clock::time_point t_sub, t_done;
+    std::atomic<int> state{0};  // 0 queued, 1 running, 2 done
+    int status = PB_OK;
+};
+
+struct Slot {
+    int grid = 0;
+    pb_plan plan = nullptr;
+    pb_slot_config cfg{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    double *x = nullptr, *f = nullptr, *y = nullptr, *U = nullptr;  // pinned staging
+    bool busy = false;
+    std::vector<Req*> reqs;
+    std::vector<pb_solve_params> params;
+};
+
+std::string g_srv_err;
+
+}  // namespace
+
+struct pb_server_s {
+    pb_server_config cfg{};
+    std::vector<Slot> slots;
+    std::vector<int> grids;
+    long long device_bytes = 0;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Req*> inbox;
+    std::unordered_map<long long, Req*> reqs;
+    std::vector<std::deque<Req*>> queues;  // per grid index
+    std::thread worker;
+    std::atomic<bool> stop{false};
+    std::atomic<long long> next_id{1}, submitted{0}, completed{0}, failed{0}, rejected{0}, batches{0},
+        batched_instances{0};
+    int device = 0;
+};
+
+namespace {
+
+int grid_index(pb_server_s* S, int g)
+{
+    for (size_t i = 0; i < S->grids.size(); i++)
+        if (S->grids[i] >= g) return (int)i;
+    return -1;
+}
+
+void finish_slot(pb_server_s* S, Slot& sl, int status)
+{
+    size_t off = 0;
+    for (Req* r : sl.reqs) {
+        size_t nb = 3 * (size_t)r->n_tgt_eff;
+        if (status == PB_OK) std::memcpy(r->U, sl.U + off, nb * sizeof(double));
+        off += nb;
+        r->status = status;
+        r->t_done = Clock::now();
+        r->state.store(2);
+        if (status == PB_OK)
+            S->completed++;
+        else
+            S->failed++;
+    }
+    sl.reqs.clear();
+    sl.busy = false;
+}
+
+bool dispatch(pb_server_s* S, Slot& sl, std::deque<Req*>& q)
+{
+    if (q.empty()) return false;
+    const pb_slot_config& c = sl.cfg;
+    long long ns = 0, nt = 0, ny = 0;
+    sl.reqs.clear();
+    sl.params.clear();
+    while (!q.empty() && (int)sl.reqs.size() < c.max_instances) {
+        Req* r = q.front();
+        long long n = r->p.n_src, m = r->n_tgt_eff;
+        if (ns + n > c.max_src || nt + m > c.max_tgt) break;
+        ns += n;
+        nt += m;
+        if (r->p.n_tgt > 0) ny += m;
+        q.pop_front();
+        sl.reqs.push_back(r);
+        pb_solve_params p = r->p;
+        p.M[0] = p.M[1] = p.M[2] = sl.grid;
+        sl.params.push_back(p);
+    }
+    if (sl.reqs.empty()) return false;
+    int rc = pb_plan_bind(sl.plan, sl.params.data(), (int)sl.params.size());
+    if (rc == PB_ERR_BUDGET && sl.reqs.size() > 1) {
+        // cells over capacity: put all back but the first and bind it alone
+        for (size_t k = sl.reqs.size(); k-- > 1;) q.push_front(sl.reqs[k]);
+        sl.reqs.resize(1);
+        sl.params.resize(1);
+        ns = sl.reqs[0]->p.n_src;
+        nt = sl.reqs[0]->n_tgt_eff;
+        ny = sl.reqs[0]->p.n_tgt > 0 ? nt : 0;
+        rc = pb_plan_bind(sl.plan, sl.params.data(), 1);
+    }
+    if (rc != PB_OK) {
+        finish_slot(S, sl, rc);
+        return true;
+    }
+    size_t xo = 0, yo = 0;
+    for (Req* r : sl.reqs) {
+        size_t n3 = 3 * (size_t)r->p.n_src;
+        std::memcpy(sl.x + xo, r->x, n3 * sizeof(double));
+        std::memcpy(sl.f + xo, r->f, n3 * sizeof(double));
+        xo += n3;
+        if (r->p.n_tgt > 0) {
+            size_t m3 = 3 * (size_t)r->p.n_tgt;
+            std::memcpy(sl.y + yo, r->y, m3 * sizeof(double));
+            yo += m3;
+        }
+        r->state.store(1);
+    }
+    rc = pb_plan_execute(sl.plan, sl.x, sl.f, sl.y, sl.U, PB_HOST_PINNED, sl.stream);
+    if (rc == PB_OK && cudaEventRecord(sl.done, sl.stream) != cudaSuccess) rc = PB_ERR_CUDA;
+    if (rc != PB_OK) {
+        finish_slot(S, sl, rc);
+        return true;
+    }
+    sl.busy = true;
+    S->batches++;
+    S->batched_instances += (long long)sl.reqs.size();
+    return true;
+}
+
+void worker_loop(pb_server_s* S)
+{
+    cudaSetDevice(S->device);
+    while (!S->stop.load()) {
+        bool did = false;
+        for (Slot& sl : S->slots) {
+            if (!sl.busy) continue;
+            cudaError_t e = cudaEventQuery(sl.done);
+            if (e == cudaSuccess) {
+                finish_slot(S, sl, PB_OK);
+                did = true;
+            } else if (e != cudaErrorNotReady) {
+                cudaGetLastError();
+                finish_slot(S, sl, PB_ERR_CUDA);
+                did = true;
+            }
+        }
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            while (!S->inbox.empty()) {
+                Req* r = S->inbox.front();
+                S->inbox.pop_front();
+                S->queues[r->grid].push_back(r);
+            }
+        }
+        for (Slot& sl : S->slots) {
+            if (sl.busy) continue;
+            int gi = grid_index(S, sl.grid);
+            if (gi >= 0 && dispatch(S, sl, S->queues[gi])) did = true;
+        }
+        if (!did) {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cv.wait_for(lk, std::chrono::microseconds(50), [&] { return !S->inbox.empty() || S->stop.load(); });
+        }
+    }
+}
+
+void destroy_slots(pb_server_s* S)
+{
+    for (Slot& sl : S->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.plan) pb_plan_destroy(sl.plan);
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+        for (double* p : {sl.x, sl.f, sl.y, sl.U})
+            if (p) cudaFreeHost(p);
+    }
+    S->slots.clear();
+}
+
+}  // namespace
+
+extern "C" {
+
+int pb_server_create(const pb_server_config* cfg_in, pb_server* out)
+{
+    if (!out) return PB_ERR_INVALID;
+    *out = nullptr;
+    if (pb_device_count() <= 0) return PB_ERR_CUDA;
+    pb_server_config cfg = cfg_in ? *cfg_in : pb_server_config{};
+    if (cfg.budget_bytes <= 0) cfg.budget_bytes = 150LL << 30;
+    if (cfg.max_batch <= 0) cfg.max_batch = 16;
+    if (cfg.slots_per_grid <= 0) cfg.slots_per_grid = 2;
+    if (cfg.max_src <= 0) cfg.max_src = 1 << 18;
+    if (cfg.max_tgt <= 0) cfg.max_tgt = cfg.max_src;
+    if (cfg.n_grids <= 0) {
+        int dg[] = {8, 16, 32, 64, 128, 256};
+        cfg.n_grids = 6;
+        for (int i = 0; i < 6; i++) cfg.grids[i] = dg[i];
+    }
+    if (cfg.n_grids > 8) return PB_ERR_INVALID;
+    pb_server_s* S = new pb_server_s();
+    S->cfg = cfg;
+    cudaGetDevice(&S->device);
+    for (int i = 0; i < cfg.n_grids; i++) S->grids.push_back(cfg.grids[i]);
+    std::sort(S->grids.begin(), S->grids.end());
+    S->queues.resize(S->grids.size());
+    long long used = 0;
+    for (int g : S->grids) {
+        for (int k = 0; k < cfg.slots_per_grid; k++) {
+            Slot sl;
+            sl.grid = g;
+            sl.cfg.M[0] = sl.cfg.M[1] = sl.cfg.M[2] = g;
+            // large grids hold fewer instances: keep the grids of one slot near 1/8 of the budget share
+            long long gbytes = 3LL * g * g * g * (cfg.precision == PB_PREC_FP64 ? 8 : 4) * 2;
+            long long share = cfg.budget_bytes / (long long)(S->grids.size() * cfg.slots_per_grid);
+            int B = (int)std::max(1LL, std::min<long long>(cfg.max_batch, share / (2 * gbytes)));
+            sl.cfg.max_instances = B;
+            sl.cfg.max_src = cfg.max_src;
+            sl.cfg.max_tgt = cfg.max_tgt;
+            sl.cfg.max_cells = 1 << 21;
+            sl.cfg.precision = cfg.precision;
+            sl.cfg.npoly = 24;
+            long long est = pb_slot_estimate_bytes(&sl.cfg);
+            if (est < 0 || used + est > cfg.budget_bytes) continue;
+            int rc = pb_plan_create_slot(&sl.cfg, &sl.plan);
+            if (rc != PB_OK) {
+                g_srv_err = pb_last_error();
+                S->slots.push_back(sl);
+                destroy_slots(S);
+                delete S;
+                return rc;
+            }
+            used += est;
+            cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+            cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+            size_t xs = 3 * (size_t)cfg.max_src * sizeof(double), ts = 3 * (size_t)cfg.max_tgt * sizeof(double);
+            if (cudaMallocHost(&sl.x, xs) != cudaSuccess || cudaMallocHost(&sl.f, xs) != cudaSuccess ||
+                cudaMallocHost(&sl.y, ts) != cudaSuccess || cudaMallocHost(&sl.U, ts) != cudaSuccess) {
+                S->slots.push_back(sl);
+                destroy_slots(S);
+                delete S;
+                return PB_ERR_NOMEM;
+            }
+            S->slots.push_back(sl);
+        }
+    }
+    if (S->slots.empty()) {
+        delete S;
+        return PB_ERR_BUDGET;
+    }
+    S->device_bytes = used;
+    S->worker = std::thread(worker_loop, S);
+    *out = S;
+    return PB_OK;
+}
+
+int pb_server_submit(pb_server S, const pb_solve_params* p, const double* x, const double* f, const double* y,
+                     double* U, long long* ticket)
+{
+    if (!S || !p || !ticket) return PB_ERR_INVALID;
+    *ticket = 0;
+    if (p->precision != S->cfg.precision) return PB_ERR_INVALID;
+    if (p->n_src <= 0 || (p->n_tgt > 0 && !y) || !x || !f || !U) return PB_ERR_INVALID;
+    pb_instance_info info;
+    int rc = pb_resolve(p, &info);
+    if (rc != PB_OK) return rc;
+    int need = std::max(info.M[0], std::max(info.M[1], info.M[2]));
+    int gi = grid_index(S, need);
+    int n_tgt_eff = p->n_tgt > 0 ? p->n_tgt : p->n_src;
+    bool fits = false;
+    for (const Slot& sl : S->slots)
+        if (gi >= 0 && sl.grid == S->grids[gi] && p->n_src <= sl.cfg.max_src && n_tgt_eff <= sl.cfg.max_tgt)
+            fits = true;
+    if (!fits) {
+        S->rejected++;
+        return PB_ERR_BUDGET;
+    }
+    Req* r = new Req();
+    r->id = S->next_id++;
+    r->p = *p;
+    r->grid = gi;
+    r->n_tgt_eff = n_tgt_eff;
+    r->x = x;
+    r->f = f;
+    r->y = y;
+    r->U = U;
+    r->t_sub = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (S->cfg.queue_capacity > 0 && (long long)S->inbox.size() >= S->cfg.queue_capacity) {
+            delete r;
+            S->rejected++;
+            return PB_ERR_BUSY;
+        }
+        S->reqs[r->id] = r;
+        S->inbox.push_back(r);
+    }
+    S->submitted++;
+    S->cv.notify_one();
+    *ticket = r->id;
+    return PB_OK;
+}
+
+int pb_server_poll(pb_server S, long long ticket, int* state, int* status, double* latency_s)
+{
+    if (!S) return PB_ERR_INVALID;
+    Req* r = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        auto it = S->reqs.find(ticket);
+        if (it == S->reqs.end()) return PB_ERR_INVALID;
+        r = it->second;
+    }
+    int st = r->state.load();
+    if (state) *state = st;
+    if (st == 2) {
+        if (status) *status = r->status;
+        if (latency_s) *latency_s = std::chrono::duration<double>(r->t_done - r->t_sub).count();
+    }
+    return PB_OK;
+}
+
+int pb_server_release(pb_server S, long long ticket)
+{
+    if (!S) return PB_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return PB_ERR_INVALID;
+    if (it->second->state.load() != 2) return PB_ERR_BUSY;
+    delete it->second;
+    S->reqs.erase(it);
+    return PB_OK;
+}
+
+int pb_server_wait(pb_server S, long long ticket, double timeout_s, int* status, double* latency_s)
+{
+    auto t0 = Clock::now();
+    while (true) {
+        int state = 0;
+        int rc = pb_server_poll(S, ticket, &state, status, latency_s);
+        if (rc != PB_OK) return rc;
+        if (state == 2) return PB_OK;
+        if (timeout_s >= 0 && std::chrono::duration<double>(Clock::now() - t0).count() > timeout_s) return PB_ERR_BUSY;
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+int pb_server_drain(pb_server S, double timeout_s)
+{
+    if (!S) return PB_ERR_INVALID;
+    auto t0 = Clock::now();
+    while (S->completed.load() + S->failed.load() < S->submitted.load()) {
+        if (timeout_s >= 0 && std::chrono::duration<double>(Clock::now() - t0).count() > timeout_s) return PB_ERR_BUSY;
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    return PB_OK;
+}
+
+int pb_server_stats(pb_server S, pb_server_counters* out)
+{
+    if (!S || !out) return PB_ERR_INVALID;
+    out->submitted = S->submitted.load();
+    out->completed = S->completed.load();
+    out->failed = S->failed.load();
+    out->rejected = S->rejected.load();
+    out->batches = S->batches.load();
+    out->mean_batch = out->batches ? (double)S->batched_instances.load() / out->batches : 0.0;
+    out->device_bytes = S->device_bytes;
+    out->slots = (int)S->slots.size();
+    return PB_OK;
+}
+
+int pb_server_destroy(pb_server S)
+{
+    if (!S) return PB_OK;
+    S->stop.store(true);
+    S->cv.notify_all();
+    if (S->worker.joinable()) S->worker.join();
+    destroy_slots(S);
+    for (auto& kv : S->reqs) delete kv.second;
+    delete S;
+    return PB_OK;
+}
+
+}  // extern "C"

@@ -56,7 +56,8 @@ struct PbInst {
     int nc[3];        // cells per axis
     int S[3];         // stencil reach per axis (cells)
     int M[3];         // FFT grid
-    int P;            // Gaussian support (points per axis)
+    int P;            // Gaussian support (points), max over axes
+    int Pa[3];        // Gaussian support per axis
     int n_src, n_tgt;
     int src_off, tgt_off;     // offsets into the packed particle arrays
     int cell_off, ncell;      // offset into the packed cell arrays
