@@ -94,23 +94,48 @@ int validate(const pb_solve_params& p)
 }
 
 // Choose the grid for splitting width d (tuning fields the user left at 0).
-// s = eta / h^2 is the Gaussian width in grid units (fixed by the support).
-void grid_for(const pb_solve_params& p, double d, double s, double kconst, int* M)
+// u = d/h is the splitting width in grid units that the Gaussian needs.
+void grid_for(const pb_solve_params& p, double d, double u, double kconst, int* M)
 {
     for (int a = 0; a < 3; a++) {
         if (p.M[a] > 0) {
             M[a] = p.M[a];
             continue;
         }
-        // k-space truncation exp(-kmax^2 d^2/4) <= tol with kmax = 2 pi (M/2 - 1)/L
-        // (Nyquist planes are zeroed), and Gaussian deconvolution: the spreading
-        // width eta = s h^2 must stay below d^2/2 (with margin) so that
-        // exp(-k^2 (d^2/4 - eta/2)) still decays.
+        // k-space truncation exp(-kmax^2 d^2/4) <= tol/10 with kmax = 2 pi (M/2 - 1)/L
+        // (Nyquist planes are zeroed), and the spreading error bound on d/h
         double nk = 2.0 * std::sqrt(kconst) / d * p.L[a] / (2 * M_PI) + 1.0;
         double mk = 2.0 * nk + 2.0;
-        double md = p.L[a] * std::sqrt(2.6 * s) / d;
+        double md = p.L[a] * u / d + 2.0;
         M[a] = pow2ceil((int)std::ceil(std::max(mk, md)));
     }
+}
+
+// Spectral-Ewald error model of the Gaussian support (s = eta/h^2 in grid units):
+//   window truncation   exp(-(P/2 - 1)^2 / s)        (the window reaches (P/2-1) h)
+//   aliasing            exp(-pi^2 s (1 - s h^2/d^2))  (worst mode after deconvolution)
+// For a support P the widest admissible Gaussian minimises the d/h the
+// aliasing bound asks for.
+struct Support {
+    int P;
+    double s, u;  // u = minimal d/h
+};
+
+Support support_for(int P, double Ealias, double Etrunc, double m_std)
+{
+    Support S;
+    S.P = P;
+    if (m_std > 0) {
+        S.s = (double)P * P / (2.0 * m_std * m_std);  // the reference's eta = (P h / m)^2 / 2
+    } else {
+        S.s = std::min(2.0 * Ealias / (M_PI * M_PI), (P / 2.0 - 1.0) * (P / 2.0 - 1.0) / Etrunc);
+    }
+    double ps = M_PI * M_PI * S.s;
+    if (ps > 1.02 * Ealias)
+        S.u = std::sqrt(ps * S.s / (ps - Ealias));
+    else
+        S.u = 1e9;  // this support cannot reach the tolerance
+    return S;
 }
 
 int resolve(const pb_solve_params& p, Resolved& R)
@@ -124,27 +149,29 @@ int resolve(const pb_solve_params& p, Resolved& R)
     R.same = (p.n_tgt == 0);
     R.n_tgt = R.same ? p.n_src : p.n_tgt;
     const double kconst = std::log(10.0 / tol);      // k-space truncation exponent
-    const double ksup = std::log(1.0 / tol) + 1.0;   // Gaussian truncation and aliasing exponent
+    const double ealias = std::log(1.0 / tol) + 1.0; // aliasing exponent
+    const double etrunc = std::max(4.0, ealias - 3.0);
     const double zeta = std::sqrt(std::log(1.0 / tol)) + 0.35;
-    // Gaussian support: a window of P points reaches (P/2 - 1) h from the
-    // particle on the near side; with eta = s h^2 the truncation error is
-    // exp(-(P/2-1)^2 / s) and the grid aliasing error exp(-pi^2 s).  Given P,
-    // s = (P/2 - 1)/pi balances both at exp(-pi (P/2 - 1)); given the
-    // reference's m (support half-width in standard deviations), s = P^2/(2 m^2).
-    int P = p.P;
-    if (P == 0) {
-        P = 2 * (int)std::ceil(ksup / M_PI + 1.0);
-        P = std::max(4, std::min(32, P));
-    }
-    R.P = P;
-    double s;
-    if (p.m_std > 0) {
-        s = (double)P * P / (2.0 * p.m_std * p.m_std);
-        R.m = p.m_std;
+    const double uk = 2.0 * std::sqrt(kconst) / M_PI;  // d/h asked by the k-space truncation
+    Support sup;
+    if (p.P > 0) {
+        sup = support_for(p.P, ealias, etrunc, p.m_std);
+        if (sup.u > 1e8) sup.u = uk;  // user support below the tolerance: keep the k-space bound
     } else {
-        s = std::max(0.25, (P / 2.0 - 1.0) / M_PI);
-        R.m = P / std::sqrt(2.0 * s);
+        sup = support_for(32, ealias, etrunc, p.m_std);
+        for (int P = 6; P <= 32; P += 2) {
+            Support t = support_for(P, ealias, etrunc, p.m_std);
+            if (t.u <= 1.1 * uk) {
+                sup = t;
+                break;
+            }
+        }
     }
+    const int P = sup.P;
+    const double s = sup.s;
+    const double u = std::max(sup.u, uk);
+    R.P = P;
+    R.m = P / std::sqrt(2.0 * s);
     const double tau = p.L[0] * p.L[1] * p.L[2];
     const double Lmin = std::min(p.L[0], std::min(p.L[1], p.L[2]));
     const CostModel C = cost_model(p.precision);
@@ -161,14 +188,14 @@ int resolve(const pb_solve_params& p, Resolved& R)
             double dd = Lmin * std::pow(2.0, -1.0 - k * 0.0625);
             if (dd < 1e-6) break;
             int M[3];
-            grid_for(p, dd, s, kconst, M);
+            grid_for(p, dd, u, kconst, M);
             bool ok = true;
             for (int a = 0; a < 3; a++) {
                 if (M[a] > 1024) ok = false;
-                if (p.M[a] > 0) {  // fixed grid: d must satisfy its k-space and deconvolution limits
+                if (p.M[a] > 0) {  // fixed grid: d must satisfy its k-space and spreading limits
                     double kmax = 2 * M_PI * (M[a] / 2 - 1) / p.L[a];
                     if (kmax * dd / 2 < std::sqrt(kconst)) ok = false;
-                    if (p.L[a] / M[a] * std::sqrt(2.6 * s) > dd) ok = false;
+                    if (p.L[a] / M[a] * u > dd) ok = false;
                 }
             }
             if (!ok) continue;
@@ -187,7 +214,7 @@ int resolve(const pb_solve_params& p, Resolved& R)
     }
     R.d = d;
     R.rc = real_cut(d);
-    grid_for(p, d, s, kconst, R.M);
+    grid_for(p, d, u, kconst, R.M);
     for (int a = 0; a < 3; a++)
         if (R.M[a] > 1024)
             return fail(PB_ERR_UNSUPPORTED, "grid %d needed along axis %d exceeds 1024", R.M[a], a);
@@ -200,7 +227,7 @@ int resolve(const pb_solve_params& p, Resolved& R)
     for (int a = 0; a < 3; a++) {
         double h = p.L[a] / R.M[a];
         int Pa = R.P;
-        if (p.m_std == 0) Pa = std::max(R.P, 2 * (int)std::ceil(std::sqrt(ksup * R.eta) / h + 1.0));
+        if (p.m_std == 0) Pa = std::max(R.P, 2 * (int)std::ceil(std::sqrt(etrunc * R.eta) / h + 1.0));
         if (Pa > 32) return fail(PB_ERR_UNSUPPORTED, "anisotropic grid needs support %d > 32 along axis %d", Pa, a);
         if (Pa > R.M[a]) return fail(PB_ERR_UNSUPPORTED, "support %d exceeds grid M[%d]=%d", Pa, a, R.M[a]);
         R.Pa[a] = Pa;
@@ -236,7 +263,7 @@ struct pb_plan_s {
     std::vector<Resolved> res;
     std::vector<PbInst> hinst;
     std::vector<PbTables> htab;
-    std::vector<int> src_off, tgt_off, cell_off, y_off;
+    std::vector<int> src_off, tgt_off, cell_off, y_off, unit_off;
     int n_src = 0, n_tgt = 0, ncell = 0, npoly = 16, n_y = 0;
     std::vector<Bucket> buckets;
     size_t grid_elems = 0, spec_elems = 0;
@@ -245,7 +272,8 @@ struct pb_plan_s {
     size_t arena_bytes = 0;
     PbInst* d_inst = nullptr;
     PbTables* d_tab = nullptr;
-    int *d_src_off = nullptr, *d_tgt_off = nullptr, *d_cell_off = nullptr, *d_y_off = nullptr;
+    int *d_src_off = nullptr, *d_tgt_off = nullptr, *d_cell_off = nullptr, *d_y_off = nullptr, *d_unit_off = nullptr;
+    int ucap = 0;  // spreading tiles (capacity)
     double *x = nullptr, *f = nullptr, *y = nullptr, *ypack = nullptr, *U = nullptr;
     int *cell_of_s = nullptr, *cnt_s = nullptr, *start_s = nullptr, *fill_s = nullptr, *perm_s = nullptr,
         *perm_tmp_s = nullptr;
@@ -300,7 +328,8 @@ size_t plan_layout(pb_plan_s* P, bool assign)
     const int ns = std::max(P->n_src, 1), nt = std::max(P->n_tgt, 1), nc = std::max(P->ncell, 1);
     const int q = P->count;
     size_t o_inst = L.take<PbInst>(q), o_tab = L.take<PbTables>(q);
-    size_t o_so = L.take<int>(q + 1), o_to = L.take<int>(q + 1), o_co = L.take<int>(q + 1), o_yo = L.take<int>(q + 1);
+    size_t o_so = L.take<int>(q + 1), o_to = L.take<int>(q + 1), o_co = L.take<int>(q + 1), o_yo = L.take<int>(q + 1),
+           o_uo = L.take<int>(q + 1);
     size_t o_x = L.take<double>(3 * (size_t)ns), o_f = L.take<double>(3 * (size_t)ns);
     size_t o_y = P->all_same ? 0 : L.take<double>(3 * (size_t)std::max(P->n_y, 1));
     size_t o_yp = P->all_same ? 0 : L.take<double>(3 * (size_t)nt);
@@ -362,6 +391,7 @@ size_t plan_layout(pb_plan_s* P, bool assign)
         P->d_tgt_off = (int*)(A + o_to);
         P->d_cell_off = (int*)(A + o_co);
         P->d_y_off = (int*)(A + o_yo);
+        P->d_unit_off = (int*)(A + o_uo);
         P->x = (double*)(A + o_x);
         P->f = (double*)(A + o_f);
         P->y = P->all_same ? nullptr : (double*)(A + o_y);
@@ -449,6 +479,18 @@ int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved&
     I.ncell = R.nc[0] * R.nc[1] * R.nc[2];
     I.flags = R.flags;
     I.same = R.same;
+    // spreading tiles: ublk^3 cells whose window union fits the shared-memory box
+    {
+        int edge = tile_edge_points(P->prec == PB_PREC_FP64);
+        int B = 1 << 20;
+        for (int a = 0; a < 3; a++) {
+            double cells_per_h = R.h[a] / I.gh[a];
+            int b = (int)std::floor((edge - R.Pa[a] - 3) / cells_per_h);
+            B = std::min(B, std::max(1, b));
+        }
+        I.ublk = B;
+        for (int a = 0; a < 3; a++) I.nu[a] = (R.nc[a] + B - 1) / B;
+    }
     int trc = build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, &P->htab[q], max_terms);
     if (trc) return fail(PB_ERR_INVALID, "table construction failed");
     return PB_OK;
@@ -531,11 +573,18 @@ int build_plan_host(const pb_solve_params* p, int count, pb_plan_s* P)
     }
     if (!P->any_k) P->grid_elems = P->spec_elems = 0;
     int npoly = 16;
+    P->unit_off.assign(count + 1, 0);
+    int uo = 0;
     for (int q = 0; q < count; q++) {
         int trc = fill_instance(P, q, p[q], P->res[q], P->src_off[q], P->tgt_off[q], P->cell_off[q], 0);
         if (trc) return trc;
         npoly = std::max(npoly, P->htab[q].nd);
+        P->unit_off[q] = uo;
+        P->hinst[q].unit_off = uo;
+        uo += P->hinst[q].nu[0] * P->hinst[q].nu[1] * P->hinst[q].nu[2];
     }
+    P->unit_off[count] = uo;
+    P->ucap = uo;
     P->npoly = npoly;
     P->npoly_cap = npoly;
     P->bound = count;
@@ -573,7 +622,7 @@ int plan_alloc(pb_plan_s* P)
     }
     plan_layout(P, true);
     PB_CK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
-    P->staging_bytes = (sizeof(PbInst) + sizeof(PbTables)) * (size_t)P->count + 4 * sizeof(int) * (P->count + 1);
+    P->staging_bytes = (sizeof(PbInst) + sizeof(PbTables)) * (size_t)P->count + 5 * sizeof(int) * (P->count + 1);
     PB_CK(cudaMallocHost(&P->staging, P->staging_bytes));
     PB_CK(cudaEventCreateWithFlags(&P->ev_upload, cudaEventDisableTiming));
     PB_CK(cudaEventCreateWithFlags(&P->ev_in, cudaEventDisableTiming));
@@ -586,6 +635,7 @@ int plan_alloc(pb_plan_s* P)
     PB_CK(cudaMemcpy(P->d_tgt_off, P->tgt_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
     PB_CK(cudaMemcpy(P->d_cell_off, P->cell_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
     PB_CK(cudaMemcpy(P->d_y_off, P->y_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
+    PB_CK(cudaMemcpy(P->d_unit_off, P->unit_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
     const bool fp64 = P->prec == PB_PREC_FP64;
     for (auto& B : P->buckets) {
         std::vector<char> tw(twiddle_bytes(B.M, fp64));
@@ -656,11 +706,11 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
         size_t esz = mixed ? 4 : 8;
         cudaMemsetAsync(P->grid, 0, P->grid_elems * esz, s);
         if (mixed)
-            launch_spread<float>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
-                                 (float*)P->grid, s);
+            launch_spread_tiles<float>(P->d_inst, P->count, P->d_unit_off, P->ucap, P->start_s, P->spos_a, P->spos_b,
+                                       P->sfrc, (float*)P->grid, P->nsm, s);
         else
-            launch_spread<double>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
-                                  (double*)P->grid, s);
+            launch_spread_tiles<double>(P->d_inst, P->count, P->d_unit_off, P->ucap, P->start_s, P->spos_a,
+                                        P->spos_b, P->sfrc, (double*)P->grid, P->nsm, s);
         record(P, 3, s);
         for (auto& B : P->buckets) {
             const PbInst& I0 = P->hinst[B.inst[0]];
@@ -674,11 +724,11 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
         }
         record(P, 4, s);
         if (mixed)
-            launch_gather<float>(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->tpos_a, P->tpos_b,
-                                 (const float*)P->grid, (float*)P->u_k, s);
+            launch_gather_tiles<float>(P->d_inst, P->count, P->d_unit_off, P->ucap, P->start_t, P->tpos_a,
+                                       P->tpos_b, (const float*)P->grid, (float*)P->u_k, P->nsm, s);
         else
-            launch_gather<double>(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->tpos_a, P->tpos_b,
-                                  (const double*)P->grid, (double*)P->u_k, s);
+            launch_gather_tiles<double>(P->d_inst, P->count, P->d_unit_off, P->ucap, P->start_t, P->tpos_a,
+                                        P->tpos_b, (const double*)P->grid, (double*)P->u_k, P->nsm, s);
     } else {
         record(P, 3, s);
         record(P, 4, s);
@@ -759,6 +809,9 @@ int build_slot_host(const pb_slot_config* cfg, pb_plan_s* P)
         P->hinst[q].ncell = 0;
     }
     P->buckets.push_back(Bk);
+    P->unit_off.assign(B + 1, 0);
+    for (int q = 0; q < B; q++) P->hinst[q].unit_off = 0;
+    P->ucap = cfg->max_cells;
     P->bound = 0;
     P->act_src = P->act_tgt = P->act_y = 0;
     return PB_OK;
@@ -817,7 +870,7 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
     // the previous binding's upload must have left the staging buffer
     cudaError_t e = cudaEventSynchronize(P->ev_upload);
     if (e != cudaSuccess) return fail(PB_ERR_CUDA, "%s", cudaGetErrorString(e));
-    int so = 0, to = 0, co = 0, yo = 0;
+    int so = 0, to = 0, co = 0, yo = 0, uo = 0;
     bool any_zero = false;
     for (int q = 0; q < P->count; q++) {
         P->src_off[q] = so;
@@ -829,6 +882,9 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
             if (rc) return rc;
             P->res[q] = R[q];
             P->par[q] = pp[q];
+            P->unit_off[q] = uo;
+            P->hinst[q].unit_off = uo;
+            uo += P->hinst[q].nu[0] * P->hinst[q].nu[1] * P->hinst[q].nu[2];
             so += R[q].n_src;
             to += R[q].n_tgt;
             if (!R[q].same) yo += R[q].n_tgt;
@@ -842,8 +898,12 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
             I.tgt_off = to;
             I.cell_off = co;
             I.ncell = 0;
+            P->unit_off[q] = uo;
+            I.unit_off = uo;
         }
     }
+    P->unit_off[P->count] = uo;
+    if (uo > P->ucap) return fail(PB_ERR_BUDGET, "spreading tiles exceed the plan capacity");
     P->src_off[P->count] = so;
     P->tgt_off[P->count] = to;
     P->cell_off[P->count] = co;
@@ -857,6 +917,7 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
     std::memcpy(st + oo + ob, P->tgt_off.data(), ob);
     std::memcpy(st + oo + 2 * ob, P->cell_off.data(), ob);
     std::memcpy(st + oo + 3 * ob, P->y_off.data(), ob);
+    std::memcpy(st + oo + 4 * ob, P->unit_off.data(), ob);
     P->upload_pending = true;
     P->bound = count;
     P->act_src = (int)ns;
@@ -1005,6 +1066,7 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
         PB_CK(cudaMemcpyAsync(P->d_tgt_off, st + oo + ob, ob, cudaMemcpyHostToDevice, s));
         PB_CK(cudaMemcpyAsync(P->d_cell_off, st + oo + 2 * ob, ob, cudaMemcpyHostToDevice, s));
         PB_CK(cudaMemcpyAsync(P->d_y_off, st + oo + 3 * ob, ob, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_unit_off, st + oo + 4 * ob, ob, cudaMemcpyHostToDevice, s));
         PB_CK(cudaEventRecord(P->ev_upload, s));
         P->upload_pending = false;
     }

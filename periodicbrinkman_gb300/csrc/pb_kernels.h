@@ -54,6 +54,15 @@ void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int nc
 template <class T>
 void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const void* pos_a,
                    const void* pos_b, const T* grid, T* u_k, cudaStream_t s);
+// Tiled versions: one block per tile of ublk^3 cells (PbInst.ublk/nu/unit_off),
+// the union of the windows in shared memory; ucap = capacity of tiles.
+template <class T>
+void launch_spread_tiles(const PbInst* inst, int ninst, const int* unit_off, int ucap, const int* cstart,
+                         const void* pos_a, const void* pos_b, const void* frc, T* grid, int nsm, cudaStream_t s);
+template <class T>
+void launch_gather_tiles(const PbInst* inst, int ninst, const int* unit_off, int ucap, const int* cstart,
+                         const void* pos_a, const void* pos_b, const T* grid, T* u_k, int nsm, cudaStream_t s);
+int tile_edge_points(bool fp64);
 // Batched 3D R2C -> Green multiply -> C2R over `nvol` volumes of equal size
 // (3 components per instance, instances contiguous).
 template <class T>

@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                             float4 p = S.s_hi[jj];
                             float dx = th[0] - p.x, dy = th[1] - p.y, dz = th[2] - p.z;
                             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                            unsigned in = r2 < rc2, nb = r2 < rs2, ns = r2 < rtiny2;
+                            unsigned in = r2 < rc2, nb = r2 < rs2, ns = (r2 < rtiny2) | (r2 == 0.f);
                             mn |= (in & (nb ^ 1u)) << jj;
                             mb |= (nb & (ns ^ 1u)) << jj;
                             ms |= ns << jj;
@@ -339,9 +339,15 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                                 double H1, H2;
                                 if (T.blob) {
                                     series_H(T, rr, H1, H2);
-                                } else {
+                                } else if (rr == 0.0) {
                                     H1 = T.self1;  // coincident points, eps = 0: the reference's r -> 0 limit
                                     H2 = 0;
+                                } else {  // eps = 0, nearly coincident: singular kernel from the polynomial
+                                    float r2f = (float)rr, ri = rsqrtf(r2f);
+                                    ri = ri * fmaf(-0.5f * r2f * ri, ri, 1.5f);
+                                    float tt = fmaf(r2f * ri, tds, tdo);
+                                    H1 = (double)(horner<NP>(c1, tt) * ri);
+                                    H2 = (double)(horner<NP>(c2, tt) * (ri * ri * ri));
                                 }
                                 double fd = f.x * dx + f.y * dy + f.z * dz;
                                 atomicAdd(&S.acc64[0][t], H1 * f.x + H2 * fd * dx);

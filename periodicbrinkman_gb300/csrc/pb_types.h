@@ -66,7 +66,10 @@ struct PbInst {
     int flags;
     int same;                 // targets are the sources
     int bucket;               // FFT size bucket
-    int pad;
+    int ublk;                 // cells per edge of a spreading tile (0: per-particle spreading)
+    int nu[3];                // spreading tiles per axis
+    int unit_off;             // first spreading tile of the instance
+    int pad2;
 };
 
 }  // namespace pb
