@@ -422,16 +422,22 @@ void pbo_reg_quad(double r, double a, double d1, double d2, int mode, double *H1
 {
     gl_init();
     double dmin = (mode == 1 && d2 < d1) ? d2 : d1;
+    double dmax = (mode == 1 && d2 > d1) ? d2 : d1;
     double K = 14.0 / dmin;
     double w = 1.0 / dmin;
     if (r > 0 && 1.5 / r < w) w = 1.5 / r;
     int nu = (int)ceil(K / w);
-    double *edges = (double *)malloc(sizeof(double) * (nu + 32));
+    double *edges = (double *)malloc(sizeof(double) * (nu + 64));
     int ne = 0;
     for (int i = 0; i <= nu; i++) edges[ne++] = K * i / nu;
     for (int j = -4; j <= 4; j++) {
         double e = a * ldexp(1.0, j);
         if (e > 0 && e < K) edges[ne++] = e;
+    }
+    /* the wider blob decays on the k scale 1/dmax: resolve it too */
+    for (int i = 1; i <= 28; i++) {
+        double e = 0.5 * i / dmax;
+        if (e < K) edges[ne++] = e;
     }
     qsort(edges, ne, sizeof(double), cmp_dbl);
     double s1 = 0, s2 = 0;

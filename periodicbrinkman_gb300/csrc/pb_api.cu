@@ -148,10 +148,11 @@ int resolve(const pb_solve_params& p, Resolved& R)
     R.n_src = p.n_src;
     R.same = (p.n_tgt == 0);
     R.n_tgt = R.same ? p.n_src : p.n_tgt;
-    const double kconst = std::log(10.0 / tol);      // k-space truncation exponent
-    const double ealias = std::log(1.0 / tol) + 1.0; // aliasing exponent
+    // error budgets aim at tol/2 so that the sum of the parts stays below tol
+    const double kconst = std::log(20.0 / tol);      // k-space truncation exponent
+    const double ealias = std::log(2.0 / tol) + 1.0; // aliasing exponent
     const double etrunc = std::max(4.0, ealias - 3.0);
-    const double zeta = std::sqrt(std::log(1.0 / tol)) + 0.35;
+    const double zeta = std::sqrt(std::log(2.0 / tol)) + 0.35;
     const double uk = 2.0 * std::sqrt(kconst) / M_PI;  // d/h asked by the k-space truncation
     Support sup;
     if (p.P > 0) {
@@ -239,6 +240,7 @@ int resolve(const pb_solve_params& p, Resolved& R)
         R.nc[a] = nc;
         R.h[a] = p.L[a] / nc;
         R.S[a] = (int)std::ceil(R.rc / R.h[a] - 1e-12);
+        if (R.S[a] > 15) return fail(PB_ERR_UNSUPPORTED, "real-space cutoff spans more than 15 cells along axis %d", a);
     }
     R.pairs_est = (long long)((double)R.n_tgt * p.n_src * (4 * M_PI / 3) * R.rc * R.rc * R.rc / tau);
     return PB_OK;
@@ -263,7 +265,7 @@ struct pb_plan_s {
     std::vector<Resolved> res;
     std::vector<PbInst> hinst;
     std::vector<PbTables> htab;
-    std::vector<int> src_off, tgt_off, cell_off, y_off, unit_off;
+    std::vector<int> src_off, tgt_off, cell_off, y_off;
     int n_src = 0, n_tgt = 0, ncell = 0, npoly = 16, n_y = 0;
     std::vector<Bucket> buckets;
     size_t grid_elems = 0, spec_elems = 0;
@@ -272,8 +274,7 @@ struct pb_plan_s {
     size_t arena_bytes = 0;
     PbInst* d_inst = nullptr;
     PbTables* d_tab = nullptr;
-    int *d_src_off = nullptr, *d_tgt_off = nullptr, *d_cell_off = nullptr, *d_y_off = nullptr, *d_unit_off = nullptr;
-    int ucap = 0;  // spreading tiles (capacity)
+    int *d_src_off = nullptr, *d_tgt_off = nullptr, *d_cell_off = nullptr, *d_y_off = nullptr;
     double *x = nullptr, *f = nullptr, *y = nullptr, *ypack = nullptr, *U = nullptr;
     int *cell_of_s = nullptr, *cnt_s = nullptr, *start_s = nullptr, *fill_s = nullptr, *perm_s = nullptr,
         *perm_tmp_s = nullptr;
@@ -328,8 +329,7 @@ size_t plan_layout(pb_plan_s* P, bool assign)
     const int ns = std::max(P->n_src, 1), nt = std::max(P->n_tgt, 1), nc = std::max(P->ncell, 1);
     const int q = P->count;
     size_t o_inst = L.take<PbInst>(q), o_tab = L.take<PbTables>(q);
-    size_t o_so = L.take<int>(q + 1), o_to = L.take<int>(q + 1), o_co = L.take<int>(q + 1), o_yo = L.take<int>(q + 1),
-           o_uo = L.take<int>(q + 1);
+    size_t o_so = L.take<int>(q + 1), o_to = L.take<int>(q + 1), o_co = L.take<int>(q + 1), o_yo = L.take<int>(q + 1);
     size_t o_x = L.take<double>(3 * (size_t)ns), o_f = L.take<double>(3 * (size_t)ns);
     size_t o_y = P->all_same ? 0 : L.take<double>(3 * (size_t)std::max(P->n_y, 1));
     size_t o_yp = P->all_same ? 0 : L.take<double>(3 * (size_t)nt);
@@ -391,7 +391,6 @@ size_t plan_layout(pb_plan_s* P, bool assign)
         P->d_tgt_off = (int*)(A + o_to);
         P->d_cell_off = (int*)(A + o_co);
         P->d_y_off = (int*)(A + o_yo);
-        P->d_unit_off = (int*)(A + o_uo);
         P->x = (double*)(A + o_x);
         P->f = (double*)(A + o_f);
         P->y = P->all_same ? nullptr : (double*)(A + o_y);
@@ -479,18 +478,6 @@ int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved&
     I.ncell = R.nc[0] * R.nc[1] * R.nc[2];
     I.flags = R.flags;
     I.same = R.same;
-    // spreading tiles: ublk^3 cells whose window union fits the shared-memory box
-    {
-        int edge = tile_edge_points(P->prec == PB_PREC_FP64);
-        int B = 1 << 20;
-        for (int a = 0; a < 3; a++) {
-            double cells_per_h = R.h[a] / I.gh[a];
-            int b = (int)std::floor((edge - R.Pa[a] - 3) / cells_per_h);
-            B = std::min(B, std::max(1, b));
-        }
-        I.ublk = B;
-        for (int a = 0; a < 3; a++) I.nu[a] = (R.nc[a] + B - 1) / B;
-    }
     int trc = build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, &P->htab[q], max_terms);
     if (trc) return fail(PB_ERR_INVALID, "table construction failed");
     return PB_OK;
@@ -567,24 +554,17 @@ int build_plan_host(const pb_solve_params* p, int count, pb_plan_s* P)
             I.grid_off = (long long)P->grid_elems;
             I.spec_off = (long long)P->spec_elems;
             I.bucket = (int)b;
-            P->grid_elems += 3 * gsz;
+            P->grid_elems += 4 * gsz;
             P->spec_elems += 3 * ssz;
         }
     }
     if (!P->any_k) P->grid_elems = P->spec_elems = 0;
     int npoly = 16;
-    P->unit_off.assign(count + 1, 0);
-    int uo = 0;
     for (int q = 0; q < count; q++) {
         int trc = fill_instance(P, q, p[q], P->res[q], P->src_off[q], P->tgt_off[q], P->cell_off[q], 0);
         if (trc) return trc;
         npoly = std::max(npoly, P->htab[q].nd);
-        P->unit_off[q] = uo;
-        P->hinst[q].unit_off = uo;
-        uo += P->hinst[q].nu[0] * P->hinst[q].nu[1] * P->hinst[q].nu[2];
     }
-    P->unit_off[count] = uo;
-    P->ucap = uo;
     P->npoly = npoly;
     P->npoly_cap = npoly;
     P->bound = count;
@@ -622,7 +602,7 @@ int plan_alloc(pb_plan_s* P)
     }
     plan_layout(P, true);
     PB_CK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
-    P->staging_bytes = (sizeof(PbInst) + sizeof(PbTables)) * (size_t)P->count + 5 * sizeof(int) * (P->count + 1);
+    P->staging_bytes = (sizeof(PbInst) + sizeof(PbTables)) * (size_t)P->count + 4 * sizeof(int) * (P->count + 1);
     PB_CK(cudaMallocHost(&P->staging, P->staging_bytes));
     PB_CK(cudaEventCreateWithFlags(&P->ev_upload, cudaEventDisableTiming));
     PB_CK(cudaEventCreateWithFlags(&P->ev_in, cudaEventDisableTiming));
@@ -635,7 +615,6 @@ int plan_alloc(pb_plan_s* P)
     PB_CK(cudaMemcpy(P->d_tgt_off, P->tgt_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
     PB_CK(cudaMemcpy(P->d_cell_off, P->cell_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
     PB_CK(cudaMemcpy(P->d_y_off, P->y_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
-    PB_CK(cudaMemcpy(P->d_unit_off, P->unit_off.data(), sizeof(int) * (P->count + 1), cudaMemcpyHostToDevice));
     const bool fp64 = P->prec == PB_PREC_FP64;
     for (auto& B : P->buckets) {
         std::vector<char> tw(twiddle_bytes(B.M, fp64));
@@ -686,9 +665,9 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
             launch_prepare_fp64(P->ypack, nullptr, P->perm_t, P->n_tgt, P->d_tgt_off, P->d_inst, P->count,
                                 (Dbl4*)P->tpos_a, nullptr, s);
     }
-    launch_count_chunks(P->start_t, P->ncell, P->chunks, s);
+    launch_count_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->chunks, s);
     launch_exclusive_scan(P->chunks, P->chunk_start, P->ncell, P->scan_tmp, s);
-    launch_emit_items(P->start_t, P->chunk_start, P->ncell, P->d_cell_off, P->count, P->items, s);
+    launch_emit_items(P->start_t, P->chunk_start, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items, s);
     record(P, 1, s);
     if (P->any_real) {
         const int* nitems = P->chunk_start + P->ncell;
@@ -706,11 +685,11 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
         size_t esz = mixed ? 4 : 8;
         cudaMemsetAsync(P->grid, 0, P->grid_elems * esz, s);
         if (mixed)
-            launch_spread_tiles<float>(P->d_inst, P->count, P->d_unit_off, P->ucap, P->start_s, P->spos_a, P->spos_b,
-                                       P->sfrc, (float*)P->grid, P->nsm, s);
+            launch_spread<float>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
+                                 (float*)P->grid, s);
         else
-            launch_spread_tiles<double>(P->d_inst, P->count, P->d_unit_off, P->ucap, P->start_s, P->spos_a,
-                                        P->spos_b, P->sfrc, (double*)P->grid, P->nsm, s);
+            launch_spread<double>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
+                                  (double*)P->grid, s);
         record(P, 3, s);
         for (auto& B : P->buckets) {
             const PbInst& I0 = P->hinst[B.inst[0]];
@@ -724,11 +703,11 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
         }
         record(P, 4, s);
         if (mixed)
-            launch_gather_tiles<float>(P->d_inst, P->count, P->d_unit_off, P->ucap, P->start_t, P->tpos_a,
-                                       P->tpos_b, (const float*)P->grid, (float*)P->u_k, P->nsm, s);
+            launch_gather<float>(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->tpos_a, P->tpos_b,
+                                 (const float*)P->grid, (float*)P->u_k, s);
         else
-            launch_gather_tiles<double>(P->d_inst, P->count, P->d_unit_off, P->ucap, P->start_t, P->tpos_a,
-                                        P->tpos_b, (const double*)P->grid, (double*)P->u_k, P->nsm, s);
+            launch_gather<double>(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->tpos_a, P->tpos_b,
+                                  (const double*)P->grid, (double*)P->u_k, s);
     } else {
         record(P, 3, s);
         record(P, 4, s);
@@ -800,7 +779,7 @@ int build_slot_host(const pb_slot_config* cfg, pb_plan_s* P)
         P->hinst[q].grid_off = (long long)P->grid_elems;
         P->hinst[q].spec_off = (long long)P->spec_elems;
         P->hinst[q].bucket = 0;
-        P->grid_elems += 3 * gsz;
+        P->grid_elems += 4 * gsz;
         P->spec_elems += 3 * ssz;
         P->par[q] = d;
         P->res[q] = R;
@@ -809,9 +788,6 @@ int build_slot_host(const pb_slot_config* cfg, pb_plan_s* P)
         P->hinst[q].ncell = 0;
     }
     P->buckets.push_back(Bk);
-    P->unit_off.assign(B + 1, 0);
-    for (int q = 0; q < B; q++) P->hinst[q].unit_off = 0;
-    P->ucap = cfg->max_cells;
     P->bound = 0;
     P->act_src = P->act_tgt = P->act_y = 0;
     return PB_OK;
@@ -870,7 +846,7 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
     // the previous binding's upload must have left the staging buffer
     cudaError_t e = cudaEventSynchronize(P->ev_upload);
     if (e != cudaSuccess) return fail(PB_ERR_CUDA, "%s", cudaGetErrorString(e));
-    int so = 0, to = 0, co = 0, yo = 0, uo = 0;
+    int so = 0, to = 0, co = 0, yo = 0;
     bool any_zero = false;
     for (int q = 0; q < P->count; q++) {
         P->src_off[q] = so;
@@ -882,9 +858,6 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
             if (rc) return rc;
             P->res[q] = R[q];
             P->par[q] = pp[q];
-            P->unit_off[q] = uo;
-            P->hinst[q].unit_off = uo;
-            uo += P->hinst[q].nu[0] * P->hinst[q].nu[1] * P->hinst[q].nu[2];
             so += R[q].n_src;
             to += R[q].n_tgt;
             if (!R[q].same) yo += R[q].n_tgt;
@@ -898,12 +871,8 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
             I.tgt_off = to;
             I.cell_off = co;
             I.ncell = 0;
-            P->unit_off[q] = uo;
-            I.unit_off = uo;
         }
     }
-    P->unit_off[P->count] = uo;
-    if (uo > P->ucap) return fail(PB_ERR_BUDGET, "spreading tiles exceed the plan capacity");
     P->src_off[P->count] = so;
     P->tgt_off[P->count] = to;
     P->cell_off[P->count] = co;
@@ -917,7 +886,6 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
     std::memcpy(st + oo + ob, P->tgt_off.data(), ob);
     std::memcpy(st + oo + 2 * ob, P->cell_off.data(), ob);
     std::memcpy(st + oo + 3 * ob, P->y_off.data(), ob);
-    std::memcpy(st + oo + 4 * ob, P->unit_off.data(), ob);
     P->upload_pending = true;
     P->bound = count;
     P->act_src = (int)ns;
@@ -1066,7 +1034,6 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
         PB_CK(cudaMemcpyAsync(P->d_tgt_off, st + oo + ob, ob, cudaMemcpyHostToDevice, s));
         PB_CK(cudaMemcpyAsync(P->d_cell_off, st + oo + 2 * ob, ob, cudaMemcpyHostToDevice, s));
         PB_CK(cudaMemcpyAsync(P->d_y_off, st + oo + 3 * ob, ob, cudaMemcpyHostToDevice, s));
-        PB_CK(cudaMemcpyAsync(P->d_unit_off, st + oo + 4 * ob, ob, cudaMemcpyHostToDevice, s));
         PB_CK(cudaEventRecord(P->ev_upload, s));
         P->upload_pending = false;
     }

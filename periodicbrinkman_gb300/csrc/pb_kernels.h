@@ -30,10 +30,12 @@ void launch_prepare_mixed(const double* pos, const double* frc, const int* perm,
                           cudaStream_t s);
 void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                          const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, cudaStream_t s);
-// Work items: one per (target cell, chunk of <= 32 targets): int4 {inst, cell, first, count}.
-void launch_count_chunks(const int* start, int ncell_tot, int* chunks, cudaStream_t s);
-void launch_emit_items(const int* start, const int* chunk_start, int ncell_tot, const int* cell_offsets,
-                       int ninst, int4* items, cudaStream_t s);
+// Work items: up to 32 consecutive targets of one cell row spanning <= 8 cells:
+// int4 {inst, first target, local row, count | za << 8 | zb << 16}.
+void launch_count_items(const int* start, int ncell_tot, const int* cell_offsets, const PbInst* inst, int ninst,
+                        int* counts, cudaStream_t s);
+void launch_emit_items(const int* start, const int* item_start, int ncell_tot, const int* cell_offsets,
+                       const PbInst* inst, int ninst, int4* items, cudaStream_t s);
 
 // ---- real space (pb_real.cu) ----
 // Mixed precision: FP32 polynomial kernel, hi/lo displacements, Kahan sums.
@@ -54,15 +56,6 @@ void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int nc
 template <class T>
 void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const void* pos_a,
                    const void* pos_b, const T* grid, T* u_k, cudaStream_t s);
-// Tiled versions: one block per tile of ublk^3 cells (PbInst.ublk/nu/unit_off),
-// the union of the windows in shared memory; ucap = capacity of tiles.
-template <class T>
-void launch_spread_tiles(const PbInst* inst, int ninst, const int* unit_off, int ucap, const int* cstart,
-                         const void* pos_a, const void* pos_b, const void* frc, T* grid, int nsm, cudaStream_t s);
-template <class T>
-void launch_gather_tiles(const PbInst* inst, int ninst, const int* unit_off, int ucap, const int* cstart,
-                         const void* pos_a, const void* pos_b, const T* grid, T* u_k, int nsm, cudaStream_t s);
-int tile_edge_points(bool fp64);
 // Batched 3D R2C -> Green multiply -> C2R over `nvol` volumes of equal size
 // (3 components per instance, instances contiguous).
 template <class T>

@@ -10,6 +10,8 @@
 // complex by the packed half-length transform), y, and x; the x pass of the
 // forward transform is fused with the Green multiplication and the x pass of
 // the inverse, so the spectrum is read and written once for all three.
+#include <algorithm>
+
 #include "pb_device.cuh"
 #include "pb_kernels.h"
 
@@ -182,6 +184,80 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     }
 }
 
+// FP32 grids interleave the three components of a point in one float4, so a
+// point costs one vector atomic (spread) or one 16-byte load (gather).
+__global__ void __launch_bounds__(kSpreadWarps * 32)
+    k_spread_f4(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
+                const float4* __restrict__ pb, const float4* __restrict__ frc, float* __restrict__ grid)
+{
+    __shared__ float wgt[kSpreadWarps][3][kMaxP];
+    __shared__ int gidx[kSpreadWarps][3][kMaxP];
+    const int ntot = *ntot_p;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int s = blockIdx.x * kSpreadWarps + w;
+    if (s >= ntot) return;
+    double x[3], fv[3];
+    int q;
+    load_pos(pa, pb, s, x, q);
+    load_frc(frc, s, fv);
+    const PbInst& I = inst[q];
+    window<float>(I, x, lane, wgt[w], gidx[w]);
+    __syncwarp();
+    const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
+    float4* g4 = reinterpret_cast<float4*>(grid + I.grid_off);
+    const float f0 = (float)fv[0], f1 = (float)fv[1], f2 = (float)fv[2];
+    for (int id = lane; id < P3; id += 32) {
+        int px = id / P2, r = id - px * P2, py = r / Pz, pz = r - py * Pz;
+        float wv = wgt[w][0][px] * wgt[w][1][py] * wgt[w][2][pz];
+        size_t o = ((size_t)gidx[w][0][px] * I.M[1] + gidx[w][1][py]) * I.M[2] + gidx[w][2][pz];
+        atomicAdd(g4 + o, make_float4(f0 * wv, f1 * wv, f2 * wv, 0.f));
+    }
+}
+
+__global__ void __launch_bounds__(kSpreadWarps * 32)
+    k_gather_f4(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
+                const float4* __restrict__ pb, const float* __restrict__ grid, float* __restrict__ u_k)
+{
+    __shared__ float wgt[kSpreadWarps][3][kMaxP];
+    __shared__ int gidx[kSpreadWarps][3][kMaxP];
+    const int ntot = *ntot_p;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int s = blockIdx.x * kSpreadWarps + w;
+    if (s >= ntot) return;
+    double x[3];
+    int q;
+    load_pos(pa, pb, s, x, q);
+    const PbInst& I = inst[q];
+    window<float>(I, x, lane, wgt[w], gidx[w]);
+    __syncwarp();
+    const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
+    const float4* g4 = reinterpret_cast<const float4*>(grid + I.grid_off);
+    float s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0;
+    for (int id = lane; id < P3; id += 32) {
+        int px = id / P2, r = id - px * P2, py = r / Pz, pz = r - py * Pz;
+        float wv = wgt[w][0][px] * wgt[w][1][py] * wgt[w][2][pz];
+        size_t o = ((size_t)gidx[w][0][px] * I.M[1] + gidx[w][1][py]) * I.M[2] + gidx[w][2][pz];
+        float4 v = __ldg(g4 + o);
+        kahan_add(s0, c0, wv * v.x);
+        kahan_add(s1, c1, wv * v.y);
+        kahan_add(s2, c2, wv * v.z);
+    }
+    s0 -= c0;
+    s1 -= c1;
+    s2 -= c2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(kFull, s0, o);
+        s1 += __shfl_xor_sync(kFull, s1, o);
+        s2 += __shfl_xor_sync(kFull, s2, o);
+    }
+    if (lane == 0) {
+        u_k[3 * (size_t)s] = s0;
+        u_k[3 * (size_t)s + 1] = s1;
+        u_k[3 * (size_t)s + 2] = s2;
+    }
+}
+
 template <class T>
 void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int ncap, const void* pos_a,
                    const void* pos_b, const void* frc, T* grid, cudaStream_t s)
@@ -190,8 +266,8 @@ void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int nc
     int blocks = (ncap + kSpreadWarps - 1) / kSpreadWarps;
     const int* ntot = src_offsets + ninst;
     if (sizeof(T) == 4)
-        k_spread<T, float4, float4><<<blocks, kSpreadWarps * 32, 0, s>>>(
-            inst, ntot, (const float4*)pos_a, (const float4*)pos_b, (const float4*)frc, grid);
+        k_spread_f4<<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const float4*)pos_a, (const float4*)pos_b,
+                                                         (const float4*)frc, (float*)grid);
     else
         k_spread<T, Dbl4, Dbl4><<<blocks, kSpreadWarps * 32, 0, s>>>(
             inst, ntot, (const Dbl4*)pos_a, (const Dbl4*)pos_b, (const Dbl4*)frc, grid);
@@ -205,8 +281,8 @@ void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int nc
     int blocks = (ncap + kSpreadWarps - 1) / kSpreadWarps;
     const int* ntot = tgt_offsets + ninst;
     if (sizeof(T) == 4)
-        k_gather<T, float4><<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const float4*)pos_a,
-                                                                   (const float4*)pos_b, grid, u_k);
+        k_gather_f4<<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const float4*)pos_a, (const float4*)pos_b,
+                                                         (const float*)grid, (float*)u_k);
     else
         k_gather<T, Dbl4><<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const Dbl4*)pos_a,
                                                                     (const Dbl4*)pos_b, grid, u_k);
@@ -308,10 +384,18 @@ void fill_twiddles(const int* M, bool fp64, void* host_buf)
     for (int k = 0; k <= Nh; k++) put(o.r + k, -2 * kPiD * k / M[2]);
 }
 
+// Planar FP64 grids keep four planes per instance (three components and an
+// unused one): grid line of spectrum line L = ((3 b + c) xy + rest).
+__device__ __forceinline__ size_t plane_line(long long L, long long xy)
+{
+    long long v = L / xy, rest = L - v * xy, b = v / 3, c = v - 3 * b;
+    return (size_t)((4 * b + c) * xy + rest);
+}
+
 // z pass, forward: real lines of length Mz -> Nh+1 complex (packed half-length FFT).
 template <class T>
 __global__ void k_fft_z_fwd(const T* __restrict__ grid, typename Cx<T>::t* __restrict__ spec, long long nlines, int Mz,
-                            int lpb, const typename Cx<T>::t* __restrict__ tw, TwOff o)
+                            int lpb, const typename Cx<T>::t* __restrict__ tw, TwOff o, long long xy)
 {
     typedef typename Cx<T>::t T2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -322,7 +406,7 @@ __global__ void k_fft_z_fwd(const T* __restrict__ grid, typename Cx<T>::t* __res
     int nl = (int)min((long long)lpb, nlines - l0);
     for (int idx = threadIdx.x; idx < nl * Nh; idx += blockDim.x) {
         int l = idx / Nh, i = idx - l * Nh;
-        const T2* src = (const T2*)(grid + (size_t)(l0 + l) * Mz);
+        const T2* src = (const T2*)(grid + plane_line(l0 + l, xy) * Mz);
         A[l * Nh + i] = src[i];
     }
     __syncthreads();
@@ -349,7 +433,7 @@ __global__ void k_fft_z_fwd(const T* __restrict__ grid, typename Cx<T>::t* __res
 // z pass, inverse: Nh+1 complex -> real line of length Mz.
 template <class T>
 __global__ void k_fft_z_inv(const typename Cx<T>::t* __restrict__ spec, T* __restrict__ grid, long long nlines, int Mz,
-                            int lpb, const typename Cx<T>::t* __restrict__ tw, TwOff o)
+                            int lpb, const typename Cx<T>::t* __restrict__ tw, TwOff o, long long xy)
 {
     typedef typename Cx<T>::t T2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -381,8 +465,85 @@ __global__ void k_fft_z_inv(const typename Cx<T>::t* __restrict__ spec, T* __res
     T2* R = (Nh > 1) ? stockham<T2>(A, B, Nh, nl, Nh, 1, tw + o.zh, true, false) : A;
     for (int idx = threadIdx.x; idx < nl * Nh; idx += blockDim.x) {
         int l = idx / Nh, i = idx - l * Nh;
-        T2* dst = (T2*)(grid + (size_t)(l0 + l) * Mz);
+        T2* dst = (T2*)(grid + plane_line(l0 + l, xy) * Mz);
         dst[i] = R[l * Nh + i];
+    }
+}
+
+// z passes for FP32 grids with interleaved components (float4 per point):
+// one grid line (instance, x, y) gives the three spectrum lines of its components.
+__global__ void k_fft_z_fwd4(const float4* __restrict__ grid, float2* __restrict__ spec, long long nlines, int Mx,
+                             int My, int Mz, int lpb, const float2* __restrict__ tw, TwOff o)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* A = (float2*)smem_raw;
+    const int Nh = Mz / 2, Mzh = Nh + 1;
+    float2* B = A + 3 * lpb * Nh;
+    long long l0 = (long long)blockIdx.x * lpb;
+    int nl = (int)min((long long)lpb, nlines - l0);
+    for (int idx = threadIdx.x; idx < nl * Nh; idx += blockDim.x) {
+        int l = idx / Nh, i = idx - l * Nh;
+        const float4* src = grid + (size_t)(l0 + l) * Mz;
+        float4 a = src[2 * i], b = src[2 * i + 1];
+        A[(3 * l + 0) * Nh + i] = make_float2(a.x, b.x);
+        A[(3 * l + 1) * Nh + i] = make_float2(a.y, b.y);
+        A[(3 * l + 2) * Nh + i] = make_float2(a.z, b.z);
+    }
+    __syncthreads();
+    float2* R = (Nh > 1) ? stockham<float2>(A, B, Nh, 3 * nl, Nh, 1, tw + o.zh, false, false) : A;
+    const float2* rt = tw + o.r;
+    const long long xy = (long long)Mx * My;
+    for (int idx = threadIdx.x; idx < 3 * nl * Mzh; idx += blockDim.x) {
+        int lc = idx / Mzh, k = idx - lc * Mzh;
+        int l = lc / 3, c = lc - 3 * l;
+        float2 zk = R[lc * Nh + (k == Nh ? 0 : k)];
+        float2 zm = R[lc * Nh + (k == 0 ? 0 : Nh - k)];
+        float2 E, Od;
+        E.x = 0.5f * (zk.x + zm.x);
+        E.y = 0.5f * (zk.y - zm.y);
+        Od.x = 0.5f * (zk.y + zm.y);
+        Od.y = -0.5f * (zk.x - zm.x);
+        float2 wo = cmul(rt[k], Od);
+        long long line = l0 + l, bi = line / xy, rest = line - bi * xy;
+        spec[((size_t)(3 * bi + c) * xy + rest) * Mzh + k] = make_float2(E.x + wo.x, E.y + wo.y);
+    }
+}
+
+__global__ void k_fft_z_inv4(const float2* __restrict__ spec, float4* __restrict__ grid, long long nlines, int Mx,
+                             int My, int Mz, int lpb, const float2* __restrict__ tw, TwOff o)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* A = (float2*)smem_raw;
+    const int Nh = Mz / 2, Mzh = Nh + 1;
+    float2* B = A + 3 * lpb * Nh;
+    const float2* rt = tw + o.r;
+    long long l0 = (long long)blockIdx.x * lpb;
+    int nl = (int)min((long long)lpb, nlines - l0);
+    const long long xy = (long long)Mx * My;
+    for (int idx = threadIdx.x; idx < 3 * nl * Nh; idx += blockDim.x) {
+        int lc = idx / Nh, k = idx - lc * Nh;
+        int l = lc / 3, c = lc - 3 * l;
+        long long line = l0 + l, bi = line / xy, rest = line - bi * xy;
+        const float2* src = spec + ((size_t)(3 * bi + c) * xy + rest) * Mzh;
+        float2 xk = src[k], xm = src[Nh - k];
+        float2 e, dlt;
+        e.x = xk.x + xm.x;
+        e.y = xk.y - xm.y;
+        dlt.x = xk.x - xm.x;
+        dlt.y = xk.y + xm.y;
+        float2 wc = rt[k];
+        wc.y = -wc.y;
+        float2 od = cmul(wc, dlt);
+        A[lc * Nh + k] = make_float2(e.x - od.y, e.y + od.x);
+    }
+    __syncthreads();
+    float2* R = (Nh > 1) ? stockham<float2>(A, B, Nh, 3 * nl, Nh, 1, tw + o.zh, true, false) : A;
+    for (int idx = threadIdx.x; idx < nl * Nh; idx += blockDim.x) {
+        int l = idx / Nh, i = idx - l * Nh;
+        float2 u0 = R[(3 * l) * Nh + i], u1 = R[(3 * l + 1) * Nh + i], u2 = R[(3 * l + 2) * Nh + i];
+        float4* dst = grid + (size_t)(l0 + l) * Mz;
+        dst[2 * i] = make_float4(u0.x, u1.x, u2.x, 0.f);
+        dst[2 * i + 1] = make_float4(u0.y, u1.y, u2.y, 0.f);
     }
 }
 
@@ -516,8 +677,19 @@ void launch_kspace_fft(const PbInst* inst_dev, const int* bucket_inst, int nb, l
     int lpb = (int)(2048 / (Nh > 0 ? Nh : 1));
     if (lpb < 1) lpb = 1;
     size_t sm = (size_t)2 * lpb * Nh * cs;
-    cudaFuncSetAttribute(k_fft_z_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_z_fwd<T><<<(unsigned)((nlines + lpb - 1) / lpb), 256, sm, s>>>(grid, spec, nlines, Mz, lpb, tw, o);
+    // FP32: interleaved float4 grid lines, three components per line
+    long long nlines4 = (long long)nb * Mx * My;
+    int lpb4 = std::max(1, lpb / 3);
+    size_t sm4 = (size_t)2 * 3 * lpb4 * Nh * cs;
+    if (sizeof(T) == 4) {
+        cudaFuncSetAttribute(k_fft_z_fwd4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+        k_fft_z_fwd4<<<(unsigned)((nlines4 + lpb4 - 1) / lpb4), 256, sm4, s>>>(
+            (const float4*)grid, (float2*)spec, nlines4, Mx, My, Mz, lpb4, (const float2*)tw, o);
+    } else {
+        cudaFuncSetAttribute(k_fft_z_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_fft_z_fwd<T><<<(unsigned)((nlines + lpb - 1) / lpb), 256, sm, s>>>(grid, spec, nlines, Mz, lpb, tw, o,
+                                                                              (long long)Mx * My);
+    }
     // y forward
     int twy = pick_tw(My, 1, cs, smax);
     size_t smy = (size_t)2 * twy * My * cs;
@@ -534,8 +706,15 @@ void launch_kspace_fft(const PbInst* inst_dev, const int* bucket_inst, int nb, l
     // y inverse
     k_fft_y<T><<<(unsigned)nby, 256, smy, s>>>(spec, nvol, Mx, My, Mzh, twy, tw, o.y, true);
     // z inverse
-    cudaFuncSetAttribute(k_fft_z_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_z_inv<T><<<(unsigned)((nlines + lpb - 1) / lpb), 256, sm, s>>>(spec, grid, nlines, Mz, lpb, tw, o);
+    if (sizeof(T) == 4) {
+        cudaFuncSetAttribute(k_fft_z_inv4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+        k_fft_z_inv4<<<(unsigned)((nlines4 + lpb4 - 1) / lpb4), 256, sm4, s>>>(
+            (const float2*)spec, (float4*)grid, nlines4, Mx, My, Mz, lpb4, (const float2*)tw, o);
+    } else {
+        cudaFuncSetAttribute(k_fft_z_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_fft_z_inv<T><<<(unsigned)((nlines + lpb - 1) / lpb), 256, sm, s>>>(spec, grid, nlines, Mz, lpb, tw, o,
+                                                                              (long long)Mx * My);
+    }
 }
 
 template void launch_kspace_fft<float>(const PbInst*, const int*, int, long long, const int*, float*, void*,
@@ -644,331 +823,5 @@ void launch_force_sums(const double* frc, const int* offsets, int ninst, double*
     if (ninst <= 0) return;
     k_force_sums<<<ninst, 256, 0, s>>>(frc, offsets, ninst, out);
 }
-
-}  // namespace pb
-
-// ---------------------------------------------------------------------------
-// Tiled spreading and gathering
-// ---------------------------------------------------------------------------
-// A tile is a block of ublk^3 real-space cells; its particles are contiguous
-// z-runs of the cell-sorted arrays.  The union of their Gaussian windows is a
-// small box of the grid held in shared memory: spreading accumulates every
-// particle into it with plain read-modify-writes (the whole block works on one
-// particle at a time, each thread on distinct points) and adds the box to the
-// global grid once; gathering loads the box once and every warp interpolates
-// its targets from shared memory.
-namespace pb {
-
-constexpr int kTileThreads = 512;
-
-template <class T>
-struct TileCap {
-    static constexpr int points = sizeof(T) == 4 ? 10648 : 5832;  // 22^3 / 18^3 points, three components
-};
-
-struct TileGeom {
-    int q, c0[3], c1[3];  // instance, cell range [c0, c1) per axis
-    int lo[3], R[3];      // grid box origin (unwrapped) and size
-};
-
-__device__ __forceinline__ void tile_geom(const PbInst* __restrict__ inst, const int* __restrict__ unit_off, int ninst,
-                                          int u, TileGeom& G)
-{
-    int q = find_instance(unit_off, ninst, u);
-    const PbInst& I = inst[q];
-    int local = u - unit_off[q];
-    int uz = local % I.nu[2];
-    int r = local / I.nu[2];
-    int uy = r % I.nu[1], ux = r / I.nu[1];
-    int uu[3] = {ux, uy, uz};
-    G.q = q;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        G.c0[a] = uu[a] * I.ublk;
-        G.c1[a] = min(G.c0[a] + I.ublk, I.nc[a]);
-        double s = I.h[a] / I.gh[a];
-        int f0 = (int)floor(G.c0[a] * s), f1 = (int)floor(G.c1[a] * s);
-        G.lo[a] = f0 - I.Pa[a] / 2;  // one point of margin below the lowest window start
-        G.R[a] = (f1 + I.Pa[a] / 2 + 1) - G.lo[a] + 1;
-    }
-}
-
-template <class T, class PV, class FV>
-__global__ void __launch_bounds__(kTileThreads)
-    k_spread_tiles(const PbInst* __restrict__ inst, int ninst, const int* __restrict__ unit_off,
-                   const int* __restrict__ cstart, const PV* __restrict__ pa, const PV* __restrict__ pb,
-                   const FV* __restrict__ frc, T* __restrict__ grid)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* reg = (T*)smem_raw;
-    __shared__ T wts[3][kMaxP];
-    __shared__ int wst[3];
-    __shared__ T fsh[3];
-    __shared__ int inbox;
-    const int total = unit_off[ninst];
-    for (int u = blockIdx.x; u < total; u += gridDim.x) {
-        TileGeom G;
-        tile_geom(inst, unit_off, ninst, u, G);
-        const PbInst& I = inst[G.q];
-        const int R = G.R[0] * G.R[1] * G.R[2];
-        // any particles in the tile?
-        int cnt = 0;
-        for (int cx = G.c0[0]; cx < G.c1[0]; cx++)
-            for (int cy = G.c0[1]; cy < G.c1[1]; cy++) {
-                int row = I.cell_off + (cx * I.nc[1] + cy) * I.nc[2];
-                cnt += cstart[row + G.c1[2]] - cstart[row + G.c0[2]];
-            }
-        if (cnt == 0) continue;
-        const bool boxed = R <= TileCap<T>::points;
-        if (boxed)
-            for (int i = threadIdx.x; i < 3 * R; i += blockDim.x) reg[i] = (T)0;
-        __syncthreads();
-        const size_t comp = (size_t)I.M[0] * I.M[1] * I.M[2];
-        T* g0 = grid + I.grid_off;
-        const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
-        for (int cx = G.c0[0]; cx < G.c1[0]; cx++)
-            for (int cy = G.c0[1]; cy < G.c1[1]; cy++) {
-                int row = I.cell_off + (cx * I.nc[1] + cy) * I.nc[2];
-                int b = cstart[row + G.c0[2]], e = cstart[row + G.c1[2]];
-                for (int s = b; s < e; s++) {
-                    if (threadIdx.x < 3 * 32) {
-                        int a = threadIdx.x >> 5, p = threadIdx.x & 31;
-                        double x[3];
-                        int qq;
-                        load_pos(pa, pb, s, x, qq);
-                        if (p < I.Pa[a]) {
-                            double h = I.gh[a];
-                            int gs = (int)floor(x[a] / h) - I.Pa[a] / 2 + 1;
-                            T dx = (T)(x[a] - (double)(gs + p) * h);
-                            wts[a][p] = exp(-dx * dx / (T)I.eta);
-                            if (p == 0) wst[a] = gs - G.lo[a];
-                        }
-                        if (threadIdx.x == 0) {
-                            double fv[3];
-                            load_frc(frc, s, fv);
-                            fsh[0] = (T)fv[0];
-                            fsh[1] = (T)fv[1];
-                            fsh[2] = (T)fv[2];
-                        }
-                    }
-                    __syncthreads();
-                    if (threadIdx.x == 0)
-                        inbox = boxed && wst[0] >= 0 && wst[1] >= 0 && wst[2] >= 0 && wst[0] + I.Pa[0] <= G.R[0] &&
-                                wst[1] + Py <= G.R[1] && wst[2] + Pz <= G.R[2];
-                    __syncthreads();
-                    const T f0 = fsh[0], f1 = fsh[1], f2 = fsh[2];
-                    if (inbox) {
-                        for (int id = threadIdx.x; id < P3; id += blockDim.x) {
-                            int px = id / P2, rr = id - px * P2, py = rr / Pz, pz = rr - py * Pz;
-                            T wv = wts[0][px] * wts[1][py] * wts[2][pz];
-                            int ri = ((wst[0] + px) * G.R[1] + wst[1] + py) * G.R[2] + wst[2] + pz;
-                            reg[ri] += f0 * wv;
-                            reg[R + ri] += f1 * wv;
-                            reg[2 * R + ri] += f2 * wv;
-                        }
-                    } else {  // window outside the box (or box too large): straight to the grid
-                        for (int id = threadIdx.x; id < P3; id += blockDim.x) {
-                            int px = id / P2, rr = id - px * P2, py = rr / Pz, pz = rr - py * Pz;
-                            T wv = wts[0][px] * wts[1][py] * wts[2][pz];
-                            int gx = (G.lo[0] + wst[0] + px) % I.M[0], gy = (G.lo[1] + wst[1] + py) % I.M[1],
-                                gz = (G.lo[2] + wst[2] + pz) % I.M[2];
-                            gx += gx < 0 ? I.M[0] : 0;
-                            gy += gy < 0 ? I.M[1] : 0;
-                            gz += gz < 0 ? I.M[2] : 0;
-                            size_t o = ((size_t)gx * I.M[1] + gy) * I.M[2] + gz;
-                            atomicAdd(g0 + o, f0 * wv);
-                            atomicAdd(g0 + comp + o, f1 * wv);
-                            atomicAdd(g0 + 2 * comp + o, f2 * wv);
-                        }
-                    }
-                    __syncthreads();
-                }
-            }
-        if (boxed) {
-            for (int i = threadIdx.x; i < R; i += blockDim.x) {
-                int iz = i % G.R[2], r2 = i / G.R[2], iy = r2 % G.R[1], ix = r2 / G.R[1];
-                int gx = (G.lo[0] + ix) % I.M[0], gy = (G.lo[1] + iy) % I.M[1], gz = (G.lo[2] + iz) % I.M[2];
-                gx += gx < 0 ? I.M[0] : 0;
-                gy += gy < 0 ? I.M[1] : 0;
-                gz += gz < 0 ? I.M[2] : 0;
-                size_t o = ((size_t)gx * I.M[1] + gy) * I.M[2] + gz;
-                T v0 = reg[i], v1 = reg[R + i], v2 = reg[2 * R + i];
-                if (v0 != (T)0) atomicAdd(g0 + o, v0);
-                if (v1 != (T)0) atomicAdd(g0 + comp + o, v1);
-                if (v2 != (T)0) atomicAdd(g0 + 2 * comp + o, v2);
-            }
-        }
-        __syncthreads();
-    }
-}
-
-template <class T, class PV>
-__global__ void __launch_bounds__(kTileThreads)
-    k_gather_tiles(const PbInst* __restrict__ inst, int ninst, const int* __restrict__ unit_off,
-                   const int* __restrict__ cstart, const PV* __restrict__ pa, const PV* __restrict__ pb,
-                   const T* __restrict__ grid, T* __restrict__ u_k)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* reg = (T*)smem_raw;
-    constexpr int NW = kTileThreads / 32;
-    __shared__ T wts[NW][3][kMaxP];
-    __shared__ int wst[NW][3];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int total = unit_off[ninst];
-    for (int u = blockIdx.x; u < total; u += gridDim.x) {
-        TileGeom G;
-        tile_geom(inst, unit_off, ninst, u, G);
-        const PbInst& I = inst[G.q];
-        const int R = G.R[0] * G.R[1] * G.R[2];
-        int cnt = 0;
-        for (int cx = G.c0[0]; cx < G.c1[0]; cx++)
-            for (int cy = G.c0[1]; cy < G.c1[1]; cy++) {
-                int row = I.cell_off + (cx * I.nc[1] + cy) * I.nc[2];
-                cnt += cstart[row + G.c1[2]] - cstart[row + G.c0[2]];
-            }
-        if (cnt == 0) continue;
-        const bool boxed = R <= TileCap<T>::points;
-        const size_t comp = (size_t)I.M[0] * I.M[1] * I.M[2];
-        const T* g0 = grid + I.grid_off;
-        if (boxed)
-            for (int i = threadIdx.x; i < R; i += blockDim.x) {
-                int iz = i % G.R[2], r2 = i / G.R[2], iy = r2 % G.R[1], ix = r2 / G.R[1];
-                int gx = (G.lo[0] + ix) % I.M[0], gy = (G.lo[1] + iy) % I.M[1], gz = (G.lo[2] + iz) % I.M[2];
-                gx += gx < 0 ? I.M[0] : 0;
-                gy += gy < 0 ? I.M[1] : 0;
-                gz += gz < 0 ? I.M[2] : 0;
-                size_t o = ((size_t)gx * I.M[1] + gy) * I.M[2] + gz;
-                reg[i] = g0[o];
-                reg[R + i] = g0[comp + o];
-                reg[2 * R + i] = g0[2 * comp + o];
-            }
-        __syncthreads();
-        const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
-        // the tile's targets, one warp each
-        int k = 0;
-        for (int cx = G.c0[0]; cx < G.c1[0]; cx++)
-            for (int cy = G.c0[1]; cy < G.c1[1]; cy++) {
-                int row = I.cell_off + (cx * I.nc[1] + cy) * I.nc[2];
-                int b = cstart[row + G.c0[2]], e = cstart[row + G.c1[2]];
-                for (int s = b; s < e; s++, k++) {
-                    if ((k % NW) != w) continue;
-                    double x[3];
-                    int qq;
-                    load_pos(pa, pb, s, x, qq);
-#pragma unroll
-                    for (int a = 0; a < 3; a++) {
-                        if (lane < I.Pa[a]) {
-                            double h = I.gh[a];
-                            int gs = (int)floor(x[a] / h) - I.Pa[a] / 2 + 1;
-                            T dx = (T)(x[a] - (double)(gs + lane) * h);
-                            wts[w][a][lane] = exp(-dx * dx / (T)I.eta);
-                            if (lane == 0) wst[w][a] = gs - G.lo[a];
-                        }
-                    }
-                    __syncwarp();
-                    const bool inbox = boxed && wst[w][0] >= 0 && wst[w][1] >= 0 && wst[w][2] >= 0 &&
-                                       wst[w][0] + I.Pa[0] <= G.R[0] && wst[w][1] + Py <= G.R[1] &&
-                                       wst[w][2] + Pz <= G.R[2];
-                    T s0 = 0, s1 = 0, s2 = 0, e0 = 0, e1 = 0, e2 = 0;
-                    for (int id = lane; id < P3; id += 32) {
-                        int px = id / P2, rr = id - px * P2, py = rr / Pz, pz = rr - py * Pz;
-                        T wv = wts[w][0][px] * wts[w][1][py] * wts[w][2][pz];
-                        T v0, v1, v2;
-                        if (inbox) {
-                            int ri = ((wst[w][0] + px) * G.R[1] + wst[w][1] + py) * G.R[2] + wst[w][2] + pz;
-                            v0 = reg[ri];
-                            v1 = reg[R + ri];
-                            v2 = reg[2 * R + ri];
-                        } else {
-                            int gx = (G.lo[0] + wst[w][0] + px) % I.M[0], gy = (G.lo[1] + wst[w][1] + py) % I.M[1],
-                                gz = (G.lo[2] + wst[w][2] + pz) % I.M[2];
-                            gx += gx < 0 ? I.M[0] : 0;
-                            gy += gy < 0 ? I.M[1] : 0;
-                            gz += gz < 0 ? I.M[2] : 0;
-                            size_t o = ((size_t)gx * I.M[1] + gy) * I.M[2] + gz;
-                            v0 = g0[o];
-                            v1 = g0[comp + o];
-                            v2 = g0[2 * comp + o];
-                        }
-                        T y = wv * v0 - e0, t = s0 + y;
-                        e0 = (t - s0) - y;
-                        s0 = t;
-                        y = wv * v1 - e1;
-                        t = s1 + y;
-                        e1 = (t - s1) - y;
-                        s1 = t;
-                        y = wv * v2 - e2;
-                        t = s2 + y;
-                        e2 = (t - s2) - y;
-                        s2 = t;
-                    }
-                    s0 -= e0;
-                    s1 -= e1;
-                    s2 -= e2;
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        s0 += __shfl_xor_sync(kFull, s0, o);
-                        s1 += __shfl_xor_sync(kFull, s1, o);
-                        s2 += __shfl_xor_sync(kFull, s2, o);
-                    }
-                    if (lane == 0) {
-                        u_k[3 * (size_t)s] = s0;
-                        u_k[3 * (size_t)s + 1] = s1;
-                        u_k[3 * (size_t)s + 2] = s2;
-                    }
-                    __syncwarp();
-                }
-            }
-        __syncthreads();
-    }
-}
-
-int tile_edge_points(bool fp64) { return fp64 ? 18 : 22; }
-
-template <class T>
-void launch_spread_tiles(const PbInst* inst, int ninst, const int* unit_off, int ucap, const int* cstart,
-                         const void* pos_a, const void* pos_b, const void* frc, T* grid, int nsm, cudaStream_t s)
-{
-    if (ucap <= 0) return;
-    size_t smem = (size_t)3 * TileCap<T>::points * sizeof(T);
-    int blocks = std::min(ucap, nsm);
-    if (sizeof(T) == 4) {
-        cudaFuncSetAttribute(k_spread_tiles<T, float4, float4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_spread_tiles<T, float4, float4><<<blocks, kTileThreads, smem, s>>>(
-            inst, ninst, unit_off, cstart, (const float4*)pos_a, (const float4*)pos_b, (const float4*)frc, grid);
-    } else {
-        cudaFuncSetAttribute(k_spread_tiles<T, Dbl4, Dbl4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_spread_tiles<T, Dbl4, Dbl4><<<blocks, kTileThreads, smem, s>>>(
-            inst, ninst, unit_off, cstart, (const Dbl4*)pos_a, (const Dbl4*)pos_b, (const Dbl4*)frc, grid);
-    }
-}
-
-template <class T>
-void launch_gather_tiles(const PbInst* inst, int ninst, const int* unit_off, int ucap, const int* cstart,
-                         const void* pos_a, const void* pos_b, const T* grid, T* u_k, int nsm, cudaStream_t s)
-{
-    if (ucap <= 0) return;
-    size_t smem = (size_t)3 * TileCap<T>::points * sizeof(T);
-    int blocks = std::min(ucap, nsm);
-    if (sizeof(T) == 4) {
-        cudaFuncSetAttribute(k_gather_tiles<T, float4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_gather_tiles<T, float4><<<blocks, kTileThreads, smem, s>>>(inst, ninst, unit_off, cstart,
-                                                                      (const float4*)pos_a, (const float4*)pos_b, grid,
-                                                                      u_k);
-    } else {
-        cudaFuncSetAttribute(k_gather_tiles<T, Dbl4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_gather_tiles<T, Dbl4><<<blocks, kTileThreads, smem, s>>>(inst, ninst, unit_off, cstart, (const Dbl4*)pos_a,
-                                                                     (const Dbl4*)pos_b, grid, u_k);
-    }
-}
-
-template void launch_spread_tiles<float>(const PbInst*, int, const int*, int, const int*, const void*, const void*,
-                                         const void*, float*, int, cudaStream_t);
-template void launch_spread_tiles<double>(const PbInst*, int, const int*, int, const int*, const void*, const void*,
-                                          const void*, double*, int, cudaStream_t);
-template void launch_gather_tiles<float>(const PbInst*, int, const int*, int, const int*, const void*, const void*,
-                                         const float*, float*, int, cudaStream_t);
-template void launch_gather_tiles<double>(const PbInst*, int, const int*, int, const int*, const void*, const void*,
-                                          const double*, double*, int, cudaStream_t);
 
 }  // namespace pb

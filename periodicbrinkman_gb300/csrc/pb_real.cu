@@ -1,10 +1,11 @@
 // Real-space Ewald sum over a device-built cell list.
 //
-// Work item = (instance, target cell, chunk of <= 32 targets), one warp per
-// item, items pulled from a global counter by a persistent grid.  Each lane
-// owns one target.  The sources of the (2S+1)^3 stencil are visited as
-// contiguous z-runs of the cell-sorted source array, staged 32 at a time in
-// shared memory.  Mixed precision: each lane classifies its 32 candidate
+// Work item = (instance, cell row (c0, c1), z-range [za, zb] of at most 8
+// cells, up to 32 consecutive sorted targets), one warp per item, items pulled
+// from a global counter by a persistent grid.  Each lane owns one target.  The
+// sources of the stencil (rows c0 +- S, c1 +- S; cells za - S .. zb + S) are
+// visited as contiguous z-runs of the cell-sorted source array, staged 32 at a
+// time in shared memory.  Mixed precision: each lane classifies its 32 candidate
 // pairs (inside the cutoff / inside the blob region / below r_tiny), the warp
 // compacts them into target-major queues in shared memory, and every lane then
 // evaluates one queued pair at a time, so the FMA pipe sees full warps and the
@@ -28,22 +29,76 @@ namespace pb {
 
 constexpr int kRealWarps = 4;
 
+constexpr int kMaxReach = 15;  // stencil reach S per axis
+constexpr int kZTab = 8 + 2 * kMaxReach;
+
+// item = {instance, first target, local row c0*nc1 + c1, count | za << 8 | zb << 16}
 struct ItemFrame {
-    int q, c0, c1, c2;
+    int q, c0, c1, za, zb, first, count;
     double O[3];
 };
 
 __device__ __forceinline__ void item_frame(const PbInst& I, int4 it, ItemFrame& F)
 {
-    int local = it.y - I.cell_off;
     F.q = it.x;
-    F.c2 = local % I.nc[2];
-    int r = local / I.nc[2];
-    F.c1 = r % I.nc[1];
-    F.c0 = r / I.nc[1];
+    F.first = it.y;
+    F.c0 = it.z / I.nc[1];
+    F.c1 = it.z % I.nc[1];
+    F.count = it.w & 0xff;
+    F.za = (it.w >> 8) & 0xff;
+    F.zb = (it.w >> 16) & 0xff;
     F.O[0] = F.c0 * I.h[0];
     F.O[1] = F.c1 * I.h[1];
-    F.O[2] = F.c2 * I.h[2];
+    F.O[2] = F.za * I.h[2];
+}
+
+// Per-item frame tables: for every stencil offset along an axis, the wrapped
+// cell index, whether the image shift is zero, and Q = O - shift as an FP32
+// hi/lo pair, so the inner loops need no FP64.
+struct __align__(8) FrameTabs {
+    float2 qx[2 * kMaxReach + 1], qy[2 * kMaxReach + 1], qz[kZTab];
+    int wx[2 * kMaxReach + 1], wy[2 * kMaxReach + 1], wz[kZTab];
+    int zx[2 * kMaxReach + 1], zy[2 * kMaxReach + 1], zz[kZTab];
+};
+
+__device__ __forceinline__ void fill_frame_tabs(const PbInst& I, const ItemFrame& F, FrameTabs& T, int lane)
+{
+    const int nx = 2 * I.S[0] + 1, ny = 2 * I.S[1] + 1, nz = F.zb - F.za + 2 * I.S[2] + 1;
+    for (int i = lane; i < nx + ny + nz; i += 32) {
+        int ax, g, k;
+        if (i < nx) {
+            ax = 0;
+            k = i;
+            g = F.c0 + i - I.S[0];
+        } else if (i < nx + ny) {
+            ax = 1;
+            k = i - nx;
+            g = F.c1 + k - I.S[1];
+        } else {
+            ax = 2;
+            k = i - nx - ny;
+            g = F.za + k - I.S[2];
+        }
+        const int n = I.nc[ax];
+        int w = ((g % n) + n) % n;
+        int sc = (g - w) / n;  // image shift count
+        double Q = F.O[ax] - (double)sc * I.L[ax];
+        float hi, lo;
+        split_double(Q, hi, lo);
+        if (ax == 0) {
+            T.qx[k] = make_float2(hi, lo);
+            T.wx[k] = w;
+            T.zx[k] = sc == 0;
+        } else if (ax == 1) {
+            T.qy[k] = make_float2(hi, lo);
+            T.wy[k] = w;
+            T.zy[k] = sc == 0;
+        } else {
+            T.qz[k] = make_float2(hi, lo);
+            T.wz[k] = w;
+            T.zz[k] = sc == 0;
+        }
+    }
 }
 
 template <int NP>
@@ -70,6 +125,7 @@ struct __align__(16) RealWarpSmem {
     double acc64[3][32];                 // per-target FP64 sums of series pairs
     unsigned short q[3][1024];           // pair queues (t << 5 | j): screened, blob region, series
     float te1[kMaxPoly], te2[kMaxPoly];  // blob polynomials of the current instance
+    FrameTabs ft;                        // the current item's frame tables
 };
 
 // Warp-wide exclusive prefix sum (64-bit, three packed 16-bit counters).
@@ -160,8 +216,9 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
         }
         ItemFrame F;
         item_frame(I, it, F);
-        const bool active = lane < it.w;
-        const int tidx = it.z + (active ? lane : 0);
+        fill_frame_tabs(I, F, S.ft, lane);
+        const bool active = lane < F.count;
+        const int tidx = F.first + (active ? lane : 0);
         const int self_src = I.same ? tidx - I.tgt_off + I.src_off : -1;
         float th[3], tl[3];
         {
@@ -178,31 +235,27 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
         }
         S.t_hi[lane] = make_float4(th[0], th[1], th[2], 0.f);
         S.t_lo[lane] = make_float4(tl[0], tl[1], tl[2], 0.f);
+        __syncwarp();
         float s0 = 0, s1 = 0, s2 = 0, k0 = 0, k1 = 0, k2 = 0;
+        const int nzt = F.zb - F.za + 2 * I.S[2] + 1;
 
-        for (int o0 = -I.S[0]; o0 <= I.S[0]; o0++) {
-            int g0 = F.c0 + o0;
-            int w0 = ((g0 % I.nc[0]) + I.nc[0]) % I.nc[0];
-            double sh0 = (double)((g0 - w0) / I.nc[0]) * I.L[0];
-            for (int o1 = -I.S[1]; o1 <= I.S[1]; o1++) {
-                int g1 = F.c1 + o1;
-                int w1 = ((g1 % I.nc[1]) + I.nc[1]) % I.nc[1];
-                double sh1 = (double)((g1 - w1) / I.nc[1]) * I.L[1];
-                int row = I.cell_off + (w0 * I.nc[1] + w1) * I.nc[2];
-                int g2 = F.c2 - I.S[2];
-                const int g2end = F.c2 + I.S[2];
-                while (g2 <= g2end) {
-                    // maximal run of unwrapped z cells sharing one image shift
-                    int w2 = ((g2 % I.nc[2]) + I.nc[2]) % I.nc[2];
-                    int run = min(g2end - g2 + 1, I.nc[2] - w2);
-                    double sh2 = (double)((g2 - w2) / I.nc[2]) * I.L[2];
-                    int b = src_start[row + w2], e = src_start[row + w2 + run];
-                    g2 += run;
-                    const bool zero_shift = (sh0 == 0.0) && (sh1 == 0.0) && (sh2 == 0.0);
-                    float qh[3], ql[3];
-                    split_double(F.O[0] - sh0, qh[0], ql[0]);
-                    split_double(F.O[1] - sh1, qh[1], ql[1]);
-                    split_double(F.O[2] - sh2, qh[2], ql[2]);
+        for (int i0 = 0; i0 <= 2 * I.S[0]; i0++) {
+            const float2 qx = S.ft.qx[i0];
+            const int w0 = S.ft.wx[i0], z0 = S.ft.zx[i0];
+            for (int i1 = 0; i1 <= 2 * I.S[1]; i1++) {
+                const float2 qy = S.ft.qy[i1];
+                const int w1 = S.ft.wy[i1], z1 = S.ft.zy[i1];
+                const int row = I.cell_off + (w0 * I.nc[1] + w1) * I.nc[2];
+                int i2 = 0;
+                while (i2 < nzt) {
+                    // maximal run of z cells sharing one image shift (contiguous wrapped cells)
+                    const int w2 = S.ft.wz[i2];
+                    const int run = min(nzt - i2, I.nc[2] - w2);
+                    const float2 qz = S.ft.qz[i2];
+                    const bool zero_shift = z0 && z1 && S.ft.zz[i2];
+                    const int b = src_start[row + w2], e = src_start[row + w2 + run];
+                    i2 += run;
+                    const float qh[3] = {qx.x, qy.x, qz.x}, ql[3] = {qx.y, qy.y, qz.y};
                     for (int base = b; base < e; base += 32) {
                         const int j = base + lane;
                         const int ncand = min(32, e - base);
@@ -436,10 +489,11 @@ __global__ void __launch_bounds__(kRealWarps * 32)
         const double rs2 = (double)T.rs2;
         ItemFrame F;
         item_frame(I, it, F);
-        const bool active = lane < it.w;
-        const int tidx = it.z + (active ? lane : 0);
+        const bool active = lane < F.count;
+        const int tidx = F.first + (active ? lane : 0);
         const int self_src = I.same ? tidx - I.tgt_off + I.src_off : -1;
         Dbl4 tp = tpos[tidx];
+        if (!active) tp.x = tp.y = tp.z = 3.0e300;  // inactive lanes pair with nothing
         double v0 = 0, v1 = 0, v2 = 0;
         for (int o0 = -I.S[0]; o0 <= I.S[0]; o0++) {
             int g0 = F.c0 + o0;
@@ -450,8 +504,8 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                 int w1 = ((g1 % I.nc[1]) + I.nc[1]) % I.nc[1];
                 double sh1 = (double)((g1 - w1) / I.nc[1]) * I.L[1];
                 int row = I.cell_off + (w0 * I.nc[1] + w1) * I.nc[2];
-                int g2 = F.c2 - I.S[2];
-                const int g2end = F.c2 + I.S[2];
+                int g2 = F.za - I.S[2];
+                const int g2end = F.zb + I.S[2];
                 while (g2 <= g2end) {
                     int w2 = ((g2 % I.nc[2]) + I.nc[2]) % I.nc[2];
                     int run = min(g2end - g2 + 1, I.nc[2] - w2);

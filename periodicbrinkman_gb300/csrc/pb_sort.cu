@@ -217,40 +217,81 @@ void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, 
     k_prepare_fp64<<<(ncap + 255) / 256, 256, 0, s>>>(pos, frc, perm, offsets, inst, ninst, pos_out, frc_out);
 }
 
-__global__ void k_count_chunks(const int* __restrict__ start, int ncell, int* __restrict__ chunks)
+// Work items of the real-space kernel: each cell row (c0, c1) of an instance
+// is walked along z and cut into items of <= 32 consecutive targets spanning
+// <= 8 cells (a cell with more than 32 targets gives items of its own).  One
+// thread per row start; counts first, then emission after a scan.
+template <bool EMIT>
+__device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q, int rowl, int4* items, int k0,
+                         int& nitems)
 {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    int n = start[c + 1] - start[c];
-    chunks[c] = (n + 31) >> 5;
-}
-
-void launch_count_chunks(const int* start, int ncell_tot, int* chunks, cudaStream_t s)
-{
-    if (ncell_tot <= 0) return;
-    k_count_chunks<<<(ncell_tot + 255) / 256, 256, 0, s>>>(start, ncell_tot, chunks);
-}
-
-__global__ void k_emit_items(const int* __restrict__ start, const int* __restrict__ chunk_start, int ncell,
-                             const int* __restrict__ cell_offsets, int ninst, int4* __restrict__ items)
-{
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    int b = start[c], n = start[c + 1] - b;
-    if (n == 0) return;
-    int q = find_instance(cell_offsets, ninst, c);
-    int k0 = chunk_start[c];
-    for (int k = 0; k * 32 < n; k++) {
-        int cnt = min(32, n - 32 * k);
-        items[k0 + k] = make_int4(q, c, b + 32 * k, cnt);
+    int z = 0, k = 0;
+    while (z < nz) {
+        int n = start[row0 + z + 1] - start[row0 + z];
+        if (n == 0) {
+            z++;
+            continue;
+        }
+        if (n > 32) {
+            int b = start[row0 + z];
+            for (int c = 0; c * 32 < n; c++, k++)
+                if (EMIT) items[k0 + k] = make_int4(q, b + 32 * c, rowl, min(32, n - 32 * c) | (z << 8) | (z << 16));
+            z++;
+            continue;
+        }
+        int za = z, tot = 0;
+        while (z < nz && z - za < 8) {
+            int m = start[row0 + z + 1] - start[row0 + z];
+            if (tot + m > 32) break;
+            tot += m;
+            z++;
+        }
+        if (EMIT) items[k0 + k] = make_int4(q, start[row0 + za], rowl, tot | (za << 8) | ((z - 1) << 16));
+        k++;
     }
+    nitems = k;
 }
 
-void launch_emit_items(const int* start, const int* chunk_start, int ncell_tot, const int* cell_offsets, int ninst,
-                       int4* items, cudaStream_t s)
+__global__ void k_count_items(const int* __restrict__ start, int ncell, const int* __restrict__ cell_offsets,
+                              const PbInst* __restrict__ inst, int ninst, int* __restrict__ counts)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    int q = find_instance(cell_offsets, ninst, c);
+    const PbInst& I = inst[q];
+    int local = c - I.cell_off;
+    int n = 0;
+    if (local < I.ncell && local % I.nc[2] == 0) walk_row<false>(start, c, I.nc[2], q, local / I.nc[2], nullptr, 0, n);
+    counts[c] = n;
+}
+
+__global__ void k_emit_items(const int* __restrict__ start, const int* __restrict__ item_start, int ncell,
+                             const int* __restrict__ cell_offsets, const PbInst* __restrict__ inst, int ninst,
+                             int4* __restrict__ items)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    int q = find_instance(cell_offsets, ninst, c);
+    const PbInst& I = inst[q];
+    int local = c - I.cell_off;
+    int n = 0;
+    if (local < I.ncell && local % I.nc[2] == 0)
+        walk_row<true>(start, c, I.nc[2], q, local / I.nc[2], items, item_start[c], n);
+}
+
+void launch_count_items(const int* start, int ncell_tot, const int* cell_offsets, const PbInst* inst, int ninst,
+                        int* counts, cudaStream_t s)
 {
     if (ncell_tot <= 0) return;
-    k_emit_items<<<(ncell_tot + 255) / 256, 256, 0, s>>>(start, chunk_start, ncell_tot, cell_offsets, ninst, items);
+    k_count_items<<<(ncell_tot + 255) / 256, 256, 0, s>>>(start, ncell_tot, cell_offsets, inst, ninst, counts);
+}
+
+void launch_emit_items(const int* start, const int* item_start, int ncell_tot, const int* cell_offsets,
+                       const PbInst* inst, int ninst, int4* items, cudaStream_t s)
+{
+    if (ncell_tot <= 0) return;
+    k_emit_items<<<(ncell_tot + 255) / 256, 256, 0, s>>>(start, item_start, ncell_tot, cell_offsets, inst, ninst,
+                                                          items);
 }
 
 }  // namespace pb

@@ -61,15 +61,13 @@ struct PbInst {
     int n_src, n_tgt;
     int src_off, tgt_off;     // offsets into the packed particle arrays
     int cell_off, ncell;      // offset into the packed cell arrays
-    long long grid_off;       // offset (real elements) of component 0 of the real grid
+    long long grid_off;       // offset (real elements) of the instance's grid (4 values per point:
+                              // FP32 interleaved xyz+pad, FP64 three planes + an unused one)
     long long spec_off;       // offset (complex elements) of component 0 of the spectrum
     int flags;
     int same;                 // targets are the sources
     int bucket;               // FFT size bucket
-    int ublk;                 // cells per edge of a spreading tile (0: per-particle spreading)
-    int nu[3];                // spreading tiles per axis
-    int unit_off;             // first spreading tile of the instance
-    int pad2;
+    int pad;
 };
 
 }  // namespace pb
