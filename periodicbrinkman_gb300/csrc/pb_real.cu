@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                             float dx = th[0] - p.x, dy = th[1] - p.y, dz = th[2] - p.z;
                             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                             unsigned in = r2 < rc2, nb = r2 < rs2, ns = (r2 < rtiny2) | (r2 == 0.f);
-                            mn |= (in & (nb ^ 1u)) << jj;
+                            mn |= (in & ((nb | ns) ^ 1u)) << jj;  // eps = 0: no blob region, r = 0 is series
                             mb |= (nb & (ns ^ 1u)) << jj;
                             ms |= ns << jj;
                         }
