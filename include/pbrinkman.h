@@ -121,6 +121,24 @@ int pb_fft_brinkman(double* U, const double* y, int m_tgt, const double* f, cons
                     const double* L, const int* M, const int* P, int msd, int C, double e, double tol, double d,
                     double alpha);
 
+/* No counterpart in the reference.  pb_fft_brinkman's k-space velocities for
+ * callers that cannot allocate device memory: code that runs where
+ * cudaMalloc/cudaFree would block or synchronise the device (a real-time
+ * loop), or a host program whose device memory is all owned by its own pool.
+ * Same arguments and results as pb_fft_brinkman, minus C and tol, but U, y,
+ * f and xn are DEVICE pointers and the work is queued on `stream` (NULL =
+ * legacy default stream) without a synchronise.  Allocates nothing: all
+ * intermediates live in one fixed array of 21.2 MB (20.2 MiB) compiled into the
+ * library, which every GPU that loads the library holds until the process
+ * exits.  Limits: M[a] <= 64, n <= 65536, m_tgt <= 65536; larger sizes return
+ * PB_ERR_UNSUPPORTED.  The first call on a device looks up the array's
+ * device address for that device (make it before any stream capture).  All
+ * calls share the array, so calls that overlap on the GPU race: serialise
+ * them on one stream. */
+int pb_fft_brinkman_static(double* U, const double* y, int m_tgt, const double* f, const double* xn, int n,
+                           const double* L, const int* M, const int* P, int msd, double e, double d, double alpha,
+                           void* stream);
+
 /* ---- evaluator ----------------------------------------------------------- */
 
 /* One-shot solve.  x, f: 3 x n_src; y: 3 x n_tgt (NULL when n_tgt == 0);

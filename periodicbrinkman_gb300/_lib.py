@@ -149,6 +149,8 @@ def lib():
                                           dp, C.c_int, vp]
     L.pb_fft_brinkman.argtypes = [dp, dp, C.c_int, dp, dp, C.c_int, dp, ip, ip, C.c_int, C.c_int, C.c_double,
                                   C.c_double, C.c_double, C.c_double]
+    L.pb_fft_brinkman_static.argtypes = [vp, vp, C.c_int, vp, vp, C.c_int, dp, ip, ip, C.c_int, C.c_double,
+                                         C.c_double, C.c_double, vp]
     L.pb_solve.argtypes = [C.POINTER(SolveParams), vp, vp, vp, vp, C.c_int, vp]
     L.pb_plan_create.argtypes = [C.POINTER(SolveParams), C.c_int, C.POINTER(vp)]
     L.pb_plan_execute.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp]

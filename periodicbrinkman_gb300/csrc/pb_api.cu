@@ -447,11 +447,10 @@ size_t plan_layout(pb_plan_s* P, bool assign)
     return L.off;
 }
 
-// Per-instance descriptor and tables (grid_off/spec_off/bucket are kept).
-int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved& R, int src_off, int tgt_off,
-                  int cell_off, int max_terms)
+// Per-instance descriptor fields from the resolved parameters
+// (grid_off/spec_off/bucket are kept).
+void set_inst_fields(PbInst& I, const pb_solve_params& p, const Resolved& R, int src_off, int tgt_off, int cell_off)
 {
-    PbInst& I = P->hinst[q];
     for (int a = 0; a < 3; a++) {
         I.L[a] = p.L[a];
         I.h[a] = R.h[a];
@@ -478,6 +477,13 @@ int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved&
     I.ncell = R.nc[0] * R.nc[1] * R.nc[2];
     I.flags = R.flags;
     I.same = R.same;
+}
+
+// Per-instance descriptor and tables (grid_off/spec_off/bucket are kept).
+int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved& R, int src_off, int tgt_off,
+                  int cell_off, int max_terms)
+{
+    set_inst_fields(P->hinst[q], p, R, src_off, tgt_off, cell_off);
     int trc = build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, &P->htab[q], max_terms);
     if (trc) return fail(PB_ERR_INVALID, "table construction failed");
     return PB_OK;
@@ -894,8 +900,21 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
     return PB_OK;
 }
 
-namespace {
-}  // namespace
+namespace pb {
+
+int api_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
+int kspace_instance(const pb_solve_params& p, PbInst* inst)
+{
+    Resolved R;
+    int rc = resolve(p, R);
+    if (rc) return rc;
+    std::memset(inst, 0, sizeof(PbInst));
+    set_inst_fields(*inst, p, R, 0, 0, 0);
+    return PB_OK;
+}
+
+}  // namespace pb
 
 extern "C" {
 
