@@ -76,6 +76,11 @@ __device__ __forceinline__ void load_frc(const Dbl4* f, int i, double* v)
 constexpr int kSpreadWarps = 8;
 constexpr int kMaxP = 32;
 
+// Lanes own positions of the y-z plane of the window (and, for windows with
+// fewer than 32 y-z points, a residue class of x) and loop over x, so the
+// inner loops carry no index division.  `xs` = first x of the lane, `R` = x step.
+__device__ __forceinline__ int window_lanes(int Py, int Pz) { return Py * Pz >= 32 ? 1 : 32 / (Py * Pz); }
+
 // Per-axis Gaussian weights exp(-(x - (g0+p) h)^2 / eta) and wrapped grid
 // indices of the P-point window centred on x (lane p computes entry p).
 template <class T>
@@ -115,17 +120,21 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const PbInst& I = inst[q];
     window<T>(I, x, lane, wgt[w], gidx[w]);
     __syncwarp();
-    const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
-    const size_t comp = (size_t)I.M[0] * I.M[1] * I.M[2];
+    const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
+    const size_t comp = (size_t)I.M[0] * I.M[1] * I.M[2], M12 = (size_t)I.M[1] * I.M[2];
     T* g0 = grid + I.grid_off;
-    const T f0 = (T)fv[0], f1 = (T)fv[1], f2 = (T)fv[2];
-    for (int id = lane; id < P3; id += 32) {
-        int px = id / P2, r = id - px * P2, py = r / Pz, pz = r - py * Pz;
-        T wv = wgt[w][0][px] * wgt[w][1][py] * wgt[w][2][pz];
-        size_t o = ((size_t)gidx[w][0][px] * I.M[1] + gidx[w][1][py]) * I.M[2] + gidx[w][2][pz];
-        atomicAdd(g0 + o, f0 * wv);
-        atomicAdd(g0 + comp + o, f1 * wv);
-        atomicAdd(g0 + 2 * comp + o, f2 * wv);
+    for (int id = lane; id < P2 * R; id += 32) {
+        const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
+        const T wyz = wgt[w][1][py] * wgt[w][2][pz];
+        const T h0 = (T)fv[0] * wyz, h1 = (T)fv[1] * wyz, h2 = (T)fv[2] * wyz;
+        const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
+        for (int px = xs; px < Px; px += R) {
+            const T wx = wgt[w][0][px];
+            const size_t o = (size_t)gidx[w][0][px] * M12 + oyz;
+            atomicAdd(g0 + o, h0 * wx);
+            atomicAdd(g0 + comp + o, h1 * wx);
+            atomicAdd(g0 + 2 * comp + o, h2 * wx);
+        }
     }
 }
 
@@ -146,27 +155,31 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const PbInst& I = inst[q];
     window<T>(I, x, lane, wgt[w], gidx[w]);
     __syncwarp();
-    const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
-    const size_t comp = (size_t)I.M[0] * I.M[1] * I.M[2];
+    const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
+    const size_t comp = (size_t)I.M[0] * I.M[1] * I.M[2], M12 = (size_t)I.M[1] * I.M[2];
     const T* g0 = grid + I.grid_off;
     T s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0;
-    for (int id = lane; id < P3; id += 32) {
-        int px = id / P2, r = id - px * P2, py = r / Pz, pz = r - py * Pz;
-        T wv = wgt[w][0][px] * wgt[w][1][py] * wgt[w][2][pz];
-        size_t o = ((size_t)gidx[w][0][px] * I.M[1] + gidx[w][1][py]) * I.M[2] + gidx[w][2][pz];
-        T v0 = wv * __ldg(g0 + o), v1 = wv * __ldg(g0 + comp + o), v2 = wv * __ldg(g0 + 2 * comp + o);
-        // Kahan: running value s - c
-        T y = v0 - c0, t = s0 + y;
-        c0 = (t - s0) - y;
-        s0 = t;
-        y = v1 - c1;
-        t = s1 + y;
-        c1 = (t - s1) - y;
-        s1 = t;
-        y = v2 - c2;
-        t = s2 + y;
-        c2 = (t - s2) - y;
-        s2 = t;
+    for (int id = lane; id < P2 * R; id += 32) {
+        const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
+        const T wyz = wgt[w][1][py] * wgt[w][2][pz];
+        const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
+        for (int px = xs; px < Px; px += R) {
+            const T wv = wgt[w][0][px] * wyz;
+            const size_t o = (size_t)gidx[w][0][px] * M12 + oyz;
+            T v0 = wv * __ldg(g0 + o), v1 = wv * __ldg(g0 + comp + o), v2 = wv * __ldg(g0 + 2 * comp + o);
+            // Kahan: running value s - c
+            T y = v0 - c0, t = s0 + y;
+            c0 = (t - s0) - y;
+            s0 = t;
+            y = v1 - c1;
+            t = s1 + y;
+            c1 = (t - s1) - y;
+            s1 = t;
+            y = v2 - c2;
+            t = s2 + y;
+            c2 = (t - s2) - y;
+            s2 = t;
+        }
     }
     s0 -= c0;
     s1 -= c1;
@@ -203,14 +216,18 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const PbInst& I = inst[q];
     window<float>(I, x, lane, wgt[w], gidx[w]);
     __syncwarp();
-    const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
+    const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
+    const size_t M12 = (size_t)I.M[1] * I.M[2];
     float4* g4 = reinterpret_cast<float4*>(grid + I.grid_off);
-    const float f0 = (float)fv[0], f1 = (float)fv[1], f2 = (float)fv[2];
-    for (int id = lane; id < P3; id += 32) {
-        int px = id / P2, r = id - px * P2, py = r / Pz, pz = r - py * Pz;
-        float wv = wgt[w][0][px] * wgt[w][1][py] * wgt[w][2][pz];
-        size_t o = ((size_t)gidx[w][0][px] * I.M[1] + gidx[w][1][py]) * I.M[2] + gidx[w][2][pz];
-        atomicAdd(g4 + o, make_float4(f0 * wv, f1 * wv, f2 * wv, 0.f));
+    for (int id = lane; id < P2 * R; id += 32) {
+        const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
+        const float wyz = wgt[w][1][py] * wgt[w][2][pz];
+        const float h0 = (float)fv[0] * wyz, h1 = (float)fv[1] * wyz, h2 = (float)fv[2] * wyz;
+        const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
+        for (int px = xs; px < Px; px += R) {
+            const float wx = wgt[w][0][px];
+            atomicAdd(g4 + (size_t)gidx[w][0][px] * M12 + oyz, make_float4(h0 * wx, h1 * wx, h2 * wx, 0.f));
+        }
     }
 }
 
@@ -230,17 +247,21 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const PbInst& I = inst[q];
     window<float>(I, x, lane, wgt[w], gidx[w]);
     __syncwarp();
-    const int Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, P3 = I.Pa[0] * P2;
+    const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
+    const size_t M12 = (size_t)I.M[1] * I.M[2];
     const float4* g4 = reinterpret_cast<const float4*>(grid + I.grid_off);
     float s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0;
-    for (int id = lane; id < P3; id += 32) {
-        int px = id / P2, r = id - px * P2, py = r / Pz, pz = r - py * Pz;
-        float wv = wgt[w][0][px] * wgt[w][1][py] * wgt[w][2][pz];
-        size_t o = ((size_t)gidx[w][0][px] * I.M[1] + gidx[w][1][py]) * I.M[2] + gidx[w][2][pz];
-        float4 v = __ldg(g4 + o);
-        kahan_add(s0, c0, wv * v.x);
-        kahan_add(s1, c1, wv * v.y);
-        kahan_add(s2, c2, wv * v.z);
+    for (int id = lane; id < P2 * R; id += 32) {
+        const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
+        const float wyz = wgt[w][1][py] * wgt[w][2][pz];
+        const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
+        for (int px = xs; px < Px; px += R) {
+            const float wv = wgt[w][0][px] * wyz;
+            const float4 v = __ldg(g4 + (size_t)gidx[w][0][px] * M12 + oyz);
+            kahan_add(s0, c0, wv * v.x);
+            kahan_add(s1, c1, wv * v.y);
+            kahan_add(s2, c2, wv * v.z);
+        }
     }
     s0 -= c0;
     s1 -= c1;

@@ -101,12 +101,14 @@ __device__ __forceinline__ void fill_frame_tabs(const PbInst& I, const ItemFrame
     }
 }
 
+// Both polynomials (T1, T2) of one argument in packed FP32x2 FMAs.
 template <int NP>
-__device__ __forceinline__ float horner(const float (&c)[NP], float t)
+__device__ __forceinline__ float2 horner2(const float2 (&c)[NP], float t)
 {
-    float h = c[NP - 1];
+    const float2 tt = make_float2(t, t);
+    float2 h = c[NP - 1];
 #pragma unroll
-    for (int k = NP - 2; k >= 0; k--) h = fmaf(h, t, c[k]);
+    for (int k = NP - 2; k >= 0; k--) h = __ffma2_rn(h, tt, c[k]);
     return h;
 }
 
@@ -121,10 +123,11 @@ __device__ __forceinline__ float horner_g(const float* __restrict__ c, int n, fl
 struct __align__(16) RealWarpSmem {
     float4 s_hi[32], s_lo[32], s_f[32];  // staged sources: frame-relative hi, lo; force
     float4 t_hi[32], t_lo[32];           // the item's targets: frame-relative hi, lo
+    float c_x[32], c_y[32], c_z[32];     // staged sources, hi parts by axis (classification)
     float acc[3][32];                    // per-target partial sums of the current chunk
     double acc64[3][32];                 // per-target FP64 sums of series pairs
     unsigned short q[3][1024];           // pair queues (t << 5 | j): screened, blob region, series
-    float te1[kMaxPoly], te2[kMaxPoly];  // blob polynomials of the current instance
+    float2 te[kMaxPoly];                 // blob polynomials (T1, T2) of the current instance
     FrameTabs ft;                        // the current item's frame tables
 };
 
@@ -176,9 +179,9 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
     const unsigned lt = (1u << lane) - 1u;
 
     const int nitems = *nitems_ptr;
-    float c1[NP], c2[NP];
+    float2 c12[NP];
     int cur_q = -1;
-    float tds = 0, tdo = 0, rc2 = 0, rs2 = 0, rtiny2 = 0, tes = 0, teo = 0;
+    float tds = 0, tdo = 0, rc2 = 0, rare2 = 0, rtiny2 = 0, tes = 0, teo = 0;
     int ne = 1;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
@@ -197,22 +200,17 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
         if (it.x != cur_q) {
             cur_q = it.x;
 #pragma unroll
-            for (int k = 0; k < NP; k++) {
-                c1[k] = T.pd1[k];
-                c2[k] = T.pd2[k];
-            }
+            for (int k = 0; k < NP; k++) c12[k] = make_float2(T.pd1[k], T.pd2[k]);
             tds = T.td_scale;
             tdo = T.td_off;
             rc2 = T.rc2;
-            rs2 = T.rs2;
+            // rare pairs: the blob region (eps > 0), else coincident points only
+            rare2 = T.blob ? T.rs2 : 1.17549435e-38f;
             rtiny2 = T.rtiny2f;
             tes = T.te_scale;
             teo = T.te_off;
             ne = T.ne > 0 ? T.ne : 1;
-            if (lane < kMaxPoly) {
-                S.te1[lane] = T.pe1[lane];
-                S.te2[lane] = T.pe2[lane];
-            }
+            if (lane < kMaxPoly) S.te[lane] = make_float2(T.pe1[lane], T.pe2[lane]);
         }
         ItemFrame F;
         item_frame(I, it, F);
@@ -273,18 +271,45 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                             S.s_hi[lane] = make_float4(p3[0], p3[1], p3[2], 0.f);
                             S.s_lo[lane] = make_float4(l3[0], l3[1], l3[2], 0.f);
                             S.s_f[lane] = sfrc[j];
+                            S.c_x[lane] = p3[0];
+                            S.c_y[lane] = p3[1];
+                            S.c_z[lane] = p3[2];
+                        } else {  // padding: far from every target, active (finite) or not (+3e30)
+                            S.c_x[lane] = -3.0e30f;
+                            S.c_y[lane] = -3.0e30f;
+                            S.c_z[lane] = -3.0e30f;
                         }
                         __syncwarp();
                         // classify candidate pairs of this lane's target: screened / blob region / series
-                        unsigned mn = 0, mb = 0, ms = 0;
-                        for (int jj = 0; jj < ncand; jj++) {
+                        // (two candidates per packed FP32x2 operation; padded to 32)
+                        unsigned mi = 0, mr = 0;
+                        {
+                            const float2 ntx = make_float2(-th[0], -th[0]), nty = make_float2(-th[1], -th[1]),
+                                         ntz = make_float2(-th[2], -th[2]);
+#pragma unroll
+                            for (int jj = 0; jj < 32; jj += 2) {
+                                const float2 dx = __fadd2_rn(*reinterpret_cast<const float2*>(&S.c_x[jj]), ntx);
+                                const float2 dy = __fadd2_rn(*reinterpret_cast<const float2*>(&S.c_y[jj]), nty);
+                                const float2 dz = __fadd2_rn(*reinterpret_cast<const float2*>(&S.c_z[jj]), ntz);
+                                float2 r2 = __fmul2_rn(dx, dx);
+                                r2 = __ffma2_rn(dy, dy, r2);
+                                r2 = __ffma2_rn(dz, dz, r2);
+                                if (r2.x < rc2) mi |= 1u << jj;
+                                if (r2.y < rc2) mi |= 2u << jj;
+                                if (r2.x < rare2) mr |= 1u << jj;
+                                if (r2.y < rare2) mr |= 2u << jj;
+                            }
+                        }
+                        unsigned mn = mi & ~mr, mb = 0, ms = 0;
+                        for (unsigned m = mr; m; m &= m - 1) {  // rare: blob region or series
+                            const int jj = __ffs(m) - 1;
                             float4 p = S.s_hi[jj];
                             float dx = th[0] - p.x, dy = th[1] - p.y, dz = th[2] - p.z;
                             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                            unsigned in = r2 < rc2, nb = r2 < rs2, ns = (r2 < rtiny2) | (r2 == 0.f);
-                            mn |= (in & ((nb | ns) ^ 1u)) << jj;  // eps = 0: no blob region, r = 0 is series
-                            mb |= (nb & (ns ^ 1u)) << jj;
-                            ms |= ns << jj;
+                            if ((r2 < rtiny2) | (r2 == 0.f))
+                                ms |= 1u << jj;
+                            else
+                                mb |= 1u << jj;
                         }
                         if (zero_shift && self_src >= base && self_src < base + ncand)
                             ms &= ~(1u << (self_src - base));  // self pair: added in FP64 by the combine kernel
@@ -318,14 +343,18 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                         }
                         __syncwarp();
                         const int nn = (int)(tot & 0xffff), nbq = (int)((tot >> 16) & 0xffff), nsq = (int)(tot >> 32);
-                        // screened pairs: T(r) polynomial of S - R_d only
-                        for (int e0 = 0; e0 < nn; e0 += 32) {
-                            const int ei = e0 + lane;
-                            float v0 = 0, v1 = 0, v2 = 0;
-                            int key = -1 - lane;
-                            if (ei < nn) {
+                        // screened pairs: T(r) polynomial of S - R_d only.  Lane l takes the
+                        // contiguous block [l K, (l+1) K) of the target-major queue and sums
+                        // runs of one target in registers: a target that starts inside the
+                        // block is added by this lane alone; the block's first target (which
+                        // may continue from earlier lanes) goes through one segmented reduction.
+                        {
+                            const int K = (nn + 31) >> 5;
+                            const int eb = min(lane * K, nn), ee = min(eb + K, nn);
+                            int cur = -1, first = -1;
+                            float a0 = 0, a1 = 0, a2 = 0, f0 = 0, f1 = 0, f2 = 0;
+                            for (int ei = eb; ei < ee; ei++) {
                                 const int qv = S.q[0][ei], t = qv >> 5, jj = qv & 31;
-                                key = t;
                                 float4 p = S.s_hi[jj], pl = S.s_lo[jj], f = S.s_f[jj];
                                 float4 a = S.t_hi[t], al = S.t_lo[t];
                                 float dx = (a.x - p.x) + (al.x - pl.x);
@@ -335,15 +364,49 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                                 float ri = rsqrtf(r2);
                                 ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
                                 float r = r2 * ri;
-                                float tt = fmaf(r, tds, tdo);
-                                float T1 = horner<NP>(c1, tt), T2 = horner<NP>(c2, tt);
-                                float H1 = T1 * ri, H2 = T2 * (ri * ri * ri);
+                                const float2 T12 = horner2<NP>(c12, fmaf(r, tds, tdo));
+                                float H1 = T12.x * ri, H2 = T12.y * (ri * ri * ri);
                                 float g = H2 * fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
-                                v0 = fmaf(H1, f.x, g * dx);
-                                v1 = fmaf(H1, f.y, g * dy);
-                                v2 = fmaf(H1, f.z, g * dz);
+                                const float v0 = fmaf(H1, f.x, g * dx);
+                                const float v1 = fmaf(H1, f.y, g * dy);
+                                const float v2 = fmaf(H1, f.z, g * dz);
+                                if (t != cur) {
+                                    if (cur >= 0) {
+                                        if (first < 0) {
+                                            first = cur;
+                                            f0 = a0;
+                                            f1 = a1;
+                                            f2 = a2;
+                                        } else {
+                                            S.acc[0][cur] += a0;
+                                            S.acc[1][cur] += a1;
+                                            S.acc[2][cur] += a2;
+                                        }
+                                    }
+                                    cur = t;
+                                    a0 = v0;
+                                    a1 = v1;
+                                    a2 = v2;
+                                } else {
+                                    a0 += v0;
+                                    a1 += v1;
+                                    a2 += v2;
+                                }
                             }
-                            segment_reduce_add(v0, v1, v2, key, lane, S.acc);
+                            if (cur >= 0) {
+                                if (first < 0) {
+                                    first = cur;
+                                    f0 = a0;
+                                    f1 = a1;
+                                    f2 = a2;
+                                } else {
+                                    S.acc[0][cur] += a0;
+                                    S.acc[1][cur] += a1;
+                                    S.acc[2][cur] += a2;
+                                }
+                            }
+                            __syncwarp();
+                            if (nn > 0) segment_reduce_add(f0, f1, f2, first >= 0 ? first : -1 - lane, lane, S.acc);
                         }
                         // blob-region pairs: subtract the polynomial of S - R_eps
                         for (int e0 = 0; e0 < nbq; e0 += 32) {
@@ -362,15 +425,12 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                                 float ri = rsqrtf(r2);
                                 ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
                                 float r = r2 * ri;
-                                float tt = fmaf(r, tds, tdo);
-                                float T1 = horner<NP>(c1, tt), T2 = horner<NP>(c2, tt);
-                                float te = fmaf(r, tes, teo);
-                                float E1 = S.te1[ne - 1], E2 = S.te2[ne - 1];
-                                for (int k = ne - 2; k >= 0; k--) {
-                                    E1 = fmaf(E1, te, S.te1[k]);
-                                    E2 = fmaf(E2, te, S.te2[k]);
-                                }
-                                float H1 = (T1 - E1) * ri, H2 = (T2 - E2) * (ri * ri * ri);
+                                const float2 T12 = horner2<NP>(c12, fmaf(r, tds, tdo));
+                                const float te = fmaf(r, tes, teo);
+                                const float2 tt = make_float2(te, te);
+                                float2 E = S.te[ne - 1];
+                                for (int k = ne - 2; k >= 0; k--) E = __ffma2_rn(E, tt, S.te[k]);
+                                float H1 = (T12.x - E.x) * ri, H2 = (T12.y - E.y) * (ri * ri * ri);
                                 float g = H2 * fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
                                 v0 = fmaf(H1, f.x, g * dx);
                                 v1 = fmaf(H1, f.y, g * dy);
@@ -398,9 +458,9 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                                 } else {  // eps = 0, nearly coincident: singular kernel from the polynomial
                                     float r2f = (float)rr, ri = rsqrtf(r2f);
                                     ri = ri * fmaf(-0.5f * r2f * ri, ri, 1.5f);
-                                    float tt = fmaf(r2f * ri, tds, tdo);
-                                    H1 = (double)(horner<NP>(c1, tt) * ri);
-                                    H2 = (double)(horner<NP>(c2, tt) * (ri * ri * ri));
+                                    const float2 T12 = horner2<NP>(c12, fmaf(r2f * ri, tds, tdo));
+                                    H1 = (double)(T12.x * ri);
+                                    H2 = (double)(T12.y * (ri * ri * ri));
                                 }
                                 double fd = f.x * dx + f.y * dy + f.z * dz;
                                 atomicAdd(&S.acc64[0][t], H1 * f.x + H2 * fd * dx);
@@ -460,6 +520,8 @@ void launch_real_mixed(int npoly, const PbInst* inst, const PbTables* tab, const
         PB_LAUNCH_REAL(20);
     else if (npoly <= 24)
         PB_LAUNCH_REAL(24);
+    else if (npoly <= 26)
+        PB_LAUNCH_REAL(26);
     else
         PB_LAUNCH_REAL(28);
 #undef PB_LAUNCH_REAL
