@@ -752,7 +752,7 @@ int build_slot_host(const pb_slot_config* cfg, pb_plan_s* P)
     P->n_tgt = std::max(cfg->max_tgt, 1);
     P->n_y = P->n_tgt;
     P->ncell = cfg->max_cells;
-    P->npoly = P->npoly_cap = std::max(16, std::min(kMaxPoly, cfg->npoly > 0 ? cfg->npoly : 24));
+    P->npoly = P->npoly_cap = std::max(16, std::min(kMaxPoly, cfg->npoly > 0 ? cfg->npoly : 20));
     P->res.resize(B);
     P->hinst.resize(B);
     P->htab.resize(B);
@@ -1226,22 +1226,38 @@ int pb_debug_pair_kernel(double alpha, double d, double eps, double rc, int n, c
             continue;
         }
         float ri = 1.0f / rf;
-        float t = rf * T.td_scale + T.td_off;
-        float T1 = T.pd1[T.nd - 1], T2 = T.pd2[T.nd - 1];
-        for (int k = T.nd - 2; k >= 0; k--) {
-            T1 = std::fma(T1, t, T.pd1[k]);
-            T2 = std::fma(T2, t, T.pd2[k]);
-        }
-        if (r2 < T.rs2) {
-            float te = rf * T.te_scale + T.te_off;
-            float E1 = T.pe1[T.ne - 1], E2 = T.pe2[T.ne - 1];
-            for (int k = T.ne - 2; k >= 0; k--) {
-                E1 = std::fma(E1, te, T.pe1[k]);
-                E2 = std::fma(E2, te, T.pe2[k]);
+        auto poly = [&](const float* c1, const float* c2, int n, float t, float& p1, float& p2) {
+            p1 = c1[n - 1];
+            p2 = c2[n - 1];
+            for (int k = n - 2; k >= 0; k--) {
+                p1 = std::fma(p1, t, c1[k]);
+                p2 = std::fma(p2, t, c2[k]);
             }
-            T1 -= E1;
-            T2 -= E2;
+        };
+        auto cheb = [&](const float* c1, const float* c2, int n, float t, float& p1, float& p2) {
+            float a1 = 0, a2 = 0, b1 = 0, b2 = 0;  // Clenshaw, as the kernel does
+            for (int k = n - 1; k >= 1; k--) {
+                float n1 = std::fma(2.f * t, a1, c1[k] - b1), n2 = std::fma(2.f * t, a2, c2[k] - b2);
+                b1 = a1;
+                b2 = a2;
+                a1 = n1;
+                a2 = n2;
+            }
+            p1 = std::fma(t, a1, c1[0] - b1);
+            p2 = std::fma(t, a2, c2[0] - b2);
+        };
+        float T1, T2;
+        if (r2 < T.rs2) {  // blob piece: H itself
+            float h1, h2;
+            cheb(T.cb1, T.cb2, T.nb, std::fma(rf, T.tb_scale, T.tb_off), h1, h2);
+            H1[i] = h1;
+            H2[i] = h2 * (ri * ri);
+            continue;
         }
+        if (r2 < T.rm2)
+            cheb(T.cn1, T.cn2, T.nn, std::fma(rf, T.tn_scale, T.tn_off), T1, T2);
+        else
+            poly(T.pd1, T.pd2, T.nd, std::fma(rf, T.td_scale, T.td_off), T1, T2);
         H1[i] = T1 * ri;
         H2[i] = T2 * (ri * ri * ri);
     }

@@ -195,8 +195,8 @@ void scaled_diffH(double r, double a, double delta, const double* ser1, const do
     *T2 = r * r * r * h2;
 }
 
-std::vector<double> fit_monomial(const std::function<double(double)>& f, double lo, double hi, int nodes,
-                                 double rel_tol, int max_terms)
+std::vector<double> fit_chebyshev(const std::function<double(double)>& f, double lo, double hi, int nodes,
+                                  double rel_tol, int max_terms)
 {
     std::vector<double> v(nodes), c(nodes);
     for (int k = 0; k < nodes; k++) {
@@ -204,7 +204,7 @@ std::vector<double> fit_monomial(const std::function<double(double)>& f, double 
         v[k] = f(lo + (hi - lo) * (t + 1) / 2);
     }
     double cmax = 0;
-    std::vector<double> ct(2 * nodes * 2);
+    std::vector<double> ct(4 * nodes);
     for (int q = 0; q < 4 * nodes; q++) ct[q] = std::cos(kPi * q / (2.0 * nodes));  // cos(pi q / (2 nodes))
     for (int j = 0; j < nodes; j++) {
         double s = 0;
@@ -216,9 +216,17 @@ std::vector<double> fit_monomial(const std::function<double(double)>& f, double 
     int n = 1;
     for (int j = 0; j < nodes; j++)
         if (std::fabs(c[j]) > rel_tol * cmax) n = j + 1;
-    n = std::min(n, max_terms);
+    c.resize(std::min(n, max_terms));
+    return c;
+}
+
+std::vector<double> fit_monomial(const std::function<double(double)>& f, double lo, double hi, int nodes,
+                                 double rel_tol, int max_terms)
+{
+    std::vector<double> c = fit_chebyshev(f, lo, hi, nodes, rel_tol, max_terms);
+    const int n = (int)c.size();
     // Chebyshev -> monomial in t: T_{j+1} = 2 t T_j - T_{j-1}
-    std::vector<double> a(n, 0.0), Tm1(n, 0.0), T0(n, 0.0), T1(n, 0.0);
+    std::vector<double> a(n, 0.0), T0(n, 0.0), T1(n, 0.0);
     T0[0] = 1;
     if (n > 1) T1[1] = 1;
     for (int j = 0; j < n; j++) {
@@ -243,51 +251,80 @@ int build_tables(double a, double d, double eps, double rc, double poly_tol, PbT
     const int nser = 40;
     std::vector<double> sd1(nser), sd2(nser), se1(nser), se2(nser);
     regularized_series(a, d, nser, sd1.data(), sd2.data());
-    const int nodes = 40;
     auto Td1 = [&](double r) { double x, y; scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &x, &y); return x; };
     auto Td2 = [&](double r) { double x, y; scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &x, &y); return y; };
-    std::vector<double> p1 = fit_monomial(Td1, 0, rc, nodes, poly_tol, max_terms);
-    std::vector<double> p2 = fit_monomial(Td2, 0, rc, nodes, poly_tol, max_terms);
-    int nd = (int)std::max(p1.size(), p2.size());
-    p1.resize(nd, 0.0);
-    p2.resize(nd, 0.0);
-    for (int k = 0; k < nd; k++) {
-        t->pd1[k] = (float)p1[k];
-        t->pd2[k] = (float)p2[k];
+    // pieces: blob [0, rs], near [rs, r_mid], far [r_mid, rc]
+    const double rs = eps > 0 ? std::min(5.6 * eps, rc) : 0.0;
+    const double r_mid = std::min(rc, std::max(0.25 * rc, rs));
+    const double r_far = std::min(r_mid, 0.75 * rc);   // keeps the far interval non-degenerate
+    const double r_near = std::min(rs, 0.75 * r_mid);  // likewise for the near interval
+    auto scale_off = [](double lo, double hi, float* scale, float* off) {
+        *scale = (float)(2.0 / (hi - lo));
+        *off = (float)(-(hi + lo) / (hi - lo));
+    };
+    {
+        std::vector<double> p1 = fit_monomial(Td1, r_far, rc, 40, poly_tol, max_terms);
+        std::vector<double> p2 = fit_monomial(Td2, r_far, rc, 40, poly_tol, max_terms);
+        t->nd = (int)std::max(p1.size(), p2.size());
+        p1.resize(t->nd, 0.0);
+        p2.resize(t->nd, 0.0);
+        for (int k = 0; k < t->nd; k++) {
+            t->pd1[k] = (float)p1[k];
+            t->pd2[k] = (float)p2[k];
+        }
+        scale_off(r_far, rc, &t->td_scale, &t->td_off);
     }
-    t->nd = nd;
-    t->td_scale = (float)(2.0 / rc);
-    t->td_off = -1.0f;
+    auto cheb = [&](const std::function<double(double)>& f1, const std::function<double(double)>& f2, double lo,
+                    double hi, float* c1, float* c2, float* scale, float* off) {
+        std::vector<double> q1 = fit_chebyshev(f1, lo, hi, 64, poly_tol, kMaxCheb);
+        std::vector<double> q2 = fit_chebyshev(f2, lo, hi, 64, poly_tol, kMaxCheb);
+        int n = (int)std::max(q1.size(), q2.size());
+        q1.resize(n, 0.0);
+        q2.resize(n, 0.0);
+        for (int k = 0; k < n; k++) {
+            c1[k] = (float)q1[k];
+            c2[k] = (float)q2[k];
+        }
+        scale_off(lo, hi, scale, off);
+        return n;
+    };
+    t->nn = cheb(Td1, Td2, r_near, r_mid, t->cn1, t->cn2, &t->tn_scale, &t->tn_off);
     t->rc2 = (float)(rc * rc);
+    t->rm2 = (float)(r_mid * r_mid);
     if (eps > 0) {
         regularized_series(a, eps, nser, se1.data(), se2.data());
-        double rs = std::min(5.6 * eps, rc);
-        auto Te1 = [&](double r) { double x, y; scaled_diffH(r, a, eps, se1.data(), se2.data(), nser, &x, &y); return x; };
-        auto Te2 = [&](double r) { double x, y; scaled_diffH(r, a, eps, se1.data(), se2.data(), nser, &x, &y); return y; };
-        std::vector<double> q1 = fit_monomial(Te1, 0, rs, nodes, poly_tol, kMaxPoly);
-        std::vector<double> q2 = fit_monomial(Te2, 0, rs, nodes, poly_tol, kMaxPoly);
-        int ne = (int)std::max(q1.size(), q2.size());
-        q1.resize(ne, 0.0);
-        q2.resize(ne, 0.0);
-        for (int k = 0; k < ne; k++) {
-            t->pe1[k] = (float)q1[k];
-            t->pe2[k] = (float)q2[k];
+        for (int m = 0; m < kNumSeries; m++) {
+            t->ser1[m] = se1[m] - sd1[m];
+            t->ser2[m] = se2[m] - sd2[m];
         }
-        t->ne = ne;
-        t->te_scale = (float)(2.0 / rs);
-        t->te_off = -1.0f;
+        // R_eps - R_d: its series below eps/2, else the difference of the scaled
+        // forms (S cancels, mildly, at r >= eps/2)
+        auto HD = [&](double r, int which) {
+            if (r < 0.5 * eps) {
+                const double r2 = r * r;
+                double s = 0, p = 1;
+                for (int m = 0; m < nser; m++) {
+                    s += (which == 1 ? se1[m] - sd1[m] : se2[m] - sd2[m]) * p;
+                    p *= r2;
+                }
+                return s;
+            }
+            double d1, d2, e1, e2;
+            scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &d1, &d2);
+            scaled_diffH(r, a, eps, se1.data(), se2.data(), nser, &e1, &e2);
+            return which == 1 ? (d1 - e1) / r : (d2 - e2) / (r * r * r);
+        };
+        // H1 and r^2 H2 (the latter keeps the error of H2 r^2 uniform)
+        t->nb = cheb([&](double r) { return HD(r, 1); }, [&](double r) { return r * r * HD(r, 2); }, 0.0, rs, t->cb1,
+                     t->cb2, &t->tb_scale, &t->tb_off);
         t->rs2 = (float)(rs * rs);
         t->blob = 1;
         double rt = 0.8 * eps;
         t->rtiny2 = rt * rt;
         t->rtiny2f = (float)(rt * rt);
-        for (int m = 0; m < kNumSeries; m++) {
-            t->ser1[m] = se1[m] - sd1[m];
-            t->ser2[m] = se2[m] - sd2[m];
-        }
         t->self1 = t->ser1[0];
     } else {
-        t->ne = 0;
+        t->nb = 0;
         t->rs2 = 0;
         t->blob = 0;
         t->rtiny2 = 0;

@@ -1,11 +1,10 @@
 // Host-side FP64 mathematics of the regularized Brinkman kernel.
 //
 // Used by the plan builder to produce, once per instance (alpha, d, eps, rc):
-//   * FP32 polynomial tables of T1(r) = r*H1(r), T2(r) = r^3*H2(r) for the
-//     screened part S - R_d on [0, rc] and for the blob part S - R_eps on
-//     [0, rs], so that the real-space pair kernel is evaluated with FMAs only;
-//   * FP64 power series of R_eps - R_d in r^2, used below r_tiny where the
-//     difference of the two T-polynomials would cancel;
+//   * FP32 polynomial tables of the pair kernel by pieces (far, near, blob;
+//     see PbTables), so that it is evaluated with FMAs only and no piece is a
+//     difference of two large terms;
+//   * FP64 power series of R_eps - R_d in r^2, used below r_tiny;
 //   * the self coefficient R_eps(0) - R_d(0) (or -R_d(0) for eps = 0), the
 //     r -> 0 limit of cuda/periodicBrinkman.h:105-111.
 //
@@ -40,6 +39,11 @@ double phihat(double kn, double a, double d);
 // coefficients in t = (2 r - lo - hi)/(hi - lo) (lowest first).
 std::vector<double> fit_monomial(const std::function<double(double)>& f, double lo, double hi, int nodes,
                                  double rel_tol, int max_terms);
+
+// Chebyshev coefficients of f on [lo, hi] in t = (2 r - lo - hi)/(hi - lo),
+// truncated as fit_monomial does; f(r) = sum_k c[k] T_k(t).
+std::vector<double> fit_chebyshev(const std::function<double(double)>& f, double lo, double hi, int nodes,
+                                  double rel_tol, int max_terms);
 
 // Fill the per-instance real-space tables.  poly_tol: relative truncation of
 // the Chebyshev series (1e-9 keeps ~20 terms); max_terms caps the screened

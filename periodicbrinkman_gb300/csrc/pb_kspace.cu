@@ -76,6 +76,17 @@ __device__ __forceinline__ void load_frc(const Dbl4* f, int i, double* v)
 constexpr int kSpreadWarps = 8;
 constexpr int kMaxP = 32;
 
+// Spreading visits the cell-sorted points in an interleaved order (64 strands
+// through the sorted array), so warps in flight at the same time work on points
+// far apart and their atomics spread over the grid instead of piling onto the
+// same cache lines.  Returns -1 past the end.
+__device__ __forceinline__ int spread_order(int s, int ntot)
+{
+    const int R = (ntot + 63) >> 6;
+    const int p = (s & 63) * R + (s >> 6);
+    return (s < 64 * R && p < ntot) ? p : -1;
+}
+
 // Lanes own positions of the y-z plane of the window (and, for windows with
 // fewer than 32 y-z points, a residue class of x) and loop over x, so the
 // inner loops carry no index division.  `xs` = first x of the lane, `R` = x step.
@@ -111,8 +122,8 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     __shared__ T wgt[kSpreadWarps][3][kMaxP];
     __shared__ int gidx[kSpreadWarps][3][kMaxP];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int s = blockIdx.x * kSpreadWarps + w;
-    if (s >= ntot) return;
+    const int s = spread_order(blockIdx.x * kSpreadWarps + w, ntot);
+    if (s < 0) return;
     double x[3], fv[3];
     int q;
     load_pos(pa, pb, s, x, q);
@@ -207,8 +218,8 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     __shared__ int gidx[kSpreadWarps][3][kMaxP];
     const int ntot = *ntot_p;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int s = blockIdx.x * kSpreadWarps + w;
-    if (s >= ntot) return;
+    const int s = spread_order(blockIdx.x * kSpreadWarps + w, ntot);
+    if (s < 0) return;
     double x[3], fv[3];
     int q;
     load_pos(pa, pb, s, x, q);
@@ -284,7 +295,7 @@ void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int nc
                    const void* pos_b, const void* frc, T* grid, cudaStream_t s)
 {
     if (ncap <= 0) return;
-    int blocks = (ncap + kSpreadWarps - 1) / kSpreadWarps;
+    int blocks = (ncap + 63 + kSpreadWarps - 1) / kSpreadWarps;  // spread_order covers up to 64 R >= ntot
     const int* ntot = src_offsets + ninst;
     if (sizeof(T) == 4)
         k_spread_f4<<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const float4*)pos_a, (const float4*)pos_b,

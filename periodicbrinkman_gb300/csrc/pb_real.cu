@@ -112,6 +112,22 @@ __device__ __forceinline__ float2 horner2(const float2 (&c)[NP], float t)
     return h;
 }
 
+// Chebyshev series (two at once) by the Clenshaw recurrence; coefficients in
+// shared memory, the same for the whole warp.
+__device__ __forceinline__ float2 cheb2(const float2* __restrict__ c, int n, float t)
+{
+    const float2 t2 = make_float2(2.f * t, 2.f * t);
+    float2 b1 = make_float2(0.f, 0.f), b2 = b1;
+    for (int k = n - 1; k >= 1; k--) {
+        const float2 ck = c[k];
+        const float2 b0 = __ffma2_rn(t2, b1, make_float2(ck.x - b2.x, ck.y - b2.y));
+        b2 = b1;
+        b1 = b0;
+    }
+    const float2 c0 = c[0];
+    return __ffma2_rn(make_float2(t, t), b1, make_float2(c0.x - b2.x, c0.y - b2.y));
+}
+
 __device__ __forceinline__ float horner_g(const float* __restrict__ c, int n, float t)
 {
     float h = __ldg(&c[n - 1]);
@@ -127,7 +143,8 @@ struct __align__(16) RealWarpSmem {
     float acc[3][32];                    // per-target partial sums of the current chunk
     double acc64[3][32];                 // per-target FP64 sums of series pairs
     unsigned short q[3][1024];           // pair queues (t << 5 | j): screened, blob region, series
-    float2 te[kMaxPoly];                 // blob polynomials (T1, T2) of the current instance
+    float2 tn[kMaxCheb];                 // near piece (T1, T2) of the current instance
+    float2 tb[kMaxCheb];                 // blob piece (H1, r^2 H2) of the current instance
     FrameTabs ft;                        // the current item's frame tables
 };
 
@@ -181,8 +198,8 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
     const int nitems = *nitems_ptr;
     float2 c12[NP];
     int cur_q = -1;
-    float tds = 0, tdo = 0, rc2 = 0, rare2 = 0, rtiny2 = 0, tes = 0, teo = 0;
-    int ne = 1;
+    float tds = 0, tdo = 0, rc2 = 0, rare2 = 0, rtiny2 = 0, tbs = 0, tbo = 0, tns = 0, tno = 0, rs2 = 0;
+    int nbp = 1, nnp = 1;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         S.acc[c][lane] = 0.f;
@@ -205,12 +222,19 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
             tdo = T.td_off;
             rc2 = T.rc2;
             // rare pairs: the blob region (eps > 0), else coincident points only
-            rare2 = T.blob ? T.rs2 : 1.17549435e-38f;
+            rare2 = T.rm2;  // near piece (holds the blob region and r = 0)
+            rs2 = T.rs2;
+            tns = T.tn_scale;
+            tno = T.tn_off;
+            nnp = T.nn > 0 ? T.nn : 1;
             rtiny2 = T.rtiny2f;
-            tes = T.te_scale;
-            teo = T.te_off;
-            ne = T.ne > 0 ? T.ne : 1;
-            if (lane < kMaxPoly) S.te[lane] = make_float2(T.pe1[lane], T.pe2[lane]);
+            tbs = T.tb_scale;
+            tbo = T.tb_off;
+            nbp = T.nb > 0 ? T.nb : 1;
+            for (int k = lane; k < kMaxCheb; k += 32) {
+                S.tn[k] = make_float2(T.cn1[k], T.cn2[k]);
+                S.tb[k] = make_float2(T.cb1[k], T.cb2[k]);
+            }
         }
         ItemFrame F;
         item_frame(I, it, F);
@@ -408,7 +432,8 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                             __syncwarp();
                             if (nn > 0) segment_reduce_add(f0, f1, f2, first >= 0 ? first : -1 - lane, lane, S.acc);
                         }
-                        // blob-region pairs: subtract the polynomial of S - R_eps
+                        // near pairs (r < r_mid): the blob piece (R_eps - R_d itself) inside the
+                        // blob region, else the near piece of S - R_d
                         for (int e0 = 0; e0 < nbq; e0 += 32) {
                             const int ei = e0 + lane;
                             float v0 = 0, v1 = 0, v2 = 0;
@@ -425,12 +450,16 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                                 float ri = rsqrtf(r2);
                                 ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
                                 float r = r2 * ri;
-                                const float2 T12 = horner2<NP>(c12, fmaf(r, tds, tdo));
-                                const float te = fmaf(r, tes, teo);
-                                const float2 tt = make_float2(te, te);
-                                float2 E = S.te[ne - 1];
-                                for (int k = ne - 2; k >= 0; k--) E = __ffma2_rn(E, tt, S.te[k]);
-                                float H1 = (T12.x - E.x) * ri, H2 = (T12.y - E.y) * (ri * ri * ri);
+                                float H1, H2;
+                                if (r2 < rs2) {
+                                    const float2 h = cheb2(S.tb, nbp, fmaf(r, tbs, tbo));
+                                    H1 = h.x;
+                                    H2 = h.y * (ri * ri);
+                                } else {
+                                    const float2 T12 = cheb2(S.tn, nnp, fmaf(r, tns, tno));
+                                    H1 = T12.x * ri;
+                                    H2 = T12.y * (ri * ri * ri);
+                                }
                                 float g = H2 * fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
                                 v0 = fmaf(H1, f.x, g * dx);
                                 v1 = fmaf(H1, f.y, g * dy);
@@ -455,10 +484,10 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                                 } else if (rr == 0.0) {
                                     H1 = T.self1;  // coincident points, eps = 0: the reference's r -> 0 limit
                                     H2 = 0;
-                                } else {  // eps = 0, nearly coincident: singular kernel from the polynomial
+                                } else {  // eps = 0, nearly coincident: singular kernel from the near piece
                                     float r2f = (float)rr, ri = rsqrtf(r2f);
                                     ri = ri * fmaf(-0.5f * r2f * ri, ri, 1.5f);
-                                    const float2 T12 = horner2<NP>(c12, fmaf(r2f * ri, tds, tdo));
+                                    const float2 T12 = cheb2(S.tn, nnp, fmaf(r2f * ri, tns, tno));
                                     H1 = (double)(T12.x * ri);
                                     H2 = (double)(T12.y * (ri * ri * ri));
                                 }

@@ -256,7 +256,7 @@ int pb_server_create(const pb_server_config* cfg_in, pb_server* out)
             sl.cfg.max_tgt = cfg.max_tgt;
             sl.cfg.max_cells = 1 << 21;
             sl.cfg.precision = cfg.precision;
-            sl.cfg.npoly = 24;
+            sl.cfg.npoly = 20;
             long long est = pb_slot_estimate_bytes(&sl.cfg);
             if (est < 0 || used + est > cfg.budget_bytes) continue;
             int rc = pb_plan_create_slot(&sl.cfg, &sl.plan);

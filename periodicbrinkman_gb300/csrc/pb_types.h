@@ -22,21 +22,28 @@ __host__ __device__
     return v;
 }
 
-constexpr int kMaxPoly = 28;    // max polynomial terms per real-space table
+constexpr int kMaxPoly = 28;    // max terms of the far polynomial (held in registers)
+constexpr int kMaxCheb = 40;    // max terms of the near and blob Chebyshev series (shared memory)
 constexpr int kNumSeries = 16;  // terms of the FP64 small-r series
 
-// Per-instance real-space kernel tables (built in FP64 on the host).
-//   r >= r_tiny:  H1 = (Td1(t) - [r<rs] Te1(te)) / r,  H2 = (Td2 - [r<rs] Te2) / r^3
-//                 with t = r*td_scale + td_off in [-1,1] over [0, rc] and
-//                 te = r*te_scale + te_off over [0, rs]; Td/Te are r*H1, r^3*H2
-//                 of S - R_d and S - R_eps (monomial coefficients, FP32).
-//   r <  r_tiny:  H = R_eps - R_d from its power series in r^2 (FP64).
+// Per-instance real-space kernel tables (built in FP64 on the host).  The pair
+// kernel H = (R_eps - R_d) inside the blob region, S - R_d outside it, is
+// evaluated in FP32 by pieces chosen so that no piece cancels:
+//   far   r in [r_mid, rc]: T1 = r*H1, T2 = r^3*H2 of S - R_d, monomial
+//         coefficients in t = r*td_scale + td_off in [-1, 1] (Horner, registers)
+//   near  r in [rs, r_mid]: the same T of S - R_d as a Chebyshev series in
+//         t = r*tn_scale + tn_off (Clenshaw)
+//   blob  r in [0, rs] (eps > 0): H1 and r^2*H2 of R_eps - R_d as a Chebyshev
+//         series in t = r*tb_scale + tb_off (Clenshaw)
+//   r < r_tiny (eps > 0): H = R_eps - R_d from its FP64 power series in r^2.
+// Most pairs lie in the far piece; the other pieces are the rare path.
 struct PbTables {
-    float pd1[kMaxPoly], pd2[kMaxPoly];
-    float pe1[kMaxPoly], pe2[kMaxPoly];
-    int nd, ne;
-    float td_scale, td_off, te_scale, te_off;
-    float rc2, rs2, rtiny2f;
+    float pd1[kMaxPoly], pd2[kMaxPoly];  // far piece (monomial)
+    float cn1[kMaxCheb], cn2[kMaxCheb];  // near piece (Chebyshev)
+    float cb1[kMaxCheb], cb2[kMaxCheb];  // blob piece (Chebyshev)
+    int nd, nn, nb;
+    float td_scale, td_off, tn_scale, tn_off, tb_scale, tb_off;
+    float rc2, rm2, rs2, rtiny2f;
     int blob;  // eps > 0
     double ser1[kNumSeries], ser2[kNumSeries];
     double self1;   // H1 at r = 0
