@@ -120,14 +120,28 @@ def gen_stream(w):
     return arrive, N, alpha, eps, tol
 
 
-class InputPool:
-    """Seeded positions/forces/targets; request k uses prefixes of set k % sets."""
+def host_array(shape, pinned):
+    """float64 host array, page-locked (through torch) when `pinned`."""
+    if pinned:
+        import torch
 
-    def __init__(self, nmax, sets=8, seed=77):
+        return torch.empty(shape, dtype=torch.float64).pin_memory().numpy()
+    return np.empty(shape)
+
+
+class InputPool:
+    """Seeded positions/forces/targets; request k uses prefixes of set k % sets.
+    Page-locked when `pinned`, as a serving client's buffers would be."""
+
+    def __init__(self, nmax, sets=8, seed=77, pinned=False):
         rng = np.random.default_rng(seed)
-        self.x = [rng.random((nmax, 3)) for _ in range(sets)]
-        self.f = [rng.standard_normal((nmax, 3)) for _ in range(sets)]
-        self.y = [rng.random((nmax // 2 + 1, 3)) for _ in range(sets)]
+        self.x, self.f, self.y = [], [], []
+        for _ in range(sets):
+            for lst, shape, gen in ((self.x, (nmax, 3), rng.random), (self.f, (nmax, 3), rng.standard_normal),
+                                    (self.y, (nmax // 2 + 1, 3), rng.random)):
+                a = host_array(shape, pinned)
+                a[:] = gen(shape)
+                lst.append(a)
         self.sets = sets
 
     def get(self, k, n):
@@ -146,20 +160,34 @@ def run_serve(args, w, rank, world, dist, torch):
     import periodicbrinkman_gb300 as pb
 
     arrive, N, alpha, eps, tol = gen_stream(w)
-    pool = InputPool(w["nmax"])
+    pool = InputPool(w["nmax"], pinned=True)
     step_req = 500
     srv = serve_server(w)
+    # page-locked velocity buffers: one arena slice per request of a step / of the latency run
+    nlat = min(6000, w["nreq"])
+    per_step = max(int(np.sum(N[i:i + step_req] // 2)) for i in range(0, w["nreq"], step_req))
+    out_step = host_array((per_step + 1, 3), True)
+    out_lat = host_array((int(np.sum(N[:nlat] // 2)) + 1, 3), True)
 
-    def submit(k):
+    def submit(k, arena, off):
         x, f, y = pool.get(k, int(N[k]))
-        return srv.submit(x, f, 1.0, float(alpha[k]), float(eps[k]), y=y, tol=float(tol[k]))
+        m = y.shape[0]
+        return srv.submit(x, f, 1.0, float(alpha[k]), float(eps[k]), y=y, tol=float(tol[k]),
+                          out=arena[off:off + m]), off + m
 
     # warm-up: every slot captures its graph
     nreq = w["nreq"]
     order = np.arange(nreq)
     k_next = 0
+    def submit_step(idx):
+        ts, off = [], 0
+        for k in idx:
+            t, off = submit(k, out_step, off)
+            ts.append(t)
+        return ts
+
     for _ in range(max(args.warmup, 3)):
-        ts = [submit(int(order[(k_next + i) % nreq])) for i in range(step_req)]
+        ts = submit_step([int(order[(k_next + i) % nreq]) for i in range(step_req)])
         k_next += step_req
         for t in ts:
             srv.result(t, timeout=600)
@@ -167,14 +195,17 @@ def run_serve(args, w, rank, world, dist, torch):
     # saturated throughput: K steps of 500 requests
     if dist:
         dist.barrier()
-    step_s, h2d, d2h = [], 0, 0
+    step_s, sub_s, h2d, d2h = [], [], 0, 0
+    st0 = srv.stats()
+    k_before = st0["kernels"]
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         for s in range(args.steps):
             idx = [int(order[(k_next + i) % nreq]) for i in range(step_req)]
             k_next += step_req
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            ts = [submit(k) for k in idx]
+            ts = submit_step(idx)
+            sub_s.append(time.perf_counter() - t0)
             for t in ts:
                 srv.result(t, timeout=600)
             torch.cuda.synchronize()
@@ -182,6 +213,9 @@ def run_serve(args, w, rank, world, dist, torch):
             if s == 0:
                 h2d = int(sum(int(N[k]) * 48 + (int(N[k]) // 2) * 24 for k in idx))
                 d2h = int(sum((int(N[k]) // 2) * 24 for k in idx))
+    st1 = srv.stats()
+    launches = st1["kernels"] - k_before
+    sched_busy = st1["scheduler_busy_s"] - st0["scheduler_busy_s"]
     t_tot = float(np.sum(step_s))
     if dist:
         tt = torch.tensor([t_tot], device="cuda")
@@ -190,15 +224,15 @@ def run_serve(args, w, rank, world, dist, torch):
     value = world * args.steps * step_req / t_tot
     stats = srv.stats()
     # open-loop latency under the stream's Poisson arrivals (first 6000 requests, 3 s)
-    nlat = min(6000, nreq)
     lat = np.zeros(nlat)
     t_start = time.perf_counter()
-    tickets = []
+    tickets, off = [], 0
     for k in range(nlat):
         dt = arrive[k] - (time.perf_counter() - t_start)
         if dt > 0:
             time.sleep(dt)
-        tickets.append(submit(k))
+        t, off = submit(k, out_lat, off)
+        tickets.append(t)
     for k, t in enumerate(tickets):
         _, lat[k] = srv.result(t, timeout=600)
     srv.close()
@@ -235,9 +269,9 @@ def run_serve(args, w, rank, world, dist, torch):
         x, f, y = pool.get(int(k), int(N[k]))
         pb.solve(x, f, 1.0, float(alpha[k]), float(eps[k]), y=y, tol=float(tol[k]), precision="fp64")
     plain = len(sample) / (time.perf_counter() - t0)
-    return dict(value=value, step_s=step_s, steps=args.steps, step_req=step_req, stats=stats,
+    return dict(value=value, step_s=step_s, sub_s=sub_s, sched_busy=sched_busy, steps=args.steps, step_req=step_req, stats=stats,
                 p50=float(np.percentile(lat, 50)), p99=float(np.percentile(lat, 99)), lat_n=nlat, err=err,
-                plain=plain, h2d=h2d, d2h=d2h, clocks=clk.summary())
+                plain=plain, h2d=h2d, d2h=d2h, clocks=clk.summary(), launches=launches)
 
 
 # ---------------------------------------------------------------- single solve
@@ -369,13 +403,12 @@ def run_reference(args):
     th = oracle.num_threads()
     if args.workload == "serve":
         w = SERVE
-        vals = []
+        secs = []
         for k in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
             v, ns = cpu_sample_serve(dict(w, seed=w["seed"] + k), nsample=1, ntgt=8)
             if k >= args.warmup:
-                vals.append(v)
-        v = float(np.mean(vals))
+                secs.append(1.0 / v)
+        v = len(secs) / float(np.sum(secs))  # requests per second over the sampled requests
         sample = (f"FP64 direct-Ewald oracle restating the reference's sums ({th} threads): per step one request of "
                   f"the stream, all sources, 8 of its N/2 targets, extrapolated to all targets")
         cfg = {"workload": w["name"]}
@@ -489,13 +522,15 @@ def main():
                    "server": {"slots": st["slots"], "device_bytes": st["device_bytes"],
                               "mean_batch": st["mean_batch"]},
                    "l2": "inputs of a step (hundreds of MB) exceed L2", "parallelism": f"replicas x{world}",
-                   "timing": "host wall time between device-wide synchronizes (multi-stream server)"},
+                   "timing": "host wall time between device-wide synchronizes (multi-stream server)",
+                   "submit_s_per_step": float(np.mean(r["sub_s"])),
+                   "scheduler_busy_s_per_step": r["sched_busy"] / max(1, r["steps"])},
         "latency_s": {"p50": r["p50"], "p99": r["p99"], "requests": r["lat_n"], "arrival": "Poisson 2000/s"},
         "plain_fp64": {"value": r["plain"], "unit": "solves/s", "path": "pb_solve FP64, one solve per call",
                        "served_over_plain": r["value"] / r["plain"]},
         "e2e": {"value": r["value"], "unit": "solves/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
-        "gpu_launches": None,
+        "gpu_launches": r["launches"],
         "roofline": roof, "stage_ms_single_N1e5": stages,
         "max_rel_err": r["err"],
         "clocks": r["clocks"], "cpu_baseline": cb,

@@ -192,6 +192,7 @@ typedef struct pb_server_config {
     int max_src;            /* source capacity of a slot = largest request (0: 262144) */
     int max_tgt;            /* target capacity of a slot (0: max_src) */
     int queue_capacity;     /* pending requests before PB_ERR_BUSY (0: unbounded) */
+    int linger_us;          /* an idle slot waits up to this long for a fuller batch (0: dispatch at once) */
 } pb_server_config;
 
 typedef struct pb_server_counters {
@@ -199,6 +200,8 @@ typedef struct pb_server_counters {
     double mean_batch;      /* instances per slot execution */
     long long device_bytes; /* held by the slots */
     int slots;
+    long long kernels;      /* kernel launches of the slot executions (graph kernel nodes) */
+    double scheduler_busy_s; /* time the scheduler thread spent binding, staging and launching */
 } pb_server_counters;
 
 typedef struct pb_server_s* pb_server;

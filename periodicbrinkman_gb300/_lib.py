@@ -98,6 +98,7 @@ class ServerConfig(C.Structure):
         ("max_src", C.c_int),
         ("max_tgt", C.c_int),
         ("queue_capacity", C.c_int),
+        ("linger_us", C.c_int),
     ]
 
 
@@ -111,6 +112,8 @@ class ServerCounters(C.Structure):
         ("mean_batch", C.c_double),
         ("device_bytes", C.c_longlong),
         ("slots", C.c_int),
+        ("kernels", C.c_longlong),
+        ("scheduler_busy_s", C.c_double),
     ]
 
 

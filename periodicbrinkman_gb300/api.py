@@ -150,7 +150,7 @@ class Plan:
 
 
 def make_slot(M: int, max_instances: int, max_src: int, max_tgt: int, max_cells: int = 1 << 20,
-              precision: str | int = "mixed", npoly: int = 24) -> "Plan":
+              precision: str | int = "mixed", npoly: int = 20) -> "Plan":
     """A capacity plan (serving slot) for instances on an M^3 grid."""
     c = SlotConfig()
     for a in range(3):
@@ -183,7 +183,7 @@ class Server:
 
     def __init__(self, precision: str | int = "mixed", budget_bytes: int = 150 << 30, max_batch: int = 16,
                  slots_per_grid: int = 2, grids=(8, 16, 32, 64, 128, 256), max_src: int = 1 << 18,
-                 max_tgt: int = 0, queue_capacity: int = 0):
+                 max_tgt: int = 0, queue_capacity: int = 0, linger_us: int = 0):
         c = ServerConfig()
         c.budget_bytes = int(budget_bytes)
         c.precision = {"mixed": PB_PREC_MIXED, "fp64": PB_PREC_FP64}.get(precision, precision)
@@ -195,20 +195,30 @@ class Server:
         c.max_src = int(max_src)
         c.max_tgt = int(max_tgt)
         c.queue_capacity = int(queue_capacity)
+        c.linger_us = int(linger_us)
         self.precision = c.precision
         h = C.c_void_p()
         check(lib().pb_server_create(C.byref(c), C.byref(h)))
         self._h = h
         self._live = {}
 
-    def submit(self, x, f, L, alpha, eps, y=None, **kw) -> int:
-        """Queue one solve; returns a ticket.  Buffers are kept until done."""
+    def submit(self, x, f, L, alpha, eps, y=None, out=None, **kw) -> int:
+        """Queue one solve; returns a ticket.  Buffers are kept until done.
+
+        `out` (optional): a C-contiguous float64 (targets, 3) array for the
+        velocities.  Page-locked inputs and `out` (e.g. numpy views of
+        torch pin_memory tensors) are copied by DMA without host staging."""
         x = np.ascontiguousarray(x, dtype=np.float64)
         f = np.ascontiguousarray(f, dtype=np.float64)
         y = None if y is None else np.ascontiguousarray(y, dtype=np.float64)
         m = 0 if y is None else y.shape[0]
         p = make_params(x.shape[0], L, alpha, eps, n_tgt=m, precision=self.precision, **kw)
-        U = np.empty((m if m else x.shape[0], 3))
+        if out is None:
+            U = np.empty((m if m else x.shape[0], 3))
+        else:
+            U = out
+            if U.dtype != np.float64 or not U.flags.c_contiguous or U.shape != (m if m else x.shape[0], 3):
+                raise ValueError("out must be a C-contiguous float64 (targets, 3) array")
         t = C.c_longlong()
         check(lib().pb_server_submit(self._h, C.byref(p), x.ctypes.data, f.ctypes.data,
                                      None if y is None else y.ctypes.data, U.ctypes.data, C.byref(t)))

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "pb_internal.h"
 #include "pb_kernel_math.h"
 #include "pb_kernels.h"
 #include "pbrinkman.h"
@@ -66,10 +67,13 @@ struct CostModel {
     double pair, grid, support;
 };
 
+// Per-unit device times measured on a GB300 (N = 1e5, 128^3, P = 12): mixed
+// precision 0.65 ms / 42e6 pairs, 0.26 ms per 128^3 FFT round trip of three
+// components, 0.79 ms / (2e5 x 1728) window points spread plus gathered.
 CostModel cost_model(int prec)
 {
-    if (prec == PB_PREC_MIXED) return {3.0e-12, 2.5e-11, 1.0e-11};
-    return {1.5e-10, 6.0e-11, 3.0e-11};
+    if (prec == PB_PREC_MIXED) return {1.5e-11, 1.2e-10, 2.3e-12};
+    return {1.5e-10, 2.4e-10, 4.6e-12};
 }
 
 int validate(const pb_solve_params& p)
@@ -154,25 +158,21 @@ int resolve(const pb_solve_params& p, Resolved& R)
     const double etrunc = std::max(4.0, ealias - 3.0);
     const double zeta = std::sqrt(std::log(2.0 / tol)) + 0.35;
     const double uk = 2.0 * std::sqrt(kconst) / M_PI;  // d/h asked by the k-space truncation
-    Support sup;
+    // candidate supports: the given one, else every even P that can reach the
+    // tolerance; the splitting width and the support are chosen together for
+    // the lowest modelled cost
+    std::vector<Support> cands;
     if (p.P > 0) {
-        sup = support_for(p.P, ealias, etrunc, p.m_std);
-        if (sup.u > 1e8) sup.u = uk;  // user support below the tolerance: keep the k-space bound
+        Support t = support_for(p.P, ealias, etrunc, p.m_std);
+        if (t.u > 1e8) t.u = uk;  // user support below the tolerance: keep the k-space bound
+        cands.push_back(t);
     } else {
-        sup = support_for(32, ealias, etrunc, p.m_std);
         for (int P = 6; P <= 32; P += 2) {
             Support t = support_for(P, ealias, etrunc, p.m_std);
-            if (t.u <= 1.1 * uk) {
-                sup = t;
-                break;
-            }
+            if (t.u < 1e8) cands.push_back(t);
         }
+        if (cands.empty()) cands.push_back(support_for(32, ealias, etrunc, p.m_std));
     }
-    const int P = sup.P;
-    const double s = sup.s;
-    const double u = std::max(sup.u, uk);
-    R.P = P;
-    R.m = P / std::sqrt(2.0 * s);
     const double tau = p.L[0] * p.L[1] * p.L[2];
     const double Lmin = std::min(p.L[0], std::min(p.L[1], p.L[2]));
     const CostModel C = cost_model(p.precision);
@@ -181,38 +181,43 @@ int resolve(const pb_solve_params& p, Resolved& R)
         if (p.rc == 0 && p.eps > 0) rc = std::max(rc, zeta * p.eps);
         return rc;
     };
-    double d = p.d;
-    if (d == 0) {
-        // scan d on a log grid for the lowest modelled cost
-        double best = 1e300, bestd = Lmin / 8;
-        for (int k = 0; k < 160; k++) {
-            double dd = Lmin * std::pow(2.0, -1.0 - k * 0.0625);
+    double best = 1e300, d = p.d > 0 ? p.d : Lmin / 8;
+    Support sup = cands.front();
+    for (const Support& cand : cands) {
+        const double u = std::max(cand.u, uk);
+        for (int k = 0; k < (p.d > 0 ? 1 : 160); k++) {
+            const double dd = p.d > 0 ? p.d : Lmin * std::pow(2.0, -1.0 - k * 0.0625);
             if (dd < 1e-6) break;
             int M[3];
             grid_for(p, dd, u, kconst, M);
             bool ok = true;
             for (int a = 0; a < 3; a++) {
-                if (M[a] > 1024) ok = false;
-                if (p.M[a] > 0) {  // fixed grid: d must satisfy its k-space and spreading limits
+                if (M[a] > 1024 || cand.P > M[a]) ok = false;
+                if (p.M[a] > 0 && p.d == 0) {  // fixed grid: d must satisfy its k-space and spreading limits
                     double kmax = 2 * M_PI * (M[a] / 2 - 1) / p.L[a];
                     if (kmax * dd / 2 < std::sqrt(kconst)) ok = false;
                     if (p.L[a] / M[a] * u > dd) ok = false;
                 }
             }
-            if (!ok) continue;
+            if (!ok && !(p.d > 0 && cands.size() == 1)) continue;
             double rc = real_cut(dd);
             double pairs = (double)R.n_tgt * p.n_src * (4 * M_PI / 3) * rc * rc * rc / tau;
             double grid = (double)M[0] * M[1] * M[2];
             double cost = C.pair * pairs + C.grid * grid * std::log2(std::max(grid, 2.0)) / 21.0 +
-                          C.support * (double)(p.n_src + R.n_tgt) * P * P * P;
+                          C.support * (double)(p.n_src + R.n_tgt) * cand.P * cand.P * cand.P;
             if ((R.flags & PB_KSPACE) == 0) cost = C.pair * pairs;
             if (cost < best) {
                 best = cost;
-                bestd = dd;
+                d = dd;
+                sup = cand;
             }
         }
-        d = bestd;
     }
+    const int P = sup.P;
+    const double s = sup.s;
+    const double u = std::max(sup.u, uk);
+    R.P = P;
+    R.m = P / std::sqrt(2.0 * s);
     R.d = d;
     R.rc = real_cut(d);
     grid_for(p, d, u, kconst, R.M);
@@ -283,8 +288,8 @@ struct pb_plan_s {
     int *chunks = nullptr, *chunk_start = nullptr, *scan_tmp = nullptr, *counter = nullptr;
     int4* items = nullptr;
     void *spos_a = nullptr, *spos_b = nullptr, *sfrc = nullptr, *tpos_a = nullptr, *tpos_b = nullptr;
-    float *u_s = nullptr, *u_c = nullptr;
-    double *u_near = nullptr, *u_real = nullptr, *fsum = nullptr;
+    double *u_real = nullptr, *fsum = nullptr;
+    int item_cap = 0;         // capacity of the real-space work item array
     void *u_k = nullptr, *grid = nullptr, *spec = nullptr;
 
     // binding: a plan is a capacity; pb_plan_bind places actual instances in it
@@ -346,7 +351,8 @@ size_t plan_layout(pb_plan_s* P, bool assign)
         o_ptt = L.take<int>(nt);
     }
     size_t o_ch = L.take<int>(nc + 1), o_chs = L.take<int>(nc + 2), o_st = L.take<int>(scan_tmp_ints(nc + 1));
-    size_t o_cnt = L.take<int>(4), o_it = L.take<int4>(nt + 1);
+    const int item_cap = 4 * nt + 4096;
+    size_t o_cnt = L.take<int>(4), o_it = L.take<int4>(item_cap);
     size_t o_sa, o_sb = 0, o_sf, o_ta = 0, o_tb = 0;
     if (mixed) {
         o_sa = L.take<float4>(ns);
@@ -361,16 +367,8 @@ size_t plan_layout(pb_plan_s* P, bool assign)
         o_sf = L.take<Dbl4>(ns);
         if (!P->all_same) o_ta = L.take<Dbl4>(nt);
     }
-    size_t o_us = 0, o_uc = 0, o_un = 0, o_ur = 0, o_uk;
-    if (mixed) {
-        o_us = L.take<float>(3 * (size_t)nt);
-        o_uc = L.take<float>(3 * (size_t)nt);
-        o_un = L.take<double>(3 * (size_t)nt);
-        o_uk = L.take<float>(3 * (size_t)nt);
-    } else {
-        o_ur = L.take<double>(3 * (size_t)nt);
-        o_uk = L.take<double>(3 * (size_t)nt);
-    }
+    size_t o_ur = L.take<double>(3 * (size_t)nt);
+    size_t o_uk = mixed ? L.take<float>(3 * (size_t)nt) : L.take<double>(3 * (size_t)nt);
     size_t o_fsum = L.take<double>(3 * (size_t)q);
     size_t esz = mixed ? 4 : 8;
     size_t o_grid = L.off;
@@ -428,13 +426,8 @@ size_t plan_layout(pb_plan_s* P, bool assign)
             P->tpos_a = A + o_ta;
             P->tpos_b = mixed ? (void*)(A + o_tb) : nullptr;
         }
-        if (mixed) {
-            P->u_s = (float*)(A + o_us);
-            P->u_c = (float*)(A + o_uc);
-            P->u_near = (double*)(A + o_un);
-        } else {
-            P->u_real = (double*)(A + o_ur);
-        }
+        P->u_real = (double*)(A + o_ur);
+        P->item_cap = item_cap;
         P->u_k = A + o_uk;
         P->fsum = (double*)(A + o_fsum);
         P->grid = A + o_grid;
@@ -477,6 +470,7 @@ void set_inst_fields(PbInst& I, const pb_solve_params& p, const Resolved& R, int
     I.ncell = R.nc[0] * R.nc[1] * R.nc[2];
     I.flags = R.flags;
     I.same = R.same;
+    I.csplit = 1;  // assign_splits() refines this per batch
 }
 
 // Per-instance descriptor and tables (grid_off/spec_off/bucket are kept).
@@ -487,6 +481,39 @@ int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved&
     int trc = build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, &P->htab[q], max_terms);
     if (trc) return fail(PB_ERR_INVALID, "table construction failed");
     return PB_OK;
+}
+
+// Real-space work items per row item (csplit) of the first `count` instances.
+// A row item of a small instance carries a long candidate loop; splitting its
+// stencil columns into groups gives the GPU enough items to stay busy.  The
+// target is about 4864 items' worth of equal work (two per resident warp of a
+// GB300), bounded by the stencil columns and by the item array's capacity.
+void assign_splits(pb_plan_s* P, int count)
+{
+    double W = 0;
+    for (int q = 0; q < count; q++) W += std::max(1.0, (double)P->res[q].pairs_est);
+    std::vector<int> G(count, 1);
+    std::vector<long long> bound(count, 0);
+    long long base = 0, extra = 0;
+    for (int q = 0; q < count; q++) {
+        const Resolved& R = P->res[q];
+        const int ncol = (2 * R.S[0] + 1) * (2 * R.S[1] + 1);
+        const double per_item = 24.0 * std::max(1.0, (double)R.pairs_est) / std::max(1, R.n_tgt);
+        long long g = std::llround(per_item * 4864.0 / W);
+        G[q] = (int)std::max(1LL, std::min<long long>(g, std::min(ncol, 255)));
+        // items of an instance <= min(targets, cells + targets/32 + 1) row items
+        const long long nc = (long long)R.nc[0] * R.nc[1] * R.nc[2];
+        bound[q] = std::min<long long>(R.n_tgt, nc + R.n_tgt / 32 + 1);
+        base += bound[q];
+        extra += bound[q] * (G[q] - 1);
+    }
+    const long long room = (long long)P->item_cap - base;
+    if (extra > room) {
+        for (int q = 0; q < count; q++)
+            G[q] = 1 + (int)((long long)(G[q] - 1) * std::max(0LL, room) / extra);
+    }
+    for (int q = 0; q < count; q++) P->hinst[q].csplit = G[q];
+    for (int q = count; q < (int)P->hinst.size(); q++) P->hinst[q].csplit = 1;
 }
 
 int build_plan_host(const pb_solve_params* p, int count, pb_plan_s* P)
@@ -573,6 +600,8 @@ int build_plan_host(const pb_solve_params* p, int count, pb_plan_s* P)
     }
     P->npoly = npoly;
     P->npoly_cap = npoly;
+    P->item_cap = 4 * std::max(P->n_tgt, 1) + 4096;  // as plan_layout sizes it
+    assign_splits(P, count);
     P->bound = count;
     P->act_src = P->n_src;
     P->act_tgt = P->n_tgt;
@@ -673,23 +702,24 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
     }
     launch_count_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->chunks, s);
     launch_exclusive_scan(P->chunks, P->chunk_start, P->ncell, P->scan_tmp, s);
-    launch_emit_items(P->start_t, P->chunk_start, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items, s);
+    launch_emit_items(P->start_t, P->chunk_start, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items,
+                      P->item_cap, s);
     record(P, 1, s);
     if (P->any_real) {
         const int* nitems = P->chunk_start + P->ncell;
         if (mixed)
-            launch_real_mixed(P->npoly, P->d_inst, P->d_tab, P->items, nitems, P->n_tgt, (const float4*)P->spos_a,
-                              (const float4*)P->spos_b, (const float4*)P->sfrc, P->start_s, (const float4*)P->tpos_a,
-                              (const float4*)P->tpos_b, P->u_s, P->u_c, P->u_near, P->counter, P->nsm, s);
+            launch_real_mixed(P->npoly, P->d_inst, P->d_tab, P->items, nitems, P->item_cap,
+                              (const float4*)P->spos_a, (const float4*)P->spos_b, (const float4*)P->sfrc, P->start_s,
+                              (const float4*)P->tpos_a, (const float4*)P->tpos_b, P->n_tgt, P->u_real, P->counter,
+                              P->nsm, s);
         else
-            launch_real_fp64(P->d_inst, P->d_tab, P->items, nitems, P->n_tgt, (const Dbl4*)P->spos_a,
-                             (const Dbl4*)P->sfrc, P->start_s, (const Dbl4*)P->tpos_a, P->u_real, P->counter,
-                             P->nsm, s);
+            launch_real_fp64(P->d_inst, P->d_tab, P->items, nitems, P->item_cap, (const Dbl4*)P->spos_a,
+                             (const Dbl4*)P->sfrc, P->start_s, (const Dbl4*)P->tpos_a, P->n_tgt, P->u_real,
+                             P->counter, P->nsm, s);
     }
     record(P, 2, s);
     if (P->any_k) {
-        size_t esz = mixed ? 4 : 8;
-        cudaMemsetAsync(P->grid, 0, P->grid_elems * esz, s);
+        launch_zero_grids(P->d_inst, P->count, P->grid, mixed ? 4 : 8, s);
         if (mixed)
             launch_spread<float>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
                                  (float*)P->grid, s);
@@ -721,9 +751,8 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
     record(P, 5, s);
     if (P->any_zero) launch_force_sums(P->f, P->d_src_off, P->count, P->fsum, s);
     if (mixed)
-        launch_combine_mixed(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->perm_t, P->u_s, P->u_c, P->u_near,
-                             (const float*)P->u_k, P->any_real, P->any_k, P->fsum, P->d_tab, P->f, P->d_src_off, P->U,
-                             s);
+        launch_combine_mixed(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->perm_t, P->u_real, (const float*)P->u_k,
+                             P->any_real, P->any_k, P->fsum, P->d_tab, P->f, P->d_src_off, P->U, s);
     else
         launch_combine_fp64(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->perm_t, P->u_real,
                             (const double*)P->u_k, P->any_real, P->any_k, P->fsum, P->d_tab, P->f, P->d_src_off, P->U,
@@ -825,7 +854,11 @@ extern "C" long long pb_slot_estimate_bytes(const pb_slot_config* cfg)
     return (long long)plan_layout(&tmp, false);
 }
 
-extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
+namespace {
+
+// Binds `count` instances to a capacity plan; tables are built here unless
+// prepared ones are given.
+int bind_impl(pb_plan P, const pb_solve_params* p, const PbTables* tabs, int count)
 {
     if (!P || (count > 0 && !p) || count < 0 || count > P->count) return fail(PB_ERR_INVALID, "bad arguments");
     std::vector<Resolved> R(count);
@@ -853,22 +886,25 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
     cudaError_t e = cudaEventSynchronize(P->ev_upload);
     if (e != cudaSuccess) return fail(PB_ERR_CUDA, "%s", cudaGetErrorString(e));
     int so = 0, to = 0, co = 0, yo = 0;
-    bool any_zero = false;
     for (int q = 0; q < P->count; q++) {
         P->src_off[q] = so;
         P->tgt_off[q] = to;
         P->cell_off[q] = co;
         if (q < count) {
             P->y_off[q] = R[q].same ? -1 : yo;
-            int rc = fill_instance(P, q, pp[q], R[q], so, to, co, P->npoly_cap);
-            if (rc) return rc;
+            if (tabs) {
+                set_inst_fields(P->hinst[q], pp[q], R[q], so, to, co);
+                P->htab[q] = tabs[q];
+            } else {
+                int rc = fill_instance(P, q, pp[q], R[q], so, to, co, P->npoly_cap);
+                if (rc) return rc;
+            }
             P->res[q] = R[q];
             P->par[q] = pp[q];
             so += R[q].n_src;
             to += R[q].n_tgt;
             if (!R[q].same) yo += R[q].n_tgt;
             co += R[q].nc[0] * R[q].nc[1] * R[q].nc[2];
-            if (R[q].flags & PB_ZERO_MODE) any_zero = true;
         } else {
             P->y_off[q] = -1;
             PbInst& I = P->hinst[q];
@@ -883,7 +919,7 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
     P->tgt_off[P->count] = to;
     P->cell_off[P->count] = co;
     P->y_off[P->count] = -1;
-    (void)any_zero;
+    assign_splits(P, count);
     char* st = P->staging;
     size_t ot = sizeof(PbInst) * P->count, oo = ot + sizeof(PbTables) * P->count, ob = sizeof(int) * (P->count + 1);
     std::memcpy(st, P->hinst.data(), sizeof(PbInst) * P->count);
@@ -900,9 +936,132 @@ extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count)
     return PB_OK;
 }
 
+}  // namespace
+
+extern "C" int pb_plan_bind(pb_plan P, const pb_solve_params* p, int count) { return bind_impl(P, p, nullptr, count); }
+
 namespace pb {
 
+// Uploads a pending binding and runs the device work: eagerly on the first
+// execution (and when timing), as a captured CUDA graph afterwards.
+int upload_and_compute(pb_plan P, cudaStream_t s)
+{
+    if (P->upload_pending) {
+        char* st = P->staging;
+        size_t oi = 0, ot = oi + sizeof(PbInst) * P->count, oo = ot + sizeof(PbTables) * P->count;
+        size_t ob = sizeof(int) * (P->count + 1);
+        PB_CK(cudaMemcpyAsync(P->d_inst, st + oi, sizeof(PbInst) * P->count, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_tab, st + ot, sizeof(PbTables) * P->count, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_src_off, st + oo, ob, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_tgt_off, st + oo + ob, ob, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_cell_off, st + oo + 2 * ob, ob, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaMemcpyAsync(P->d_y_off, st + oo + 3 * ob, ob, cudaMemcpyHostToDevice, s));
+        PB_CK(cudaEventRecord(P->ev_upload, s));
+        P->upload_pending = false;
+    }
+    if (P->n_tgt <= 0 || P->act_tgt <= 0) return PB_OK;
+    if (P->timing || P->exec_count < 1) {
+        run_compute(P, s);
+    } else {
+        if (!P->gexec) {
+            cudaGraph_t g;
+            PB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            run_compute(P, s);
+            PB_CK(cudaStreamEndCapture(s, &g));
+            size_t nn = 0;
+            cudaGraphGetNodes(g, nullptr, &nn);
+            std::vector<cudaGraphNode_t> nodes(nn);
+            cudaGraphGetNodes(g, nodes.data(), &nn);
+            P->graph_kernels = 0;
+            for (auto nd : nodes) {
+                cudaGraphNodeType ty;
+                if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) P->graph_kernels++;
+            }
+            cudaError_t e = cudaGraphInstantiate(&P->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(PB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        }
+        PB_CK(cudaGraphLaunch(P->gexec, s));
+    }
+    PB_CK(cudaGetLastError());
+    return PB_OK;
+}
+
+int plan_execute_parts(pb_plan P, const double* const* xs, const double* const* fs, const double* const* ys,
+                       double* const* Us, cudaStream_t us)
+{
+    if (!P) return fail(PB_ERR_INVALID, "null plan");
+    cudaStream_t s = P->stream;
+    PB_CK(cudaEventRecord(P->ev_in, us));
+    PB_CK(cudaStreamWaitEvent(s, P->ev_in, 0));
+    for (int q = 0; q < P->bound; q++) {
+        const Resolved& R = P->res[q];
+        const size_t so = 3 * (size_t)P->src_off[q];
+        if (R.n_src > 0) {
+            PB_CK(cudaMemcpyAsync(P->x + so, xs[q], sizeof(double) * 3 * R.n_src, cudaMemcpyHostToDevice, s));
+            PB_CK(cudaMemcpyAsync(P->f + so, fs[q], sizeof(double) * 3 * R.n_src, cudaMemcpyHostToDevice, s));
+        }
+        if (!R.same && R.n_tgt > 0)
+            PB_CK(cudaMemcpyAsync(P->y + 3 * (size_t)P->y_off[q], ys[q], sizeof(double) * 3 * R.n_tgt,
+                                  cudaMemcpyHostToDevice, s));
+    }
+    int rc = upload_and_compute(P, s);
+    if (rc) return rc;
+    for (int q = 0; q < P->bound; q++) {
+        const Resolved& R = P->res[q];
+        if (R.n_tgt > 0)
+            PB_CK(cudaMemcpyAsync(Us[q], P->U + 3 * (size_t)P->tgt_off[q], sizeof(double) * 3 * R.n_tgt,
+                                  cudaMemcpyDeviceToHost, s));
+    }
+    P->exec_count++;
+    PB_CK(cudaEventRecord(P->ev_out, s));
+    PB_CK(cudaStreamWaitEvent(us, P->ev_out, 0));
+    return PB_OK;
+}
+
 int api_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
+namespace {
+void fill_info(const Resolved& R, int npoly, pb_instance_info* info)
+{
+    info->d = R.d;
+    info->rc = R.rc;
+    info->eta = R.eta;
+    info->m_std = R.m;
+    for (int a = 0; a < 3; a++) {
+        info->M[a] = R.M[a];
+        info->ncell[a] = R.nc[a];
+    }
+    info->P = R.P;
+    info->npoly = npoly;
+    info->pairs_est = R.pairs_est;
+}
+}  // namespace
+
+int resolve_info(const pb_solve_params& p, pb_instance_info* info)
+{
+    Resolved R;
+    int rc = resolve(p, R);
+    if (rc) return rc;
+    fill_info(R, 0, info);
+    return PB_OK;
+}
+
+int prepare_instance(const pb_solve_params& p, int npoly_cap, PbTables* tab, pb_instance_info* info)
+{
+    Resolved R;
+    int rc = resolve(p, R);
+    if (rc) return rc;
+    if (build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, tab, npoly_cap))
+        return fail(PB_ERR_INVALID, "table construction failed");
+    fill_info(R, tab->nd, info);
+    return PB_OK;
+}
+
+int plan_bind_prepared(pb_plan P, const pb_solve_params* p, const PbTables* tabs, int count)
+{
+    return bind_impl(P, p, tabs, count);
+}
 
 int kspace_instance(const pb_solve_params& p, PbInst* inst)
 {
@@ -1043,51 +1202,15 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
     }
     PB_CK(cudaEventRecord(P->ev_in, us));
     PB_CK(cudaStreamWaitEvent(s, P->ev_in, 0));
-    if (P->upload_pending) {
-        char* st = P->staging;
-        size_t oi = 0, ot = oi + sizeof(PbInst) * P->count, oo = ot + sizeof(PbTables) * P->count;
-        size_t ob = sizeof(int) * (P->count + 1);
-        PB_CK(cudaMemcpyAsync(P->d_inst, st + oi, sizeof(PbInst) * P->count, cudaMemcpyHostToDevice, s));
-        PB_CK(cudaMemcpyAsync(P->d_tab, st + ot, sizeof(PbTables) * P->count, cudaMemcpyHostToDevice, s));
-        PB_CK(cudaMemcpyAsync(P->d_src_off, st + oo, ob, cudaMemcpyHostToDevice, s));
-        PB_CK(cudaMemcpyAsync(P->d_tgt_off, st + oo + ob, ob, cudaMemcpyHostToDevice, s));
-        PB_CK(cudaMemcpyAsync(P->d_cell_off, st + oo + 2 * ob, ob, cudaMemcpyHostToDevice, s));
-        PB_CK(cudaMemcpyAsync(P->d_y_off, st + oo + 3 * ob, ob, cudaMemcpyHostToDevice, s));
-        PB_CK(cudaEventRecord(P->ev_upload, s));
-        P->upload_pending = false;
-    }
     cudaMemcpyKind kin = where == PB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (P->act_src > 0) {
         PB_CK(cudaMemcpyAsync(P->x, x, sizeof(double) * 3 * P->act_src, kin, s));
         PB_CK(cudaMemcpyAsync(P->f, f, sizeof(double) * 3 * P->act_src, kin, s));
     }
     if (!P->all_same && P->act_y > 0) PB_CK(cudaMemcpyAsync(P->y, y, sizeof(double) * 3 * P->act_y, kin, s));
+    int rc = upload_and_compute(P, s);
+    if (rc) return rc;
     if (P->n_tgt > 0 && P->act_tgt > 0) {
-        if (P->timing || P->exec_count < 1) {
-            run_compute(P, s);
-        } else {
-            if (!P->gexec) {
-                cudaGraph_t g;
-                PB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                run_compute(P, s);
-                PB_CK(cudaStreamEndCapture(s, &g));
-                size_t nn = 0;
-                cudaGraphGetNodes(g, nullptr, &nn);
-                std::vector<cudaGraphNode_t> nodes(nn);
-                cudaGraphGetNodes(g, nodes.data(), &nn);
-                P->graph_kernels = 0;
-                for (auto nd : nodes) {
-                    cudaGraphNodeType ty;
-                    if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
-                        P->graph_kernels++;
-                }
-                cudaError_t e = cudaGraphInstantiate(&P->gexec, g, 0);
-                cudaGraphDestroy(g);
-                if (e != cudaSuccess) return fail(PB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-            }
-            PB_CK(cudaGraphLaunch(P->gexec, s));
-        }
-        PB_CK(cudaGetLastError());
         cudaMemcpyKind kout = where == PB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
         PB_CK(cudaMemcpyAsync(U, P->U, sizeof(double) * 3 * P->act_tgt, kout, s));
     }

@@ -1,0 +1,28 @@
+// Library-internal entry points shared by the C ABI files (not exported in
+// include/pbrinkman.h).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pb_types.h"
+#include "pbrinkman.h"
+
+namespace pb {
+
+// Sets the calling thread's pb_last_error() message; returns `code`.
+int api_error(int code, const char* msg);
+// Descriptor of one k-space-only instance with all offsets 0.
+int kspace_instance(const pb_solve_params& p, PbInst* inst);
+// Resolved parameters of one instance without its tables (npoly = 0).
+int resolve_info(const pb_solve_params& p, pb_instance_info* info);
+// Resolved parameters and real-space tables of one instance, built as a plan
+// (or slot) whose far polynomial holds `npoly_cap` terms builds them.
+int prepare_instance(const pb_solve_params& p, int npoly_cap, PbTables* tab, pb_instance_info* info);
+// pb_plan_bind with tables from prepare_instance (tabs[q] belongs to p[q]).
+int plan_bind_prepared(pb_plan P, const pb_solve_params* p, const PbTables* tabs, int count);
+// Executes a bound plan with per-instance host buffers: instance q reads
+// xs[q], fs[q] (and ys[q] when it has its own targets) and writes Us[q].
+// Page-locked buffers are copied asynchronously; inputs must be finite.
+int plan_execute_parts(pb_plan P, const double* const* xs, const double* const* fs, const double* const* ys,
+                       double* const* Us, cudaStream_t stream);
+
+}  // namespace pb

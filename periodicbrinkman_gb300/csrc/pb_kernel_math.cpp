@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 namespace pb {
 
@@ -102,12 +103,13 @@ static void gauss_legendre16(double* x, double* w)
 // b = a*delta, c = 1 - e^{-b^2/4}; K_j = delta^{1-2j} Kt_j.
 static void scaled_moments(double b, int nj, double* Kt)
 {
-    double gx[16], gw[16];
-    gauss_legendre16(gx, gw);
+    static double gx[16], gw[16];
+    static std::once_flag once;
+    std::call_once(once, [] { gauss_legendre16(gx, gw); });
     double c = -std::expm1(-b * b / 4);
     double qmax = 2 * std::sqrt((double)nj) + 18.0;
     std::vector<double> edges;
-    for (double q = 0; q < qmax; q += 0.5) edges.push_back(q);
+    for (double q = 0; q < qmax; q += 1.0) edges.push_back(q);
     edges.push_back(qmax);
     for (int j = -6; j <= 4; j++) {
         double e = b * std::ldexp(1.0, j);
@@ -195,37 +197,37 @@ void scaled_diffH(double r, double a, double delta, const double* ser1, const do
     *T2 = r * r * r * h2;
 }
 
-std::vector<double> fit_chebyshev(const std::function<double(double)>& f, double lo, double hi, int nodes,
-                                  double rel_tol, int max_terms)
+namespace {
+
+// Chebyshev coefficients of samples v[k] = f(node k) (c[0] halved, untruncated).
+std::vector<double> cheb_coeffs(const std::vector<double>& v)
 {
-    std::vector<double> v(nodes), c(nodes);
-    for (int k = 0; k < nodes; k++) {
-        double t = std::cos(kPi * (k + 0.5) / nodes);
-        v[k] = f(lo + (hi - lo) * (t + 1) / 2);
-    }
-    double cmax = 0;
-    std::vector<double> ct(4 * nodes);
+    const int nodes = (int)v.size();
+    std::vector<double> c(nodes), ct(4 * nodes);
     for (int q = 0; q < 4 * nodes; q++) ct[q] = std::cos(kPi * q / (2.0 * nodes));  // cos(pi q / (2 nodes))
     for (int j = 0; j < nodes; j++) {
         double s = 0;
         for (int k = 0; k < nodes; k++) s += v[k] * ct[(j * (2 * k + 1)) % (4 * nodes)];
         c[j] = s * 2.0 / nodes;
-        cmax = std::max(cmax, std::fabs(c[j]));
     }
     c[0] *= 0.5;
-    int n = 1;
-    for (int j = 0; j < nodes; j++)
-        if (std::fabs(c[j]) > rel_tol * cmax) n = j + 1;
-    c.resize(std::min(n, max_terms));
     return c;
 }
 
-std::vector<double> fit_monomial(const std::function<double(double)>& f, double lo, double hi, int nodes,
-                                 double rel_tol, int max_terms)
+int cheb_terms(const std::vector<double>& c, double rel_tol)
 {
-    std::vector<double> c = fit_chebyshev(f, lo, hi, nodes, rel_tol, max_terms);
+    double cmax = 0;
+    for (double v : c) cmax = std::max(cmax, std::fabs(v));
+    int n = 1;
+    for (int j = 0; j < (int)c.size(); j++)
+        if (std::fabs(c[j]) > rel_tol * cmax) n = j + 1;
+    return n;
+}
+
+std::vector<double> cheb_to_monomial(const std::vector<double>& c)
+{
     const int n = (int)c.size();
-    // Chebyshev -> monomial in t: T_{j+1} = 2 t T_j - T_{j-1}
+    // T_{j+1} = 2 t T_j - T_{j-1}
     std::vector<double> a(n, 0.0), T0(n, 0.0), T1(n, 0.0);
     T0[0] = 1;
     if (n > 1) T1[1] = 1;
@@ -243,16 +245,45 @@ std::vector<double> fit_monomial(const std::function<double(double)>& f, double 
     return a;
 }
 
+}  // namespace
+
+std::vector<double> fit_chebyshev(const std::function<double(double)>& f, double lo, double hi, int nodes,
+                                  double rel_tol, int max_terms)
+{
+    std::vector<double> v(nodes);
+    for (int k = 0; k < nodes; k++) v[k] = f(lo + (hi - lo) * (std::cos(kPi * (k + 0.5) / nodes) + 1) / 2);
+    std::vector<double> c = cheb_coeffs(v);
+    c.resize(std::min(cheb_terms(c, rel_tol), max_terms));
+    return c;
+}
+
+std::vector<double> fit_monomial(const std::function<double(double)>& f, double lo, double hi, int nodes,
+                                 double rel_tol, int max_terms)
+{
+    return cheb_to_monomial(fit_chebyshev(f, lo, hi, nodes, rel_tol, max_terms));
+}
+
+void fit_chebyshev_pair(const std::function<void(double, double*, double*)>& f, double lo, double hi, int nodes,
+                        double rel_tol, int max_terms, std::vector<double>& c1, std::vector<double>& c2)
+{
+    std::vector<double> v1(nodes), v2(nodes);
+    for (int k = 0; k < nodes; k++) f(lo + (hi - lo) * (std::cos(kPi * (k + 0.5) / nodes) + 1) / 2, &v1[k], &v2[k]);
+    c1 = cheb_coeffs(v1);
+    c2 = cheb_coeffs(v2);
+    const int n = std::min(std::max(cheb_terms(c1, rel_tol), cheb_terms(c2, rel_tol)), max_terms);
+    c1.resize(n);
+    c2.resize(n);
+}
+
 int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t, int max_terms)
 {
     if (max_terms <= 0 || max_terms > kMaxPoly) max_terms = kMaxPoly;
     if (!(a > 0) || !(d > 0) || !(rc > 0) || eps < 0) return -1;
     std::memset(t, 0, sizeof(PbTables));
-    const int nser = 40;
+    const int nser = 28;  // r/delta < 1 where the series is used: terms fall like 1/m!
     std::vector<double> sd1(nser), sd2(nser), se1(nser), se2(nser);
     regularized_series(a, d, nser, sd1.data(), sd2.data());
-    auto Td1 = [&](double r) { double x, y; scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &x, &y); return x; };
-    auto Td2 = [&](double r) { double x, y; scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &x, &y); return y; };
+    auto Td = [&](double r, double* x, double* y) { scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, x, y); };
     // pieces: blob [0, rs], near [rs, r_mid], far [r_mid, rc]
     const double rs = eps > 0 ? std::min(5.6 * eps, rc) : 0.0;
     const double r_mid = std::min(rc, std::max(0.25 * rc, rs));
@@ -263,32 +294,28 @@ int build_tables(double a, double d, double eps, double rc, double poly_tol, PbT
         *off = (float)(-(hi + lo) / (hi - lo));
     };
     {
-        std::vector<double> p1 = fit_monomial(Td1, r_far, rc, 40, poly_tol, max_terms);
-        std::vector<double> p2 = fit_monomial(Td2, r_far, rc, 40, poly_tol, max_terms);
-        t->nd = (int)std::max(p1.size(), p2.size());
-        p1.resize(t->nd, 0.0);
-        p2.resize(t->nd, 0.0);
+        std::vector<double> c1, c2;
+        fit_chebyshev_pair(Td, r_far, rc, 40, poly_tol, max_terms, c1, c2);
+        std::vector<double> p1 = cheb_to_monomial(c1), p2 = cheb_to_monomial(c2);
+        t->nd = (int)p1.size();
         for (int k = 0; k < t->nd; k++) {
             t->pd1[k] = (float)p1[k];
             t->pd2[k] = (float)p2[k];
         }
         scale_off(r_far, rc, &t->td_scale, &t->td_off);
     }
-    auto cheb = [&](const std::function<double(double)>& f1, const std::function<double(double)>& f2, double lo,
-                    double hi, float* c1, float* c2, float* scale, float* off) {
-        std::vector<double> q1 = fit_chebyshev(f1, lo, hi, 64, poly_tol, kMaxCheb);
-        std::vector<double> q2 = fit_chebyshev(f2, lo, hi, 64, poly_tol, kMaxCheb);
-        int n = (int)std::max(q1.size(), q2.size());
-        q1.resize(n, 0.0);
-        q2.resize(n, 0.0);
-        for (int k = 0; k < n; k++) {
+    auto cheb = [&](const std::function<void(double, double*, double*)>& f, double lo, double hi, float* c1,
+                    float* c2, float* scale, float* off) {
+        std::vector<double> q1, q2;
+        fit_chebyshev_pair(f, lo, hi, 64, poly_tol, kMaxCheb, q1, q2);
+        for (size_t k = 0; k < q1.size(); k++) {
             c1[k] = (float)q1[k];
             c2[k] = (float)q2[k];
         }
         scale_off(lo, hi, scale, off);
-        return n;
+        return (int)q1.size();
     };
-    t->nn = cheb(Td1, Td2, r_near, r_mid, t->cn1, t->cn2, &t->tn_scale, &t->tn_off);
+    t->nn = cheb(Td, r_near, r_mid, t->cn1, t->cn2, &t->tn_scale, &t->tn_off);
     t->rc2 = (float)(rc * rc);
     t->rm2 = (float)(r_mid * r_mid);
     if (eps > 0) {
@@ -297,26 +324,29 @@ int build_tables(double a, double d, double eps, double rc, double poly_tol, PbT
             t->ser1[m] = se1[m] - sd1[m];
             t->ser2[m] = se2[m] - sd2[m];
         }
-        // R_eps - R_d: its series below eps/2, else the difference of the scaled
-        // forms (S cancels, mildly, at r >= eps/2)
-        auto HD = [&](double r, int which) {
+        // R_eps - R_d (H1 and r^2 H2, the latter keeps the error of H2 r^2 uniform): its
+        // series below eps/2, else the difference of the scaled forms (S cancels,
+        // mildly, at r >= eps/2)
+        auto HD = [&](double r, double* h1, double* r2h2) {
             if (r < 0.5 * eps) {
                 const double r2 = r * r;
-                double s = 0, p = 1;
+                double s1 = 0, s2 = 0, p = 1;
                 for (int m = 0; m < nser; m++) {
-                    s += (which == 1 ? se1[m] - sd1[m] : se2[m] - sd2[m]) * p;
+                    s1 += (se1[m] - sd1[m]) * p;
+                    s2 += (se2[m] - sd2[m]) * p;
                     p *= r2;
                 }
-                return s;
+                *h1 = s1;
+                *r2h2 = r2 * s2;
+                return;
             }
             double d1, d2, e1, e2;
             scaled_diffH(r, a, d, sd1.data(), sd2.data(), nser, &d1, &d2);
             scaled_diffH(r, a, eps, se1.data(), se2.data(), nser, &e1, &e2);
-            return which == 1 ? (d1 - e1) / r : (d2 - e2) / (r * r * r);
+            *h1 = (d1 - e1) / r;
+            *r2h2 = (d2 - e2) / r;
         };
-        // H1 and r^2 H2 (the latter keeps the error of H2 r^2 uniform)
-        t->nb = cheb([&](double r) { return HD(r, 1); }, [&](double r) { return r * r * HD(r, 2); }, 0.0, rs, t->cb1,
-                     t->cb2, &t->tb_scale, &t->tb_off);
+        t->nb = cheb(HD, 0.0, rs, t->cb1, t->cb2, &t->tb_scale, &t->tb_off);
         t->rs2 = (float)(rs * rs);
         t->blob = 1;
         double rt = 0.8 * eps;

@@ -45,6 +45,10 @@ std::vector<double> fit_monomial(const std::function<double(double)>& f, double 
 std::vector<double> fit_chebyshev(const std::function<double(double)>& f, double lo, double hi, int nodes,
                                   double rel_tol, int max_terms);
 
+// Two functions sampled together (f(r, &f1, &f2)); both truncated to the same length.
+void fit_chebyshev_pair(const std::function<void(double, double*, double*)>& f, double lo, double hi, int nodes,
+                        double rel_tol, int max_terms, std::vector<double>& c1, std::vector<double>& c2);
+
 // Fill the per-instance real-space tables.  poly_tol: relative truncation of
 // the Chebyshev series (1e-9 keeps ~20 terms); max_terms caps the screened
 // polynomial (<= 0: kMaxPoly).  Returns 0 or an error code.

@@ -30,24 +30,26 @@ void launch_prepare_mixed(const double* pos, const double* frc, const int* perm,
                           cudaStream_t s);
 void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                          const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, cudaStream_t s);
-// Work items: up to 32 consecutive targets of one cell row spanning <= 8 cells:
-// int4 {inst, first target, local row, count | za << 8 | zb << 16}.
+// Work items: up to 32 consecutive targets of one cell row spanning <= 8 cells,
+// times csplit stencil column groups:
+// int4 {inst, first target, local row, count | za << 8 | zb << 16 | group << 24}.
 void launch_count_items(const int* start, int ncell_tot, const int* cell_offsets, const PbInst* inst, int ninst,
                         int* counts, cudaStream_t s);
 void launch_emit_items(const int* start, const int* item_start, int ncell_tot, const int* cell_offsets,
-                       const PbInst* inst, int ninst, int4* items, cudaStream_t s);
+                       const PbInst* inst, int ninst, int4* items, int cap, cudaStream_t s);
 
 // ---- real space (pb_real.cu) ----
 // Mixed precision: FP32 polynomial kernel, hi/lo displacements, Kahan sums.
+// Both kernels zero u_real (3 doubles per target, ntgt_cap targets) and add
+// each work item's part into it with FP64 atomics.
 void launch_real_mixed(int npoly, const PbInst* inst, const PbTables* tab, const int4* items, const int* nitems_ptr,
-                       int nitems_max,
-                       const float4* spos_hi, const float4* spos_lo, const float4* sfrc, const int* src_start,
-                       const float4* tpos_hi, const float4* tpos_lo, float* u_s, float* u_c, double* u_near,
-                       int* counter, int nsm, cudaStream_t s);
+                       int nitems_max, const float4* spos_hi, const float4* spos_lo, const float4* sfrc,
+                       const int* src_start, const float4* tpos_hi, const float4* tpos_lo, int ntgt_cap,
+                       double* u_real, int* counter, int nsm, cudaStream_t s);
 // FP64: closed forms of the reference with the FP64 series below r_tiny.
 void launch_real_fp64(const PbInst* inst, const PbTables* tab, const int4* items, const int* nitems_ptr,
                       int nitems_max, const Dbl4* spos, const Dbl4* sfrc, const int* src_start,
-                      const Dbl4* tpos, double* u, int* counter, int nsm, cudaStream_t s);
+                      const Dbl4* tpos, int ntgt_cap, double* u, int* counter, int nsm, cudaStream_t s);
 
 // ---- k space (pb_kspace.cu) ----
 template <class T>
@@ -61,6 +63,8 @@ void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int nc
 template <class T>
 void launch_kspace_fft(const PbInst* inst_dev, const int* bucket_inst, int ninst_bucket, long long base_off,
                        const int* M, T* grid, void* spec, const void* twiddles, cudaStream_t s);
+// Zeroes the grids (4 M^3 elements of esz bytes) of instances with sources or targets.
+void launch_zero_grids(const PbInst* inst, int ninst, void* grid, int esz, cudaStream_t s);
 size_t twiddle_bytes(const int* M, bool fp64);
 void fill_twiddles(const int* M, bool fp64, void* host_buf);
 
@@ -71,9 +75,8 @@ void launch_pack_targets(const double* x, const double* y, int ncap, const int* 
 
 // ---- final combine ----
 void launch_combine_mixed(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const int* tperm,
-                          const float* u_s, const float* u_c, const double* u_near, const float* u_k, int use_real,
-                          int use_k, const double* fsum, const PbTables* tab, const double* frc,
-                          const int* src_offsets, double* U, cudaStream_t s);
+                          const double* u_real, const float* u_k, int use_real, int use_k, const double* fsum,
+                          const PbTables* tab, const double* frc, const int* src_offsets, double* U, cudaStream_t s);
 void launch_combine_fp64(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const int* tperm,
                          const double* u_real, const double* u_k, int use_real, int use_k, const double* fsum,
                          const PbTables* tab, const double* frc, const int* src_offsets, double* U, cudaStream_t s);

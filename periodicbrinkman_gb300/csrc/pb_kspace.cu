@@ -320,6 +320,24 @@ void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int nc
                                                                     (const Dbl4*)pos_b, grid, u_k);
 }
 
+// Clears the grids of the instances that have sources or targets (a capacity
+// plan's unused positions are left alone): 4 M^3 elements of esz bytes each.
+__global__ void k_zero_grids(const PbInst* __restrict__ inst, char* __restrict__ grid, int esz)
+{
+    const PbInst& I = inst[blockIdx.y];
+    if (I.n_src == 0 && I.n_tgt == 0) return;
+    const size_t n16 = (size_t)I.M[0] * I.M[1] * I.M[2] * 4 * esz / 16;
+    float4* g = reinterpret_cast<float4*>(grid + (size_t)I.grid_off * esz);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+        g[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+void launch_zero_grids(const PbInst* inst, int ninst, void* grid, int esz, cudaStream_t s)
+{
+    if (ninst <= 0) return;
+    k_zero_grids<<<dim3(256, (unsigned)ninst), 256, 0, s>>>(inst, (char*)grid, esz);
+}
+
 template void launch_spread<float>(const PbInst*, int, const int*, int, const void*, const void*, const void*, float*,
                                    cudaStream_t);
 template void launch_spread<double>(const PbInst*, int, const int*, int, const void*, const void*, const void*,
@@ -416,6 +434,15 @@ void fill_twiddles(const int* M, bool fp64, void* host_buf)
     for (int k = 0; k <= Nh; k++) put(o.r + k, -2 * kPiD * k / M[2]);
 }
 
+// FFT work of a bucket position: a capacity plan (serving slot) keeps room for
+// more instances than a batch binds; positions without sources or targets
+// are skipped (their grid stays zero, so gathering from it gives zero).
+__device__ __forceinline__ bool fft_live(const PbInst* inst, const int* bucket_inst, long long b)
+{
+    const PbInst& I = inst[bucket_inst[b]];
+    return I.n_src > 0 && I.n_tgt > 0;
+}
+
 // Planar FP64 grids keep four planes per instance (three components and an
 // unused one): grid line of spectrum line L = ((3 b + c) xy + rest).
 __device__ __forceinline__ size_t plane_line(long long L, long long xy)
@@ -427,7 +454,8 @@ __device__ __forceinline__ size_t plane_line(long long L, long long xy)
 // z pass, forward: real lines of length Mz -> Nh+1 complex (packed half-length FFT).
 template <class T>
 __global__ void k_fft_z_fwd(const T* __restrict__ grid, typename Cx<T>::t* __restrict__ spec, long long nlines, int Mz,
-                            int lpb, const typename Cx<T>::t* __restrict__ tw, TwOff o, long long xy)
+                            int lpb, const typename Cx<T>::t* __restrict__ tw, TwOff o, long long xy,
+                            const PbInst* __restrict__ inst, const int* __restrict__ bucket_inst)
 {
     typedef typename Cx<T>::t T2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -436,6 +464,7 @@ __global__ void k_fft_z_fwd(const T* __restrict__ grid, typename Cx<T>::t* __res
     T2* B = A + lpb * Nh;
     long long l0 = (long long)blockIdx.x * lpb;
     int nl = (int)min((long long)lpb, nlines - l0);
+    if (!fft_live(inst, bucket_inst, l0 / (3 * xy)) && !fft_live(inst, bucket_inst, (l0 + nl - 1) / (3 * xy))) return;
     for (int idx = threadIdx.x; idx < nl * Nh; idx += blockDim.x) {
         int l = idx / Nh, i = idx - l * Nh;
         const T2* src = (const T2*)(grid + plane_line(l0 + l, xy) * Mz);
@@ -465,7 +494,8 @@ __global__ void k_fft_z_fwd(const T* __restrict__ grid, typename Cx<T>::t* __res
 // z pass, inverse: Nh+1 complex -> real line of length Mz.
 template <class T>
 __global__ void k_fft_z_inv(const typename Cx<T>::t* __restrict__ spec, T* __restrict__ grid, long long nlines, int Mz,
-                            int lpb, const typename Cx<T>::t* __restrict__ tw, TwOff o, long long xy)
+                            int lpb, const typename Cx<T>::t* __restrict__ tw, TwOff o, long long xy,
+                            const PbInst* __restrict__ inst, const int* __restrict__ bucket_inst)
 {
     typedef typename Cx<T>::t T2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -475,6 +505,7 @@ __global__ void k_fft_z_inv(const typename Cx<T>::t* __restrict__ spec, T* __res
     const T2* rt = tw + o.r;
     long long l0 = (long long)blockIdx.x * lpb;
     int nl = (int)min((long long)lpb, nlines - l0);
+    if (!fft_live(inst, bucket_inst, l0 / (3 * xy)) && !fft_live(inst, bucket_inst, (l0 + nl - 1) / (3 * xy))) return;
     for (int idx = threadIdx.x; idx < nl * Nh; idx += blockDim.x) {
         int l = idx / Nh, k = idx - l * Nh;
         const T2* src = spec + (size_t)(l0 + l) * Mzh;
@@ -505,7 +536,8 @@ __global__ void k_fft_z_inv(const typename Cx<T>::t* __restrict__ spec, T* __res
 // z passes for FP32 grids with interleaved components (float4 per point):
 // one grid line (instance, x, y) gives the three spectrum lines of its components.
 __global__ void k_fft_z_fwd4(const float4* __restrict__ grid, float2* __restrict__ spec, long long nlines, int Mx,
-                             int My, int Mz, int lpb, const float2* __restrict__ tw, TwOff o)
+                             int My, int Mz, int lpb, const float2* __restrict__ tw, TwOff o,
+                             const PbInst* __restrict__ inst, const int* __restrict__ bucket_inst)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* A = (float2*)smem_raw;
@@ -513,6 +545,8 @@ __global__ void k_fft_z_fwd4(const float4* __restrict__ grid, float2* __restrict
     float2* B = A + 3 * lpb * Nh;
     long long l0 = (long long)blockIdx.x * lpb;
     int nl = (int)min((long long)lpb, nlines - l0);
+    const long long xy_ = (long long)Mx * My;
+    if (!fft_live(inst, bucket_inst, l0 / xy_) && !fft_live(inst, bucket_inst, (l0 + nl - 1) / xy_)) return;
     for (int idx = threadIdx.x; idx < nl * Nh; idx += blockDim.x) {
         int l = idx / Nh, i = idx - l * Nh;
         const float4* src = grid + (size_t)(l0 + l) * Mz;
@@ -542,7 +576,8 @@ __global__ void k_fft_z_fwd4(const float4* __restrict__ grid, float2* __restrict
 }
 
 __global__ void k_fft_z_inv4(const float2* __restrict__ spec, float4* __restrict__ grid, long long nlines, int Mx,
-                             int My, int Mz, int lpb, const float2* __restrict__ tw, TwOff o)
+                             int My, int Mz, int lpb, const float2* __restrict__ tw, TwOff o,
+                             const PbInst* __restrict__ inst, const int* __restrict__ bucket_inst)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* A = (float2*)smem_raw;
@@ -551,6 +586,9 @@ __global__ void k_fft_z_inv4(const float2* __restrict__ spec, float4* __restrict
     const float2* rt = tw + o.r;
     long long l0 = (long long)blockIdx.x * lpb;
     int nl = (int)min((long long)lpb, nlines - l0);
+    if (!fft_live(inst, bucket_inst, l0 / ((long long)Mx * My)) &&
+        !fft_live(inst, bucket_inst, (l0 + nl - 1) / ((long long)Mx * My)))
+        return;
     const long long xy = (long long)Mx * My;
     for (int idx = threadIdx.x; idx < 3 * nl * Nh; idx += blockDim.x) {
         int lc = idx / Nh, k = idx - lc * Nh;
@@ -582,7 +620,8 @@ __global__ void k_fft_z_inv4(const float2* __restrict__ spec, float4* __restrict
 // y pass (forward or inverse) over volumes [nvol][Mx][My][Mzh]; tile of TW z' columns.
 template <class T>
 __global__ void k_fft_y(typename Cx<T>::t* __restrict__ spec, int nvol, int Mx, int My, int Mzh, int TW,
-                        const typename Cx<T>::t* __restrict__ tw, int tw_off, bool inverse)
+                        const typename Cx<T>::t* __restrict__ tw, int tw_off, bool inverse,
+                        const PbInst* __restrict__ inst, const int* __restrict__ bucket_inst)
 {
     typedef typename Cx<T>::t T2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -592,6 +631,7 @@ __global__ void k_fft_y(typename Cx<T>::t* __restrict__ spec, int nvol, int Mx, 
     long long blk = blockIdx.x;
     int tile = (int)(blk % ntile);
     long long vx = blk / ntile;  // vol*Mx + x
+    if (!fft_live(inst, bucket_inst, vx / Mx / 3)) return;
     int z0 = tile * TW;
     int nl = min(TW, Mzh - z0);
     T2* base = spec + (size_t)vx * My * Mzh + z0;
@@ -629,6 +669,7 @@ __global__ void k_fft_x_green(typename Cx<T>::t* __restrict__ spec, const PbInst
     long long r = blk / ntile;
     int y = (int)(r % My);
     int qi = (int)(r / My);
+    if (!fft_live(inst, bucket_inst, qi)) return;
     const PbInst& I = inst[bucket_inst[qi]];
     int z0 = tile * TW;
     int nl = min(TW, Mzh - z0);
@@ -716,18 +757,19 @@ void launch_kspace_fft(const PbInst* inst_dev, const int* bucket_inst, int nb, l
     if (sizeof(T) == 4) {
         cudaFuncSetAttribute(k_fft_z_fwd4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
         k_fft_z_fwd4<<<(unsigned)((nlines4 + lpb4 - 1) / lpb4), 256, sm4, s>>>(
-            (const float4*)grid, (float2*)spec, nlines4, Mx, My, Mz, lpb4, (const float2*)tw, o);
+            (const float4*)grid, (float2*)spec, nlines4, Mx, My, Mz, lpb4, (const float2*)tw, o, inst_dev, bucket_inst);
     } else {
         cudaFuncSetAttribute(k_fft_z_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_fft_z_fwd<T><<<(unsigned)((nlines + lpb - 1) / lpb), 256, sm, s>>>(grid, spec, nlines, Mz, lpb, tw, o,
-                                                                              (long long)Mx * My);
+                                                                              (long long)Mx * My, inst_dev,
+                                                                              bucket_inst);
     }
     // y forward
     int twy = pick_tw(My, 1, cs, smax);
     size_t smy = (size_t)2 * twy * My * cs;
     cudaFuncSetAttribute(k_fft_y<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
     long long nby = (long long)nvol * Mx * ((Mzh + twy - 1) / twy);
-    k_fft_y<T><<<(unsigned)nby, 256, smy, s>>>(spec, nvol, Mx, My, Mzh, twy, tw, o.y, false);
+    k_fft_y<T><<<(unsigned)nby, 256, smy, s>>>(spec, nvol, Mx, My, Mzh, twy, tw, o.y, false, inst_dev, bucket_inst);
     // x forward + Green + x inverse
     int twx = pick_tw(Mx, 3, cs, smax);
     size_t smx = (size_t)2 * 3 * twx * Mx * cs;
@@ -736,16 +778,17 @@ void launch_kspace_fft(const PbInst* inst_dev, const int* bucket_inst, int nb, l
     k_fft_x_green<T><<<(unsigned)nbx, 256, smx, s>>>(spec, inst_dev, bucket_inst, base_off, Mx, My, Mzh, Mz, twx, tw,
                                                        o.x);
     // y inverse
-    k_fft_y<T><<<(unsigned)nby, 256, smy, s>>>(spec, nvol, Mx, My, Mzh, twy, tw, o.y, true);
+    k_fft_y<T><<<(unsigned)nby, 256, smy, s>>>(spec, nvol, Mx, My, Mzh, twy, tw, o.y, true, inst_dev, bucket_inst);
     // z inverse
     if (sizeof(T) == 4) {
         cudaFuncSetAttribute(k_fft_z_inv4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
         k_fft_z_inv4<<<(unsigned)((nlines4 + lpb4 - 1) / lpb4), 256, sm4, s>>>(
-            (const float2*)spec, (float4*)grid, nlines4, Mx, My, Mz, lpb4, (const float2*)tw, o);
+            (const float2*)spec, (float4*)grid, nlines4, Mx, My, Mz, lpb4, (const float2*)tw, o, inst_dev, bucket_inst);
     } else {
         cudaFuncSetAttribute(k_fft_z_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_fft_z_inv<T><<<(unsigned)((nlines + lpb - 1) / lpb), 256, sm, s>>>(spec, grid, nlines, Mz, lpb, tw, o,
-                                                                              (long long)Mx * My);
+                                                                              (long long)Mx * My, inst_dev,
+                                                                              bucket_inst);
     }
 }
 
@@ -758,8 +801,7 @@ template void launch_kspace_fft<double>(const PbInst*, const int*, int, long lon
 // Final FP64 combine and force sums
 // ---------------------------------------------------------------------------
 __global__ void k_combine_mixed(const PbInst* __restrict__ inst, int ninst, const int* __restrict__ tgt_offsets,
-                                const int* __restrict__ tperm, const float* __restrict__ u_s,
-                                const float* __restrict__ u_c, const double* __restrict__ u_near,
+                                const int* __restrict__ tperm, const double* __restrict__ u_real,
                                 const float* __restrict__ u_k, int use_real, int use_k, const double* __restrict__ fsum,
                                 const PbTables* __restrict__ tab, const double* __restrict__ frc,
                                 const int* __restrict__ src_offsets, double* __restrict__ U)
@@ -777,7 +819,7 @@ __global__ void k_combine_mixed(const PbInst* __restrict__ inst, int ninst, cons
         double v = 0;
         size_t o = 3 * (size_t)t + c;
         if (self) v += tab[q].self1 * frc[3 * ps + c];
-        if (use_real && (I.flags & 1)) v += ((double)u_s[o] - (double)u_c[o]) + u_near[o];
+        if (use_real && (I.flags & 1)) v += u_real[o];
         if (use_k && (I.flags & 2)) v += (double)u_k[o];
         if (I.flags & 4) v += fsum[3 * q + c] / (I.alpha * I.alpha * tau);
         U[3 * (size_t)p + c] = v;
@@ -811,13 +853,12 @@ __global__ void k_combine_fp64(const PbInst* __restrict__ inst, int ninst, const
 }
 
 void launch_combine_mixed(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const int* tperm,
-                          const float* u_s, const float* u_c, const double* u_near, const float* u_k, int use_real,
-                          int use_k, const double* fsum, const PbTables* tab, const double* frc,
-                          const int* src_offsets, double* U, cudaStream_t s)
+                          const double* u_real, const float* u_k, int use_real, int use_k, const double* fsum,
+                          const PbTables* tab, const double* frc, const int* src_offsets, double* U, cudaStream_t s)
 {
     if (ncap <= 0) return;
-    k_combine_mixed<<<(ncap + 255) / 256, 256, 0, s>>>(inst, ninst, tgt_offsets, tperm, u_s, u_c, u_near, u_k,
-                                                        use_real, use_k, fsum, tab, frc, src_offsets, U);
+    k_combine_mixed<<<(ncap + 255) / 256, 256, 0, s>>>(inst, ninst, tgt_offsets, tperm, u_real, u_k, use_real, use_k,
+                                                        fsum, tab, frc, src_offsets, U);
 }
 
 void launch_combine_fp64(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const int* tperm,

@@ -32,9 +32,10 @@ constexpr int kRealWarps = 4;
 constexpr int kMaxReach = 15;  // stencil reach S per axis
 constexpr int kZTab = 8 + 2 * kMaxReach;
 
-// item = {instance, first target, local row c0*nc1 + c1, count | za << 8 | zb << 16}
+// item = {instance, first target, local row c0*nc1 + c1, count | za << 8 | zb << 16 | group << 24}:
+// the item covers the stencil columns col = group, group + csplit, ... of its rows
 struct ItemFrame {
-    int q, c0, c1, za, zb, first, count;
+    int q, c0, c1, za, zb, first, count, group;
     double O[3];
 };
 
@@ -47,6 +48,7 @@ __device__ __forceinline__ void item_frame(const PbInst& I, int4 it, ItemFrame& 
     F.count = it.w & 0xff;
     F.za = (it.w >> 8) & 0xff;
     F.zb = (it.w >> 16) & 0xff;
+    F.group = (it.w >> 24) & 0xff;
     F.O[0] = F.c0 * I.h[0];
     F.O[1] = F.c1 * I.h[1];
     F.O[2] = F.za * I.h[2];
@@ -187,15 +189,15 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
     k_real_mixed(const PbInst* __restrict__ inst, const PbTables* __restrict__ tab, const int4* __restrict__ items,
                  const int* __restrict__ nitems_ptr, const float4* __restrict__ spos_hi, const float4* __restrict__ spos_lo,
                  const float4* __restrict__ sfrc, const int* __restrict__ src_start, const float4* __restrict__ tpos_hi,
-                 const float4* __restrict__ tpos_lo, float* __restrict__ u_s, float* __restrict__ u_c,
-                 double* __restrict__ u_near, int* __restrict__ counter)
+                 const float4* __restrict__ tpos_lo, double* __restrict__ u_real, int* __restrict__ counter,
+                 int item_cap)
 {
     __shared__ RealWarpSmem smem_all[kRealWarps];
     RealWarpSmem& S = smem_all[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
 
-    const int nitems = *nitems_ptr;
+    const int nitems = min(*nitems_ptr, item_cap);
     float2 c12[NP];
     int cur_q = -1;
     float tds = 0, tdo = 0, rc2 = 0, rare2 = 0, rtiny2 = 0, tbs = 0, tbo = 0, tns = 0, tno = 0, rs2 = 0;
@@ -261,10 +263,13 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
         float s0 = 0, s1 = 0, s2 = 0, k0 = 0, k1 = 0, k2 = 0;
         const int nzt = F.zb - F.za + 2 * I.S[2] + 1;
 
-        for (int i0 = 0; i0 <= 2 * I.S[0]; i0++) {
-            const float2 qx = S.ft.qx[i0];
-            const int w0 = S.ft.wx[i0], z0 = S.ft.zx[i0];
-            for (int i1 = 0; i1 <= 2 * I.S[1]; i1++) {
+        const int ny1 = 2 * I.S[1] + 1, ncol = (2 * I.S[0] + 1) * ny1;
+        const int csplit = max(1, I.csplit);
+        for (int col = F.group; col < ncol; col += csplit) {
+            const int i0 = col / ny1, i1 = col - i0 * ny1;
+            {
+                const float2 qx = S.ft.qx[i0];
+                const int w0 = S.ft.wx[i0], z0 = S.ft.zx[i0];
                 const float2 qy = S.ft.qy[i1];
                 const int w1 = S.ft.wy[i1], z1 = S.ft.zy[i1];
                 const int row = I.cell_off + (w0 * I.nc[1] + w1) * I.nc[2];
@@ -509,17 +514,11 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                 }
             }
         }
-        if (active) {
+        if (active) {  // the item's part of the target's sum (other column groups add theirs)
             size_t o = 3 * (size_t)tidx;
-            u_s[o] = s0;
-            u_s[o + 1] = s1;
-            u_s[o + 2] = s2;
-            u_c[o] = k0;
-            u_c[o + 1] = k1;
-            u_c[o + 2] = k2;
-            u_near[o] = S.acc64[0][lane];
-            u_near[o + 1] = S.acc64[1][lane];
-            u_near[o + 2] = S.acc64[2][lane];
+            atomicAdd(u_real + o, ((double)s0 - (double)k0) + S.acc64[0][lane]);
+            atomicAdd(u_real + o + 1, ((double)s1 - (double)k1) + S.acc64[1][lane]);
+            atomicAdd(u_real + o + 2, ((double)s2 - (double)k2) + S.acc64[2][lane]);
         }
         S.acc64[0][lane] = 0.0;
         S.acc64[1][lane] = 0.0;
@@ -531,18 +530,19 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
 void launch_real_mixed(int npoly, const PbInst* inst, const PbTables* tab, const int4* items, const int* nitems_ptr,
                        int nitems_max,
                        const float4* spos_hi, const float4* spos_lo, const float4* sfrc, const int* src_start,
-                       const float4* tpos_hi, const float4* tpos_lo, float* u_s, float* u_c, double* u_near,
-                       int* counter, int nsm, cudaStream_t s)
+                       const float4* tpos_hi, const float4* tpos_lo, int ntgt_cap, double* u_real, int* counter,
+                       int nsm, cudaStream_t s)
 {
     if (nitems_max <= 0) return;
     cudaMemsetAsync(counter, 0, sizeof(int), s);
+    cudaMemsetAsync(u_real, 0, 3 * sizeof(double) * (size_t)ntgt_cap, s);
     int blocks = nsm * 8;
     int need = (nitems_max + kRealWarps - 1) / kRealWarps;
     if (blocks > need) blocks = need;
 #define PB_LAUNCH_REAL(NP)                                                                                            \
     k_real_mixed<NP><<<blocks, kRealWarps * 32, 0, s>>>(inst, tab, items, nitems_ptr, spos_hi, spos_lo, sfrc,        \
                                                          src_start,                                                  \
-                                                         tpos_hi, tpos_lo, u_s, u_c, u_near, counter)
+                                                         tpos_hi, tpos_lo, u_real, counter, nitems_max)
     if (npoly <= 16)
         PB_LAUNCH_REAL(16);
     else if (npoly <= 20)
@@ -560,12 +560,12 @@ __global__ void __launch_bounds__(kRealWarps * 32)
     k_real_fp64(const PbInst* __restrict__ inst, const PbTables* __restrict__ tab, const int4* __restrict__ items,
                 const int* __restrict__ nitems_ptr, const Dbl4* __restrict__ spos, const Dbl4* __restrict__ sfrc,
                 const int* __restrict__ src_start, const Dbl4* __restrict__ tpos, double* __restrict__ u,
-                int* __restrict__ counter)
+                int* __restrict__ counter, int item_cap)
 {
     __shared__ Dbl4 sh_p[kRealWarps][32];
     __shared__ Dbl4 sh_f[kRealWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int nitems = *nitems_ptr;
+    const int nitems = min(*nitems_ptr, item_cap);
     while (true) {
         int item = 0;
         if (lane == 0) item = atomicAdd(counter, 1);
@@ -586,11 +586,14 @@ __global__ void __launch_bounds__(kRealWarps * 32)
         Dbl4 tp = tpos[tidx];
         if (!active) tp.x = tp.y = tp.z = 3.0e300;  // inactive lanes pair with nothing
         double v0 = 0, v1 = 0, v2 = 0;
-        for (int o0 = -I.S[0]; o0 <= I.S[0]; o0++) {
+        const int ny1 = 2 * I.S[1] + 1, ncol = (2 * I.S[0] + 1) * ny1;
+        const int csplit = max(1, I.csplit);
+        for (int col = F.group; col < ncol; col += csplit) {
+            const int o0 = col / ny1 - I.S[0], o1 = col % ny1 - I.S[1];
             int g0 = F.c0 + o0;
             int w0 = ((g0 % I.nc[0]) + I.nc[0]) % I.nc[0];
             double sh0 = (double)((g0 - w0) / I.nc[0]) * I.L[0];
-            for (int o1 = -I.S[1]; o1 <= I.S[1]; o1++) {
+            {
                 int g1 = F.c1 + o1;
                 int w1 = ((g1 % I.nc[1]) + I.nc[1]) % I.nc[1];
                 double sh1 = (double)((g1 - w1) / I.nc[1]) * I.L[1];
@@ -660,26 +663,27 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                 }
             }
         }
-        if (active) {
+        if (active) {  // the item's part of the target's sum (other column groups add theirs)
             size_t o = 3 * (size_t)tidx;
-            u[o] = v0;
-            u[o + 1] = v1;
-            u[o + 2] = v2;
+            atomicAdd(u + o, v0);
+            atomicAdd(u + o + 1, v1);
+            atomicAdd(u + o + 2, v2);
         }
     }
 }
 
 void launch_real_fp64(const PbInst* inst, const PbTables* tab, const int4* items, const int* nitems_ptr,
                       int nitems_max, const Dbl4* spos, const Dbl4* sfrc, const int* src_start,
-                      const Dbl4* tpos, double* u, int* counter, int nsm, cudaStream_t s)
+                      const Dbl4* tpos, int ntgt_cap, double* u, int* counter, int nsm, cudaStream_t s)
 {
     if (nitems_max <= 0) return;
     cudaMemsetAsync(counter, 0, sizeof(int), s);
+    cudaMemsetAsync(u, 0, 3 * sizeof(double) * (size_t)ntgt_cap, s);
     int blocks = nsm * 8;
     int need = (nitems_max + kRealWarps - 1) / kRealWarps;
     if (blocks > need) blocks = need;
     k_real_fp64<<<blocks, kRealWarps * 32, 0, s>>>(inst, tab, items, nitems_ptr, spos, sfrc, src_start, tpos, u,
-                                                   counter);
+                                                   counter, nitems_max);
 }
 
 }  // namespace pb

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -24,6 +25,7 @@
 
 #include <cuda_runtime.h>
 
+#include "pb_internal.h"
 #include "pbrinkman.h"
 
 namespace {
@@ -33,10 +35,12 @@ using Clock = std::chrono::steady_clock;
 struct Req {
     long long id;
     pb_solve_params p;
+    pb::PbTables tab;  // real-space tables, built at submission
     int grid;
     int n_tgt_eff;
     const double *x, *f, *y;
     double* U;
+    bool pin_in = false, pin_out = false;  // page-locked client buffers: copied by DMA, no staging
     Clock::time_point t_sub, t_done;
     std::atomic<int> state{0};  // 0 queued, 1 running, 2 done
     int status = PB_OK;
@@ -52,6 +56,9 @@ struct Slot {
     bool busy = false;
     std::vector<Req*> reqs;
     std::vector<pb_solve_params> params;
+    std::vector<pb::PbTables> tabs;
+    std::vector<const double*> xs, fs, ys;
+    std::vector<double*> Us;
 };
 
 std::string g_srv_err;
@@ -70,12 +77,24 @@ struct pb_server_s {
     std::vector<std::deque<Req*>> queues;  // per grid index
     std::thread worker;
     std::atomic<bool> stop{false};
-    std::atomic<long long> next_id{1}, submitted{0}, completed{0}, failed{0}, rejected{0}, batches{0},
+    std::atomic<long long> next_id{1}, submitted{0}, completed{0}, failed{0}, rejected{0}, batches{0}, kernels{0},
         batched_instances{0};
     int device = 0;
+    int npoly = 20;  // far-polynomial terms of every slot
+    std::atomic<long long> busy_ns{0};
 };
 
 namespace {
+
+bool page_locked(const void* ptr)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
 
 int grid_index(pb_server_s* S, int g)
 {
@@ -89,7 +108,7 @@ void finish_slot(pb_server_s* S, Slot& sl, int status)
     size_t off = 0;
     for (Req* r : sl.reqs) {
         size_t nb = 3 * (size_t)r->n_tgt_eff;
-        if (status == PB_OK) std::memcpy(r->U, sl.U + off, nb * sizeof(double));
+        if (status == PB_OK && !r->pin_out) std::memcpy(r->U, sl.U + off, nb * sizeof(double));
         off += nb;
         r->status = status;
         r->t_done = Clock::now();
@@ -107,9 +126,15 @@ bool dispatch(pb_server_s* S, Slot& sl, std::deque<Req*>& q)
 {
     if (q.empty()) return false;
     const pb_slot_config& c = sl.cfg;
+    // batching window: a short queue waits (up to linger_us after its oldest
+    // request arrived) for more requests to share the slot execution
+    if (S->cfg.linger_us > 0 && (int)q.size() < c.max_instances &&
+        Clock::now() - q.front()->t_sub < std::chrono::microseconds(S->cfg.linger_us))
+        return false;
     long long ns = 0, nt = 0, ny = 0;
     sl.reqs.clear();
     sl.params.clear();
+    sl.tabs.clear();
     while (!q.empty() && (int)sl.reqs.size() < c.max_instances) {
         Req* r = q.front();
         long long n = r->p.n_src, m = r->n_tgt_eff;
@@ -122,37 +147,56 @@ bool dispatch(pb_server_s* S, Slot& sl, std::deque<Req*>& q)
         pb_solve_params p = r->p;
         p.M[0] = p.M[1] = p.M[2] = sl.grid;
         sl.params.push_back(p);
+        sl.tabs.push_back(r->tab);
     }
     if (sl.reqs.empty()) return false;
-    int rc = pb_plan_bind(sl.plan, sl.params.data(), (int)sl.params.size());
+    int rc = pb::plan_bind_prepared(sl.plan, sl.params.data(), sl.tabs.data(), (int)sl.params.size());
     if (rc == PB_ERR_BUDGET && sl.reqs.size() > 1) {
         // cells over capacity: put all back but the first and bind it alone
         for (size_t k = sl.reqs.size(); k-- > 1;) q.push_front(sl.reqs[k]);
         sl.reqs.resize(1);
         sl.params.resize(1);
+        sl.tabs.resize(1);
         ns = sl.reqs[0]->p.n_src;
         nt = sl.reqs[0]->n_tgt_eff;
         ny = sl.reqs[0]->p.n_tgt > 0 ? nt : 0;
-        rc = pb_plan_bind(sl.plan, sl.params.data(), 1);
+        rc = pb::plan_bind_prepared(sl.plan, sl.params.data(), sl.tabs.data(), 1);
     }
     if (rc != PB_OK) {
         finish_slot(S, sl, rc);
         return true;
     }
-    size_t xo = 0, yo = 0;
+    // page-locked client buffers go to the device directly; others through the slot's staging
+    sl.xs.clear();
+    sl.fs.clear();
+    sl.ys.clear();
+    sl.Us.clear();
+    size_t xo = 0, yo = 0, uo = 0;
     for (Req* r : sl.reqs) {
-        size_t n3 = 3 * (size_t)r->p.n_src;
-        std::memcpy(sl.x + xo, r->x, n3 * sizeof(double));
-        std::memcpy(sl.f + xo, r->f, n3 * sizeof(double));
-        xo += n3;
-        if (r->p.n_tgt > 0) {
-            size_t m3 = 3 * (size_t)r->p.n_tgt;
-            std::memcpy(sl.y + yo, r->y, m3 * sizeof(double));
-            yo += m3;
+        size_t n3 = 3 * (size_t)r->p.n_src, m3 = 3 * (size_t)r->p.n_tgt;
+        if (r->pin_in) {
+            sl.xs.push_back(r->x);
+            sl.fs.push_back(r->f);
+            sl.ys.push_back(r->y);
+        } else {
+            std::memcpy(sl.x + xo, r->x, n3 * sizeof(double));
+            std::memcpy(sl.f + xo, r->f, n3 * sizeof(double));
+            sl.xs.push_back(sl.x + xo);
+            sl.fs.push_back(sl.f + xo);
+            xo += n3;
+            if (r->p.n_tgt > 0) {
+                std::memcpy(sl.y + yo, r->y, m3 * sizeof(double));
+                sl.ys.push_back(sl.y + yo);
+                yo += m3;
+            } else {
+                sl.ys.push_back(nullptr);
+            }
         }
+        sl.Us.push_back(r->pin_out ? r->U : sl.U + uo);
+        uo += 3 * (size_t)r->n_tgt_eff;
         r->state.store(1);
     }
-    rc = pb_plan_execute(sl.plan, sl.x, sl.f, sl.y, sl.U, PB_HOST_PINNED, sl.stream);
+    rc = pb::plan_execute_parts(sl.plan, sl.xs.data(), sl.fs.data(), sl.ys.data(), sl.Us.data(), sl.stream);
     if (rc == PB_OK && cudaEventRecord(sl.done, sl.stream) != cudaSuccess) rc = PB_ERR_CUDA;
     if (rc != PB_OK) {
         finish_slot(S, sl, rc);
@@ -160,6 +204,7 @@ bool dispatch(pb_server_s* S, Slot& sl, std::deque<Req*>& q)
     }
     sl.busy = true;
     S->batches++;
+    S->kernels += pb_plan_kernel_count(sl.plan);
     S->batched_instances += (long long)sl.reqs.size();
     return true;
 }
@@ -189,11 +234,13 @@ void worker_loop(pb_server_s* S)
                 S->queues[r->grid].push_back(r);
             }
         }
+        auto t0 = Clock::now();
         for (Slot& sl : S->slots) {
             if (sl.busy) continue;
             int gi = grid_index(S, sl.grid);
             if (gi >= 0 && dispatch(S, sl, S->queues[gi])) did = true;
         }
+        if (did) S->busy_ns += std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count();
         if (!did) {
             std::unique_lock<std::mutex> lk(S->mu);
             S->cv.wait_for(lk, std::chrono::microseconds(50), [&] { return !S->inbox.empty() || S->stop.load(); });
@@ -254,9 +301,11 @@ int pb_server_create(const pb_server_config* cfg_in, pb_server* out)
             sl.cfg.max_instances = B;
             sl.cfg.max_src = cfg.max_src;
             sl.cfg.max_tgt = cfg.max_tgt;
-            sl.cfg.max_cells = 1 << 21;
+            // cells: the autotuner keeps rc >= ~4.6 grid spacings, so an instance has
+            // at most (M/2)^3 cells
+            sl.cfg.max_cells = (int)std::min<long long>(1 << 21, (long long)B * (g / 2) * (g / 2) * (g / 2));
             sl.cfg.precision = cfg.precision;
-            sl.cfg.npoly = 20;
+            sl.cfg.npoly = S->npoly;
             long long est = pb_slot_estimate_bytes(&sl.cfg);
             if (est < 0 || used + est > cfg.budget_bytes) continue;
             int rc = pb_plan_create_slot(&sl.cfg, &sl.plan);
@@ -298,21 +347,44 @@ int pb_server_submit(pb_server S, const pb_solve_params* p, const double* x, con
     *ticket = 0;
     if (p->precision != S->cfg.precision) return PB_ERR_INVALID;
     if (p->n_src <= 0 || (p->n_tgt > 0 && !y) || !x || !f || !U) return PB_ERR_INVALID;
+    // autotune and build the real-space tables here, in the caller's thread, so
+    // the scheduler only binds; inputs are checked here too
     pb_instance_info info;
-    int rc = pb_resolve(p, &info);
+    int rc = pb::resolve_info(*p, &info);
     if (rc != PB_OK) return rc;
     int need = std::max(info.M[0], std::max(info.M[1], info.M[2]));
     int gi = grid_index(S, need);
+    // the instance runs on its slot's grid: resolve and build its tables for that grid
+    Req* r = new Req();
+    if (gi >= 0) {
+        pb_solve_params pg = *p;
+        pg.M[0] = pg.M[1] = pg.M[2] = S->grids[gi];
+        rc = pb::prepare_instance(pg, S->npoly, &r->tab, &info);
+        if (rc != PB_OK) {
+            delete r;
+            return rc;
+        }
+    }
+    const size_t n3 = 3 * (size_t)p->n_src, m3 = 3 * (size_t)std::max(p->n_tgt, 0);
+    bool finite = true;
+    for (size_t i = 0; i < n3 && finite; i++) finite = std::isfinite(x[i]) && std::isfinite(f[i]);
+    for (size_t i = 0; i < m3 && finite; i++) finite = std::isfinite(y[i]);
+    if (!finite) {
+        delete r;
+        return pb::api_error(PB_ERR_INVALID, "non-finite input");
+    }
     int n_tgt_eff = p->n_tgt > 0 ? p->n_tgt : p->n_src;
+    const long long cells = (long long)info.ncell[0] * info.ncell[1] * info.ncell[2];
     bool fits = false;
     for (const Slot& sl : S->slots)
-        if (gi >= 0 && sl.grid == S->grids[gi] && p->n_src <= sl.cfg.max_src && n_tgt_eff <= sl.cfg.max_tgt)
+        if (gi >= 0 && sl.grid == S->grids[gi] && p->n_src <= sl.cfg.max_src && n_tgt_eff <= sl.cfg.max_tgt &&
+            cells <= sl.cfg.max_cells)
             fits = true;
     if (!fits) {
+        delete r;
         S->rejected++;
         return PB_ERR_BUDGET;
     }
-    Req* r = new Req();
     r->id = S->next_id++;
     r->p = *p;
     r->grid = gi;
@@ -321,6 +393,8 @@ int pb_server_submit(pb_server S, const pb_solve_params* p, const double* x, con
     r->f = f;
     r->y = y;
     r->U = U;
+    r->pin_in = page_locked(x) && page_locked(f) && (p->n_tgt <= 0 || page_locked(y));
+    r->pin_out = page_locked(U);
     r->t_sub = Clock::now();
     {
         std::lock_guard<std::mutex> lk(S->mu);
@@ -404,6 +478,8 @@ int pb_server_stats(pb_server S, pb_server_counters* out)
     out->mean_batch = out->batches ? (double)S->batched_instances.load() / out->batches : 0.0;
     out->device_bytes = S->device_bytes;
     out->slots = (int)S->slots.size();
+    out->kernels = S->kernels.load();
+    out->scheduler_busy_s = 1e-9 * (double)S->busy_ns.load();
     return PB_OK;
 }
 

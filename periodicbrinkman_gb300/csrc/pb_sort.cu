@@ -218,14 +218,22 @@ void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, 
 }
 
 // Work items of the real-space kernel: each cell row (c0, c1) of an instance
-// is walked along z and cut into items of <= 32 consecutive targets spanning
-// <= 8 cells (a cell with more than 32 targets gives items of its own).  One
-// thread per row start; counts first, then emission after a scan.
+// is walked along z and cut into row items of <= 32 consecutive targets
+// spanning <= 8 cells (a cell with more than 32 targets gives items of its
+// own).  Each row item becomes `G` = csplit work items, one per group of
+// stencil columns, so that small instances still fill the GPU.  One thread
+// per row start; counts first, then emission after a scan.
+// Item = {instance, first target, local row, count | za << 8 | zb << 16 | group << 24}.
 template <bool EMIT>
-__device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q, int rowl, int4* items, int k0,
-                         int& nitems)
+__device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q, int rowl, int G, int4* items,
+                         int k0, int cap, int& nitems)
 {
     int z = 0, k = 0;
+    auto emit = [&](int first, int count, int za, int zb) {
+        for (int g = 0; g < G; g++, k++)
+            if (EMIT && k0 + k < cap)
+                items[k0 + k] = make_int4(q, first, rowl, count | (za << 8) | (zb << 16) | (g << 24));
+    };
     while (z < nz) {
         int n = start[row0 + z + 1] - start[row0 + z];
         if (n == 0) {
@@ -234,8 +242,7 @@ __device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q,
         }
         if (n > 32) {
             int b = start[row0 + z];
-            for (int c = 0; c * 32 < n; c++, k++)
-                if (EMIT) items[k0 + k] = make_int4(q, b + 32 * c, rowl, min(32, n - 32 * c) | (z << 8) | (z << 16));
+            for (int c = 0; c * 32 < n; c++) emit(b + 32 * c, min(32, n - 32 * c), z, z);
             z++;
             continue;
         }
@@ -246,8 +253,7 @@ __device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q,
             tot += m;
             z++;
         }
-        if (EMIT) items[k0 + k] = make_int4(q, start[row0 + za], rowl, tot | (za << 8) | ((z - 1) << 16));
-        k++;
+        emit(start[row0 + za], tot, za, z - 1);
     }
     nitems = k;
 }
@@ -261,13 +267,14 @@ __global__ void k_count_items(const int* __restrict__ start, int ncell, const in
     const PbInst& I = inst[q];
     int local = c - I.cell_off;
     int n = 0;
-    if (local < I.ncell && local % I.nc[2] == 0) walk_row<false>(start, c, I.nc[2], q, local / I.nc[2], nullptr, 0, n);
+    if (local < I.ncell && local % I.nc[2] == 0)
+        walk_row<false>(start, c, I.nc[2], q, local / I.nc[2], max(1, I.csplit), nullptr, 0, 0, n);
     counts[c] = n;
 }
 
 __global__ void k_emit_items(const int* __restrict__ start, const int* __restrict__ item_start, int ncell,
                              const int* __restrict__ cell_offsets, const PbInst* __restrict__ inst, int ninst,
-                             int4* __restrict__ items)
+                             int4* __restrict__ items, int cap)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
@@ -276,7 +283,7 @@ __global__ void k_emit_items(const int* __restrict__ start, const int* __restric
     int local = c - I.cell_off;
     int n = 0;
     if (local < I.ncell && local % I.nc[2] == 0)
-        walk_row<true>(start, c, I.nc[2], q, local / I.nc[2], items, item_start[c], n);
+        walk_row<true>(start, c, I.nc[2], q, local / I.nc[2], max(1, I.csplit), items, item_start[c], cap, n);
 }
 
 void launch_count_items(const int* start, int ncell_tot, const int* cell_offsets, const PbInst* inst, int ninst,
@@ -287,11 +294,11 @@ void launch_count_items(const int* start, int ncell_tot, const int* cell_offsets
 }
 
 void launch_emit_items(const int* start, const int* item_start, int ncell_tot, const int* cell_offsets,
-                       const PbInst* inst, int ninst, int4* items, cudaStream_t s)
+                       const PbInst* inst, int ninst, int4* items, int cap, cudaStream_t s)
 {
     if (ncell_tot <= 0) return;
     k_emit_items<<<(ncell_tot + 255) / 256, 256, 0, s>>>(start, item_start, ncell_tot, cell_offsets, inst, ninst,
-                                                          items);
+                                                          items, cap);
 }
 
 }  // namespace pb

@@ -14,13 +14,8 @@
 #include <mutex>
 
 #include "pb_device.cuh"
+#include "pb_internal.h"
 #include "pb_kernels.h"
-#include "pbrinkman.h"
-
-namespace pb {
-int api_error(int code, const char* msg);
-int kspace_instance(const pb_solve_params& p, PbInst* inst);
-}  // namespace pb
 
 using namespace pb;
 

@@ -74,6 +74,7 @@ struct PbInst {
     int flags;
     int same;                 // targets are the sources
     int bucket;               // FFT size bucket
+    int csplit;               // real-space work items per row item (stencil columns split into groups)
     int pad;
 };
 

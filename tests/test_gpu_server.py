@@ -64,8 +64,9 @@ def test_slot_capacity_is_enforced():
 
 def test_server_mix_equals_alone_and_oracle():
     rng = np.random.default_rng(32)
+    # a 50 ms batching window: the burst of 24 requests is batched whatever the GPU speed
     with Server(precision="mixed", budget_bytes=8 << 30, max_batch=8, slots_per_grid=2, grids=(16, 32, 64),
-                max_src=20000, max_tgt=20000) as srv:
+                max_src=20000, max_tgt=20000, linger_us=50000) as srv:
         reqs, tickets = [], []
         for k in range(24):
             n = int(np.exp(rng.uniform(np.log(300), np.log(3000))))
