@@ -348,43 +348,102 @@ template void launch_gather<double>(const PbInst*, int, const int*, int, const v
                                     double*, cudaStream_t);
 
 // ---------------------------------------------------------------------------
-// Shared-memory Stockham FFT (radix 2)
+// Shared-memory Stockham FFT (radix 4, with one radix-2 stage when log2 N is odd)
 // ---------------------------------------------------------------------------
 // Transforms `nl` lines of length N held in smem: element (l, i) at
 // buf[l*ls + i*es].  Forward uses W_N^k = exp(-2 pi i k/N) from tw[k] (k < N/2);
 // inverse conjugates.  Unnormalised.  Returns the buffer holding the result.
 // Thread mapping: `lfast` puts the line index in the fastest thread dimension
-// (use when es == 1 is false, i.e. lines interleaved).
+// (use when es == 1 is false, i.e. lines interleaved).  Stage with sub-size Ns
+// (autosort): inputs j + r N/R, twiddles W_{R Ns}^{r k} (k = j mod Ns), output
+// (j - k) R + k + r Ns.
 template <class T2>
 __device__ T2* stockham(T2* a, T2* b, int N, int nl, int ls, int es, const T2* __restrict__ tw, bool inverse,
                         bool lfast)
 {
-    const int half = N >> 1;
-    const int total = nl * half;
-    for (int Ns = 1; Ns < N; Ns <<= 1) {
-        const int tstep = N / (2 * Ns);
+    int lgN = 0;
+    while ((1 << lgN) < N) lgN++;
+    const float inv_nl = 1.0f / (float)nl;
+    int Ns = 1;
+    if (lgN & 1) {  // radix 2 (no twiddles at Ns = 1)
+        const int half = N >> 1, total = nl * half;
         for (int wdx = threadIdx.x; wdx < total; wdx += blockDim.x) {
             int l, j;
             if (lfast) {
-                l = wdx % nl;
-                j = wdx / nl;
+                j = __float2int_rz(((float)wdx + 0.5f) * inv_nl);
+                l = wdx - j * nl;
             } else {
-                j = wdx % half;
-                l = wdx / half;
+                j = wdx & (half - 1);
+                l = wdx >> (lgN - 1);
             }
-            T2 a0 = a[l * ls + j * es], a1 = a[l * ls + (j + half) * es];
-            int k = j & (Ns - 1);
-            T2 w = tw[k * tstep];
-            if (inverse) w.y = -w.y;
-            a1 = cmul(a1, w);
-            int di = ((j - k) << 1) + k;
-            T2 s, d;
-            s.x = a0.x + a1.x;
-            s.y = a0.y + a1.y;
-            d.x = a0.x - a1.x;
-            d.y = a0.y - a1.y;
-            b[l * ls + di * es] = s;
-            b[l * ls + (di + Ns) * es] = d;
+            const T2 a0 = a[l * ls + j * es], a1 = a[l * ls + (j + half) * es];
+            T2 s0, d0;
+            s0.x = a0.x + a1.x;
+            s0.y = a0.y + a1.y;
+            d0.x = a0.x - a1.x;
+            d0.y = a0.y - a1.y;
+            b[l * ls + (2 * j) * es] = s0;
+            b[l * ls + (2 * j + 1) * es] = d0;
+        }
+        __syncthreads();
+        T2* t = a;
+        a = b;
+        b = t;
+        Ns = 2;
+    }
+    const int quarter = N >> 2, total = nl * quarter;
+    for (; Ns < N; Ns <<= 2) {
+        const int tstep = N / (4 * Ns);
+        for (int wdx = threadIdx.x; wdx < total; wdx += blockDim.x) {
+            int l, j;
+            if (lfast) {
+                j = __float2int_rz(((float)wdx + 0.5f) * inv_nl);
+                l = wdx - j * nl;
+            } else {
+                j = wdx & (quarter - 1);
+                l = wdx >> (lgN - 2);
+            }
+            T2 v0 = a[l * ls + j * es], v1 = a[l * ls + (j + quarter) * es], v2 = a[l * ls + (j + 2 * quarter) * es],
+               v3 = a[l * ls + (j + 3 * quarter) * es];
+            const int k = j & (Ns - 1);
+            if (Ns > 1) {
+                T2 w1 = tw[k * tstep];
+                if (inverse) w1.y = -w1.y;
+                const T2 w2 = cmul(w1, w1), w3 = cmul(w2, w1);
+                v1 = cmul(v1, w1);
+                v2 = cmul(v2, w2);
+                v3 = cmul(v3, w3);
+            }
+            T2 t0, t1, t2, t3;
+            t0.x = v0.x + v2.x;
+            t0.y = v0.y + v2.y;
+            t1.x = v0.x - v2.x;
+            t1.y = v0.y - v2.y;
+            t2.x = v1.x + v3.x;
+            t2.y = v1.y + v3.y;
+            // t3 = (v1 - v3) * (-i) forward, * (+i) inverse
+            const decltype(v1.x) ex = v1.x - v3.x, ey = v1.y - v3.y;
+            if (inverse) {
+                t3.x = -ey;
+                t3.y = ex;
+            } else {
+                t3.x = ey;
+                t3.y = -ex;
+            }
+            const int o = l * ls + (((j - k) << 2) + k) * es;
+            T2 X;
+            X.x = t0.x + t2.x;
+            X.y = t0.y + t2.y;
+            b[o] = X;
+            X.x = t1.x + t3.x;
+            X.y = t1.y + t3.y;
+            b[o + Ns * es] = X;
+            X.x = t0.x - t2.x;
+            X.y = t0.y - t2.y;
+            b[o + 2 * Ns * es] = X;
+            X.x = t1.x - t3.x;
+            X.y = t1.y - t3.y;
+            b[o + 3 * Ns * es] = X;
         }
         __syncthreads();
         T2* t = a;
