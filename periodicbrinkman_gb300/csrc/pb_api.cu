@@ -285,7 +285,7 @@ struct pb_plan_s {
         *perm_tmp_s = nullptr;
     int *cell_of_t = nullptr, *cnt_t = nullptr, *start_t = nullptr, *fill_t = nullptr, *perm_t = nullptr,
         *perm_tmp_t = nullptr;
-    int *chunks = nullptr, *chunk_start = nullptr, *scan_tmp = nullptr, *counter = nullptr;
+    int *scan_tmp = nullptr, *counter = nullptr;
     int4* items = nullptr;
     void *spos_a = nullptr, *spos_b = nullptr, *sfrc = nullptr, *tpos_a = nullptr, *tpos_b = nullptr;
     double *u_real = nullptr, *fsum = nullptr;
@@ -350,7 +350,7 @@ size_t plan_layout(pb_plan_s* P, bool assign)
         o_pt = L.take<int>(nt);
         o_ptt = L.take<int>(nt);
     }
-    size_t o_ch = L.take<int>(nc + 1), o_chs = L.take<int>(nc + 2), o_st = L.take<int>(scan_tmp_ints(nc + 1));
+    size_t o_st = L.take<int>(scan_tmp_ints(nc + 1));
     const int item_cap = 4 * nt + 4096;
     size_t o_cnt = L.take<int>(4), o_it = L.take<int4>(item_cap);
     size_t o_sa, o_sb = 0, o_sf, o_ta = 0, o_tb = 0;
@@ -411,8 +411,6 @@ size_t plan_layout(pb_plan_s* P, bool assign)
             P->start_t = P->start_s;
             P->perm_t = P->perm_s;
         }
-        P->chunks = (int*)(A + o_ch);
-        P->chunk_start = (int*)(A + o_chs);
         P->scan_tmp = (int*)(A + o_st);
         P->counter = (int*)(A + o_cnt);
         P->items = (int4*)(A + o_it);
@@ -666,9 +664,9 @@ void bin_and_sort(pb_plan_s* P, const double* pos, int n, const int* d_off, int*
     cudaMemsetAsync(cnt, 0, sizeof(int) * (P->ncell + 1), s);
     cudaMemsetAsync(fill, 0, sizeof(int) * (P->ncell + 1), s);
     launch_bin(pos, n, d_off, P->d_inst, P->count, cell_of, cnt, s);
-    launch_exclusive_scan(cnt, start, P->ncell, P->scan_tmp, s);
+    launch_exclusive_scan(cnt, start, P->ncell, P->scan_tmp, s, P->d_cell_off + P->count);
     launch_scatter(cell_of, n, d_off + P->count, start, fill, perm_tmp, s);
-    launch_sort_cells(perm_tmp, perm, start, P->ncell, s);
+    launch_sort_cells(perm_tmp, perm, start, P->ncell, P->d_cell_off + P->count, P->nsm, s);
 }
 
 void record(pb_plan_s* P, int k, cudaStream_t s)
@@ -700,13 +698,11 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
             launch_prepare_fp64(P->ypack, nullptr, P->perm_t, P->n_tgt, P->d_tgt_off, P->d_inst, P->count,
                                 (Dbl4*)P->tpos_a, nullptr, s);
     }
-    launch_count_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->chunks, s);
-    launch_exclusive_scan(P->chunks, P->chunk_start, P->ncell, P->scan_tmp, s);
-    launch_emit_items(P->start_t, P->chunk_start, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items,
-                      P->item_cap, s);
+    launch_build_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items, P->item_cap,
+                       P->counter + 1, P->nsm, s);
     record(P, 1, s);
     if (P->any_real) {
-        const int* nitems = P->chunk_start + P->ncell;
+        const int* nitems = P->counter + 1;
         if (mixed)
             launch_real_mixed(P->npoly, P->d_inst, P->d_tab, P->items, nitems, P->item_cap,
                               (const float4*)P->spos_a, (const float4*)P->spos_b, (const float4*)P->sfrc, P->start_s,
@@ -749,7 +745,7 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
         record(P, 4, s);
     }
     record(P, 5, s);
-    if (P->any_zero) launch_force_sums(P->f, P->d_src_off, P->count, P->fsum, s);
+    if (P->any_zero) launch_force_sums(P->d_inst, P->f, P->d_src_off, P->count, P->fsum, s);
     if (mixed)
         launch_combine_mixed(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->perm_t, P->u_real, (const float*)P->u_k,
                              P->any_real, P->any_k, P->fsum, P->d_tab, P->f, P->d_src_off, P->U, s);

@@ -16,14 +16,16 @@ namespace pb {
 void launch_bin(const double* pos, int ncap, const int* offsets, const PbInst* inst, int ninst,
                 int* cell_of, int* counts, cudaStream_t s);
 // Exclusive scan of n ints into out (out has n+1 entries; out[n] = total).
-// tmp must hold scan_tmp_ints(n) ints.
+// tmp must hold scan_tmp_ints(n) ints.  With n_act (device), only the first
+// *n_act entries may be nonzero and out is valid up to index *n_act.
 size_t scan_tmp_ints(int n);
-void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s);
+void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s, const int* n_act = nullptr);
 // perm[start[c] + k] = particle, fill must be zeroed.
 void launch_scatter(const int* cell_of, int ncap, const int* ntot, const int* start, int* fill, int* perm,
                     cudaStream_t s);
-// Sort each cell's perm entries ascending (deterministic order).
-void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell, cudaStream_t s);
+// Sort each cell's perm entries ascending (deterministic order); *ncell = actual cells.
+void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap, const int* ncell, int nsm,
+                       cudaStream_t s);
 // Sorted particle records.  Mixed: pos_hi (x,y,z, w = instance bits), pos_lo, frc.
 void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                           const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out,
@@ -33,10 +35,10 @@ void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, 
 // Work items: up to 32 consecutive targets of one cell row spanning <= 8 cells,
 // times csplit stencil column groups:
 // int4 {inst, first target, local row, count | za << 8 | zb << 16 | group << 24}.
-void launch_count_items(const int* start, int ncell_tot, const int* cell_offsets, const PbInst* inst, int ninst,
-                        int* counts, cudaStream_t s);
-void launch_emit_items(const int* start, const int* item_start, int ncell_tot, const int* cell_offsets,
-                       const PbInst* inst, int ninst, int4* items, int cap, cudaStream_t s);
+// Builds the items of all row-start cells (cell_offsets[ninst] = actual cells);
+// *nitems = number of items (may exceed cap: the real-space kernels clamp).
+void launch_build_items(const int* start, int ncell_cap, const int* cell_offsets, const PbInst* inst, int ninst,
+                        int4* items, int cap, int* nitems, int nsm, cudaStream_t s);
 
 // ---- real space (pb_real.cu) ----
 // Mixed precision: FP32 polynomial kernel, hi/lo displacements, Kahan sums.
@@ -81,7 +83,8 @@ void launch_combine_fp64(const PbInst* inst, int ninst, const int* tgt_offsets, 
                          const double* u_real, const double* u_k, int use_real, int use_k, const double* fsum,
                          const PbTables* tab, const double* frc, const int* src_offsets, double* U, cudaStream_t s);
 // Per-instance force sums (for the optional k = 0 mode): out[3*q + c] = sum f.
-void launch_force_sums(const double* frc, const int* offsets, int ninst, double* out, cudaStream_t s);
+void launch_force_sums(const PbInst* inst, const double* frc, const int* offsets, int ninst, double* out,
+                       cudaStream_t s);
 
 // ---- dense mobility matrix (pb_dense.cu) ----
 int launch_dense_matrix(double* dA, const double* dx, int m, const double* dx0, int n, double a, double d, double e,

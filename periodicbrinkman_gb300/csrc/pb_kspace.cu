@@ -929,31 +929,30 @@ void launch_combine_fp64(const PbInst* inst, int ninst, const int* tgt_offsets, 
                                                        use_k, fsum, tab, frc, src_offsets, U);
 }
 
-__global__ void k_force_sums(const double* __restrict__ frc, const int* __restrict__ offsets, int ninst,
-                             double* __restrict__ out)
+// Per-instance force sums for the k = 0 mode (only instances that ask for it):
+// blockIdx.y = instance, blocks stride over its sources, FP64 atomics.
+__global__ void k_force_sums(const PbInst* __restrict__ inst, const double* __restrict__ frc,
+                             const int* __restrict__ offsets, double* __restrict__ out)
 {
-    int q = blockIdx.x;
-    if (q >= ninst) return;
-    int b = offsets[q], e = offsets[q + 1];
+    const int q = blockIdx.y;
+    if (!(inst[q].flags & 4)) return;
+    const int b = offsets[q], e = offsets[q + 1];
     double s[3] = {0, 0, 0};
-    for (int p = b + threadIdx.x; p < e; p += blockDim.x)
+    for (int p = b + blockIdx.x * blockDim.x + threadIdx.x; p < e; p += gridDim.x * blockDim.x)
         for (int c = 0; c < 3; c++) s[c] += frc[3 * (size_t)p + c];
-    __shared__ double red[3][256];
-    for (int c = 0; c < 3; c++) red[c][threadIdx.x] = s[c];
-    __syncthreads();
-    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-        if ((int)threadIdx.x < st)
-            for (int c = 0; c < 3; c++) red[c][threadIdx.x] += red[c][threadIdx.x + st];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0)
-        for (int c = 0; c < 3; c++) out[3 * q + c] = red[c][0];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_xor_sync(kFull, s[c], o);
+    if ((threadIdx.x & 31) == 0)
+        for (int c = 0; c < 3; c++) atomicAdd(&out[3 * q + c], s[c]);
 }
 
-void launch_force_sums(const double* frc, const int* offsets, int ninst, double* out, cudaStream_t s)
+void launch_force_sums(const PbInst* inst, const double* frc, const int* offsets, int ninst, double* out,
+                       cudaStream_t s)
 {
     if (ninst <= 0) return;
-    k_force_sums<<<ninst, 256, 0, s>>>(frc, offsets, ninst, out);
+    cudaMemsetAsync(out, 0, 3 * sizeof(double) * (size_t)ninst, s);
+    k_force_sums<<<dim3(16, (unsigned)ninst), 256, 0, s>>>(inst, frc, offsets, out);
 }
 
 }  // namespace pb

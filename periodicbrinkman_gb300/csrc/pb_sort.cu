@@ -59,9 +59,16 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums)
     return base + x - v;
 }
 
-__global__ void k_scan_blocks(const int* __restrict__ in, int* __restrict__ out, int n, int* __restrict__ block_sums)
+// n_act (optional): entries at and beyond *n_act are zero and their outputs are
+// not needed past index *n_act, so blocks that start beyond it only report 0.
+__global__ void k_scan_blocks(const int* __restrict__ in, int* __restrict__ out, int n, int* __restrict__ block_sums,
+                              const int* __restrict__ n_act)
 {
     __shared__ int ws[32];
+    if (n_act && blockIdx.x * kScanBlock > *n_act) {
+        if (threadIdx.x == 0) block_sums[blockIdx.x] = 0;
+        return;
+    }
     int i = blockIdx.x * kScanBlock + threadIdx.x;
     int v = i < n ? in[i] : 0;
     int ex = block_exclusive_scan(v, ws);
@@ -69,15 +76,18 @@ __global__ void k_scan_blocks(const int* __restrict__ in, int* __restrict__ out,
     if (threadIdx.x == blockDim.x - 1) block_sums[blockIdx.x] = ex + v;
 }
 
-__global__ void k_scan_add(int* __restrict__ out, int n, const int* __restrict__ block_offsets)
+__global__ void k_scan_add(int* __restrict__ out, int n, const int* __restrict__ block_offsets,
+                           const int* __restrict__ n_act)
 {
+    if (n_act && blockIdx.x * kScanBlock > *n_act) return;
     int i = blockIdx.x * kScanBlock + threadIdx.x;
     if (i < n) out[i] += block_offsets[blockIdx.x];
 }
 
-__global__ void k_set_total(int* out, int n, const int* in)
+__global__ void k_set_total(int* out, int n, const int* in, const int* n_act)
 {
-    // out[n] = out[n-1] + in[n-1]
+    // out[n] = out[n-1] + in[n-1] (with fewer actual entries, out[n_act] is the total already)
+    if (n_act && *n_act < n) return;
     out[n] = (n > 0) ? out[n - 1] + in[n - 1] : 0;
 }
 
@@ -93,26 +103,26 @@ size_t scan_tmp_ints(int n)
     return total + 4;
 }
 
-static void scan_rec(const int* in, int* out, int n, int* tmp, cudaStream_t s)
+static void scan_rec(const int* in, int* out, int n, int* tmp, const int* n_act, cudaStream_t s)
 {
     int nb = (n + kScanBlock - 1) / kScanBlock;
     int* sums = tmp;
     int* sums_scan = tmp + nb + 1;
-    k_scan_blocks<<<nb, kScanBlock, 0, s>>>(in, out, n, sums);
+    k_scan_blocks<<<nb, kScanBlock, 0, s>>>(in, out, n, sums, n_act);
     if (nb > 1) {
-        scan_rec(sums, sums_scan, nb, tmp + 2 * (size_t)nb + 2, s);
-        k_scan_add<<<nb, kScanBlock, 0, s>>>(out, n, sums_scan);
+        scan_rec(sums, sums_scan, nb, tmp + 2 * (size_t)nb + 2, nullptr, s);
+        k_scan_add<<<nb, kScanBlock, 0, s>>>(out, n, sums_scan, n_act);
     }
 }
 
-void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s)
+void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s, const int* n_act)
 {
     if (n <= 0) {
         cudaMemsetAsync(out, 0, sizeof(int), s);
         return;
     }
-    scan_rec(in, out, n, tmp, s);
-    k_set_total<<<1, 1, 0, s>>>(out, n, in);
+    scan_rec(in, out, n, tmp, n_act, s);
+    k_set_total<<<1, 1, 0, s>>>(out, n, in, n_act);
 }
 
 __global__ void k_scatter(const int* __restrict__ cell_of, const int* __restrict__ ntot, const int* __restrict__ start,
@@ -132,36 +142,40 @@ void launch_scatter(const int* cell_of, int ncap, const int* ntot, const int* st
     k_scatter<<<(ncap + 255) / 256, 256, 0, s>>>(cell_of, ntot, start, fill, perm);
 }
 
-// Rank sort of each cell's entries (warp per cell): entry v goes to slot
-// start + #{u in cell : u < v}.  Entries are distinct particle indices.
+// Rank sort of each cell's entries (a warp per cell, persistent over the
+// actual cells): entry v goes to slot start + #{u in cell : u < v}.  Entries
+// are distinct particle indices.
 __global__ void k_sort_cells(const int* __restrict__ perm_in, int* __restrict__ perm_out,
-                             const int* __restrict__ start, int ncell)
+                             const int* __restrict__ start, const int* __restrict__ ncell_p)
 {
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (warp >= ncell) return;
-    int b = start[warp], e = start[warp + 1], n = e - b;
-    if (n <= 1) {
-        if (n == 1 && lane == 0) perm_out[b] = perm_in[b];
-        return;
-    }
-    if (n > 4096) {  // very large cells keep the scatter order
-        for (int i = lane; i < n; i += 32) perm_out[b + i] = perm_in[b + i];
-        return;
-    }
-    for (int i = lane; i < n; i += 32) {
-        int v = perm_in[b + i], rank = 0;
-        for (int j = 0; j < n; j++) rank += (perm_in[b + j] < v);
-        perm_out[b + rank] = v;
+    const int ncell = *ncell_p;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < ncell; cell += nwarps) {
+        const int b = start[cell], e = start[cell + 1], n = e - b;
+        if (n <= 1) {
+            if (n == 1 && lane == 0) perm_out[b] = perm_in[b];
+            continue;
+        }
+        if (n > 4096) {  // very large cells keep the scatter order
+            for (int i = lane; i < n; i += 32) perm_out[b + i] = perm_in[b + i];
+            continue;
+        }
+        for (int i = lane; i < n; i += 32) {
+            int v = perm_in[b + i], rank = 0;
+            for (int j = 0; j < n; j++) rank += (perm_in[b + j] < v);
+            perm_out[b + rank] = v;
+        }
     }
 }
 
-void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell, cudaStream_t s)
+void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap, const int* ncell, int nsm,
+                       cudaStream_t s)
 {
-    if (ncell <= 0) return;
-    long long threads = (long long)ncell * 32;
-    int blocks = (int)((threads + 255) / 256);
-    k_sort_cells<<<blocks, 256, 0, s>>>(perm, perm_tmp, start, ncell);
+    if (ncell_cap <= 0) return;
+    long long blocks = ((long long)ncell_cap * 32 + 255) / 256;
+    if (blocks > (long long)nsm * 16) blocks = (long long)nsm * 16;
+    k_sort_cells<<<(int)blocks, 256, 0, s>>>(perm, perm_tmp, start, ncell);
 }
 
 __global__ void k_prepare_mixed(const double* __restrict__ pos, const double* __restrict__ frc,
@@ -222,7 +236,7 @@ void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, 
 // spanning <= 8 cells (a cell with more than 32 targets gives items of its
 // own).  Each row item becomes `G` = csplit work items, one per group of
 // stencil columns, so that small instances still fill the GPU.  One thread
-// per row start; counts first, then emission after a scan.
+// per row start: a counting walk, then the emitting walk into its range.
 // Item = {instance, first target, local row, count | za << 8 | zb << 16 | group << 24}.
 template <bool EMIT>
 __device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q, int rowl, int G, int4* items,
@@ -258,47 +272,35 @@ __device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q,
     nitems = k;
 }
 
-__global__ void k_count_items(const int* __restrict__ start, int ncell, const int* __restrict__ cell_offsets,
-                              const PbInst* __restrict__ inst, int ninst, int* __restrict__ counts)
+// Row items of every row start cell (persistent over the actual cells); each
+// row reserves its range of the item array with one atomic.
+__global__ void k_build_items(const int* __restrict__ start, const int* __restrict__ cell_offsets,
+                              const PbInst* __restrict__ inst, int ninst, int4* __restrict__ items, int cap,
+                              int* __restrict__ nitems)
 {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    int q = find_instance(cell_offsets, ninst, c);
-    const PbInst& I = inst[q];
-    int local = c - I.cell_off;
-    int n = 0;
-    if (local < I.ncell && local % I.nc[2] == 0)
-        walk_row<false>(start, c, I.nc[2], q, local / I.nc[2], max(1, I.csplit), nullptr, 0, 0, n);
-    counts[c] = n;
+    const int ncell = cell_offsets[ninst];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+        const int q = find_instance(cell_offsets, ninst, c);
+        const PbInst& I = inst[q];
+        const int local = c - I.cell_off;
+        if (local >= I.ncell || local % I.nc[2] != 0) continue;
+        const int G = max(1, I.csplit);
+        int n = 0;
+        walk_row<false>(start, c, I.nc[2], q, local / I.nc[2], G, nullptr, 0, 0, n);
+        if (n == 0) continue;
+        const int k0 = atomicAdd(nitems, n);
+        walk_row<true>(start, c, I.nc[2], q, local / I.nc[2], G, items, k0, cap, n);
+    }
 }
 
-__global__ void k_emit_items(const int* __restrict__ start, const int* __restrict__ item_start, int ncell,
-                             const int* __restrict__ cell_offsets, const PbInst* __restrict__ inst, int ninst,
-                             int4* __restrict__ items, int cap)
+void launch_build_items(const int* start, int ncell_cap, const int* cell_offsets, const PbInst* inst, int ninst,
+                        int4* items, int cap, int* nitems, int nsm, cudaStream_t s)
 {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    int q = find_instance(cell_offsets, ninst, c);
-    const PbInst& I = inst[q];
-    int local = c - I.cell_off;
-    int n = 0;
-    if (local < I.ncell && local % I.nc[2] == 0)
-        walk_row<true>(start, c, I.nc[2], q, local / I.nc[2], max(1, I.csplit), items, item_start[c], cap, n);
-}
-
-void launch_count_items(const int* start, int ncell_tot, const int* cell_offsets, const PbInst* inst, int ninst,
-                        int* counts, cudaStream_t s)
-{
-    if (ncell_tot <= 0) return;
-    k_count_items<<<(ncell_tot + 255) / 256, 256, 0, s>>>(start, ncell_tot, cell_offsets, inst, ninst, counts);
-}
-
-void launch_emit_items(const int* start, const int* item_start, int ncell_tot, const int* cell_offsets,
-                       const PbInst* inst, int ninst, int4* items, int cap, cudaStream_t s)
-{
-    if (ncell_tot <= 0) return;
-    k_emit_items<<<(ncell_tot + 255) / 256, 256, 0, s>>>(start, item_start, ncell_tot, cell_offsets, inst, ninst,
-                                                          items, cap);
+    cudaMemsetAsync(nitems, 0, sizeof(int), s);
+    if (ncell_cap <= 0) return;
+    long long blocks = ((long long)ncell_cap + 255) / 256;
+    if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+    k_build_items<<<(int)blocks, 256, 0, s>>>(start, cell_offsets, inst, ninst, items, cap, nitems);
 }
 
 }  // namespace pb
