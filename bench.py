@@ -51,6 +51,8 @@ SERVE = dict(name="serve_stream_20000req_2000per_s_N1e3-2e5_targets_N/2_alpha1-5
 SINGLE = dict(name="single_solve_N1e5_uniform_alpha20_eps0.005_grid128_P12_tol1e-6_mixed", n=100_000, L=1.0,
               alpha=20.0, eps=0.005, M=128, P=12, tol=1e-6, seed=2000)
 METRIC = "Brinkman solves/s + p50/p99 latency at <=1e-6 rel err, served vs plain FP64"
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_real_mixed launch of the N = 1e5 solve
+REAL_DRAM_BYTES = 7.34e6
 
 
 def peaks():
@@ -312,9 +314,11 @@ def roofline_single(torch, local, steps_warm=3):
         nsm = torch.cuda.get_device_properties(local).multi_processor_count
         fp32_peak = nsm * 128 * 2 * (pk.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
         roof = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
-                "traffic": None, "kernel": "k_real_mixed",
+                "traffic": REAL_DRAM_BYTES, "kernel": "k_real_mixed",
                 "note": "FP32 SIMT pair kernel (no tensor-core work in this path); 64 flop per pair inside rc; "
-                        "peak = SMs x 128 lanes x 2 flop x max SM clock (nominal, no measured FP32 peak exists)"}
+                        "peak = SMs x 128 lanes x 2 flop x max SM clock (nominal: no measured FP32 peak exists); "
+                        "traffic = ncu dram read+write bytes of one launch of this workload "
+                        "(profiles/k_real_mixed_single_solve_N1e5.md)"}
     else:
         by = 4.0 * 3 * M3 * 6 + 36.0 * n + 24.0 * n
         i = names.index(dom)
@@ -447,8 +451,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="serve", choices=["serve", "single"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", action="store_true",
-                    help="run the single-solve plan twice (eager, then capture+replay) and exit: for ncu")
+    ap.add_argument("--profile", nargs="?", const="single", choices=["single", "slot"],
+                    help="for ncu: run the single-solve plan twice (eager, then capture+replay), or (slot) one "
+                         "128^3 serving slot holding two requests of the stream three times, and exit")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -461,6 +466,9 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if args.profile == "slot":
+        profile_slot(torch)
+        return
     if args.profile:
         w = SINGLE
         x, f = single_inputs(w)
@@ -538,6 +546,34 @@ def main():
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+def profile_slot(torch):
+    """One 128^3 serving slot (the server's capacity) with two requests of the stream, executed three times."""
+    from periodicbrinkman_gb300.api import bind, make_params, make_slot
+
+    w = SERVE
+    arrive, N, alpha, eps, tol = gen_stream(w)
+    ks = [k for k in range(400) if 60000 < N[k] < 120000][:2]
+    pool = InputPool(w["nmax"], sets=2)
+    slot = make_slot(128, max_instances=16, max_src=w["nmax"], max_tgt=w["nmax"] // 2 + 1,
+                     max_cells=min(1 << 21, 16 * 64 ** 3))
+    ps, xs, fs, ys = [], [], [], []
+    for k in ks:
+        x, f, y = pool.get(int(k), int(N[k]))
+        ps.append(make_params(x.shape[0], 1.0, float(alpha[k]), float(eps[k]), n_tgt=y.shape[0],
+                              tol=float(tol[k]), M=128))
+        xs.append(x)
+        fs.append(f)
+        ys.append(y)
+    bind(slot, ps)
+    X, F, Y = (torch.from_numpy(np.concatenate(a)).cuda() for a in (xs, fs, ys))
+    for _ in range(3):
+        slot.execute(X, F, Y)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "slot_128_two_stream_requests", "n_src": [int(N[k]) for k in ks],
+                      "kernels_per_execution": slot.kernel_count}))
+    slot.close()
 
 
 def _cpu_single():

@@ -264,15 +264,20 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     float s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0;
     for (int id = lane; id < P2 * R; id += 32) {
         const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
-        const float wyz = wgt[w][1][py] * wgt[w][2][pz];
         const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
+        // one x row of the window in plain FP32 (<= 32 same-sign-weighted terms), rows Kahan-summed
+        float r0 = 0, r1 = 0, r2 = 0;
         for (int px = xs; px < Px; px += R) {
-            const float wv = wgt[w][0][px] * wyz;
+            const float wx = wgt[w][0][px];
             const float4 v = __ldg(g4 + (size_t)gidx[w][0][px] * M12 + oyz);
-            kahan_add(s0, c0, wv * v.x);
-            kahan_add(s1, c1, wv * v.y);
-            kahan_add(s2, c2, wv * v.z);
+            r0 = fmaf(wx, v.x, r0);
+            r1 = fmaf(wx, v.y, r1);
+            r2 = fmaf(wx, v.z, r2);
         }
+        const float wyz = wgt[w][1][py] * wgt[w][2][pz];
+        kahan_add(s0, c0, wyz * r0);
+        kahan_add(s1, c1, wyz * r1);
+        kahan_add(s2, c2, wyz * r2);
     }
     s0 -= c0;
     s1 -= c1;
