@@ -426,6 +426,7 @@ size_t plan_layout(pb_plan_s* P, bool assign)
         }
         P->u_real = (double*)(A + o_ur);
         P->item_cap = item_cap;
+
         P->u_k = A + o_uk;
         P->fsum = (double*)(A + o_fsum);
         P->grid = A + o_grid;
@@ -446,6 +447,9 @@ void set_inst_fields(PbInst& I, const pb_solve_params& p, const Resolved& R, int
         I.L[a] = p.L[a];
         I.h[a] = R.h[a];
         I.gh[a] = p.L[a] / R.M[a];
+        I.gih[a] = R.M[a] / p.L[a];
+        I.iL[a] = 1.0 / p.L[a];
+        I.ih[a] = 1.0 / R.h[a];
         I.nc[a] = R.nc[a];
         I.S[a] = R.S[a];
         I.M[a] = R.M[a];

@@ -42,6 +42,16 @@ __device__ __forceinline__ double wrap_coord(double v, double L)
     return w;
 }
 
+// As wrap_coord with the inverse length given (no FP64 division; the
+// rounding of v * iL is absorbed by the range fix-up).
+__device__ __forceinline__ double wrap_coord_r(double v, double L, double iL)
+{
+    double w = fma(-L, floor(v * iL), v);
+    if (w >= L) w -= L;
+    if (w < 0) w = 0;
+    return w;
+}
+
 __device__ __forceinline__ int find_instance(const int* offsets, int ninst, int idx)
 {
     // offsets: ninst+1 ascending prefix; returns q with offsets[q] <= idx < offsets[q+1]

@@ -210,6 +210,37 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
 
 // FP32 grids interleave the three components of a point in one float4, so a
 // point costs one vector atomic (spread) or one 16-byte load (gather).
+// FP32-grid window of a point given as FP32 hi/lo pairs: lane a < 3 resolves
+// axis a in FP64 (the grid cell holding x by a multiply with the inverse
+// spacing, and the offset of x from the window start), the other lanes take
+// those by shuffle, and lane p < P computes weight p in FP32 from the offset.
+// No FP64 division: the FP64 pipe of this GPU runs at a small fraction of
+// the FP32 rate.
+__device__ __forceinline__ void window_f32(const PbInst& I, float4 h4, float4 l4, int lane, float (*wgt)[kMaxP],
+                                           int (*idx)[kMaxP])
+{
+    int g0 = 0;
+    float base = 0.f;
+    if (lane < 3) {
+        const double xa = (double)(lane == 0 ? h4.x : lane == 1 ? h4.y : h4.z) +
+                          (double)(lane == 0 ? l4.x : lane == 1 ? l4.y : l4.z);
+        const int c = min(max((int)floor(xa * I.gih[lane]), 0), I.M[lane] - 1);
+        g0 = c - I.Pa[lane] / 2 + 1;
+        base = (float)fma(-(double)g0, I.gh[lane], xa);
+    }
+    const float inv_eta = (float)(1.0 / I.eta);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int ga = __shfl_sync(kFull, g0, a);
+        const float ba = __shfl_sync(kFull, base, a);
+        if (lane < I.Pa[a]) {
+            const float dx = fmaf(-(float)lane, (float)I.gh[a], ba);
+            wgt[a][lane] = expf(-dx * dx * inv_eta);
+            idx[a][lane] = (ga + lane) & (I.M[a] - 1);  // grids are powers of two
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kSpreadWarps * 32)
     k_spread_f4(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
                 const float4* __restrict__ pb, const float4* __restrict__ frc, float* __restrict__ grid)
@@ -220,12 +251,9 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int s = spread_order(blockIdx.x * kSpreadWarps + w, ntot);
     if (s < 0) return;
-    double x[3], fv[3];
-    int q;
-    load_pos(pa, pb, s, x, q);
-    load_frc(frc, s, fv);
-    const PbInst& I = inst[q];
-    window<float>(I, x, lane, wgt[w], gidx[w]);
+    const float4 h4 = pa[s], l4 = pb[s], fv = frc[s];
+    const PbInst& I = inst[__float_as_int(h4.w)];
+    window_f32(I, h4, l4, lane, wgt[w], gidx[w]);
     __syncwarp();
     const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
     const size_t M12 = (size_t)I.M[1] * I.M[2];
@@ -233,7 +261,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     for (int id = lane; id < P2 * R; id += 32) {
         const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
         const float wyz = wgt[w][1][py] * wgt[w][2][pz];
-        const float h0 = (float)fv[0] * wyz, h1 = (float)fv[1] * wyz, h2 = (float)fv[2] * wyz;
+        const float h0 = fv.x * wyz, h1 = fv.y * wyz, h2 = fv.z * wyz;
         const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
         for (int px = xs; px < Px; px += R) {
             const float wx = wgt[w][0][px];
@@ -252,11 +280,9 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int s = blockIdx.x * kSpreadWarps + w;
     if (s >= ntot) return;
-    double x[3];
-    int q;
-    load_pos(pa, pb, s, x, q);
-    const PbInst& I = inst[q];
-    window<float>(I, x, lane, wgt[w], gidx[w]);
+    const float4 h4 = pa[s], l4 = pb[s];
+    const PbInst& I = inst[__float_as_int(h4.w)];
+    window_f32(I, h4, l4, lane, wgt[w], gidx[w]);
     __syncwarp();
     const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
     const size_t M12 = (size_t)I.M[1] * I.M[2];
@@ -772,7 +798,7 @@ __global__ void k_fft_x_green(typename Cx<T>::t* __restrict__ spec, const PbInst
             *v2 = T2{0, 0};
             continue;
         }
-        T kx = (T)(tpx * nx), ky = (T)(tpy * ny), kzv = (T)(tpz * kz);
+        T kx = (T)tpx * (T)nx, ky = (T)tpy * (T)ny, kzv = (T)tpz * (T)kz;  // in T: no FP64 work on FP32 grids
         T kn = kx * kx + ky * ky + kzv * kzv;
         T s = kfac * ((T)1 + a1oa2 * kn) * exp(-kn * gexp) / (kn * (kn + (T)a2));
         T2 A0 = *v0, A1 = *v1, A2 = *v2;

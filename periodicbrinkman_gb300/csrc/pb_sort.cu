@@ -15,8 +15,8 @@ __global__ void k_bin(const double* __restrict__ pos, const int* __restrict__ of
     int c[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        double w = wrap_coord(pos[3 * (size_t)p + a], I.L[a]);
-        int ci = (int)(w / I.h[a]);
+        double w = wrap_coord_r(pos[3 * (size_t)p + a], I.L[a], I.iL[a]);
+        int ci = (int)(w * I.ih[a]);
         c[a] = ci >= I.nc[a] ? I.nc[a] - 1 : ci;
     }
     int g = I.cell_off + (c[0] * I.nc[1] + c[1]) * I.nc[2] + c[2];
@@ -190,7 +190,7 @@ __global__ void k_prepare_mixed(const double* __restrict__ pos, const double* __
     const PbInst& I = inst[q];
     float hi[3], lo[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++) split_double(wrap_coord(pos[3 * (size_t)p + a], I.L[a]), hi[a], lo[a]);
+    for (int a = 0; a < 3; a++) split_double(wrap_coord_r(pos[3 * (size_t)p + a], I.L[a], I.iL[a]), hi[a], lo[a]);
     pos_hi[sidx] = make_float4(hi[0], hi[1], hi[2], __int_as_float(q));
     pos_lo[sidx] = make_float4(lo[0], lo[1], lo[2], 0.f);
     if (frc)
@@ -219,7 +219,7 @@ __global__ void k_prepare_fp64(const double* __restrict__ pos, const double* __r
     const PbInst& I = inst[q];
     double w[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++) w[a] = wrap_coord(pos[3 * (size_t)p + a], I.L[a]);
+    for (int a = 0; a < 3; a++) w[a] = wrap_coord_r(pos[3 * (size_t)p + a], I.L[a], I.iL[a]);
     pos_out[sidx] = make_dbl4(w[0], w[1], w[2], (double)q);
     if (frc) frc_out[sidx] = make_dbl4(frc[3 * (size_t)p], frc[3 * (size_t)p + 1], frc[3 * (size_t)p + 2], 0.0);
 }

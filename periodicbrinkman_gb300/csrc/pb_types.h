@@ -57,6 +57,9 @@ struct PbInst {
     double rc;
     double h[3];      // cell widths
     double gh[3];     // grid spacings
+    double gih[3];    // inverse grid spacings (M / L)
+    double iL[3];     // inverse box lengths
+    double ih[3];     // inverse cell widths
     double eta;       // Gaussian spreading parameter: exp(-r^2/eta)
     double kfac;      // spectral prefactor (normalisations of spread, FFT, gather)
     double zero_mode[3];  // k = 0 mean-flow velocity added to every target (or 0)
