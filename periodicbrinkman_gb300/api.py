@@ -13,9 +13,11 @@ import numpy as np
 from ._lib import (
     PB_DEVICE,
     PB_HOST,
+    PB_OK,
     PB_PREC_FP64,
     PB_PREC_MIXED,
     InstanceInfo,
+    PbError,
     ServerConfig,
     ServerCounters,
     SlotConfig,
@@ -234,9 +236,10 @@ class Server:
         """Wait for a request; returns (U, latency_s) and forgets it."""
         status, lat = C.c_int(), C.c_double()
         check(lib().pb_server_wait(self._h, ticket, float(timeout), C.byref(status), C.byref(lat)))
-        check(status.value)
         U = self._live.pop(ticket)[3]
         lib().pb_server_release(self._h, ticket)
+        if status.value != PB_OK:
+            raise PbError(status.value, f"request {ticket} failed")
         return U, lat.value
 
     def drain(self, timeout: float = 600.0) -> None:

@@ -183,34 +183,59 @@ int resolve(const pb_solve_params& p, Resolved& R)
     };
     double best = 1e300, d = p.d > 0 ? p.d : Lmin / 8;
     Support sup = cands.front();
-    for (const Support& cand : cands) {
+    // modelled cost of (support, d); +inf when the grid or the fixed-grid limits exclude it
+    auto cost_at = [&](const Support& cand, double dd) {
         const double u = std::max(cand.u, uk);
-        for (int k = 0; k < (p.d > 0 ? 1 : 160); k++) {
-            const double dd = p.d > 0 ? p.d : Lmin * std::pow(2.0, -1.0 - k * 0.0625);
+        int M[3];
+        grid_for(p, dd, u, kconst, M);
+        bool ok = true;
+        for (int a = 0; a < 3; a++) {
+            if (M[a] > 1024 || cand.P > M[a]) ok = false;
+            if (p.M[a] > 0 && p.d == 0) {  // fixed grid: d must satisfy its k-space and spreading limits
+                double kmax = 2 * M_PI * (M[a] / 2 - 1) / p.L[a];
+                if (kmax * dd / 2 < std::sqrt(kconst)) ok = false;
+                if (p.L[a] / M[a] * u > dd) ok = false;
+            }
+        }
+        if (!ok && !(p.d > 0 && cands.size() == 1)) return 1e300;
+        double rc = real_cut(dd);
+        double pairs = (double)R.n_tgt * p.n_src * (4 * M_PI / 3) * rc * rc * rc / tau;
+        double grid = (double)M[0] * M[1] * M[2];
+        if ((R.flags & PB_KSPACE) == 0) return C.pair * pairs;
+        return C.pair * pairs + C.grid * grid * std::log2(std::max(grid, 2.0)) / 21.0 +
+               C.support * (double)(p.n_src + R.n_tgt) * cand.P * cand.P * cand.P;
+    };
+    auto consider = [&](const Support& cand, double dd) {
+        const double c = cost_at(cand, dd);
+        if (c < best) {
+            best = c;
+            d = dd;
+            sup = cand;
+        }
+        return c;
+    };
+    // the smallest supports that reach the tolerance (larger ones only add window points)
+    if (cands.size() > 4) cands.resize(4);
+    for (const Support& cand : cands) {
+        if (p.d > 0) {
+            consider(cand, p.d);
+            continue;
+        }
+        // d = Lmin 2^(-1 - k/16): a coarse pass every 4th k, then the fine steps around its best
+        double cbest = 1e300;
+        int kbest = 0;
+        for (int k = 0; k < 160; k += 4) {
+            const double dd = Lmin * std::pow(2.0, -1.0 - k * 0.0625);
             if (dd < 1e-6) break;
-            int M[3];
-            grid_for(p, dd, u, kconst, M);
-            bool ok = true;
-            for (int a = 0; a < 3; a++) {
-                if (M[a] > 1024 || cand.P > M[a]) ok = false;
-                if (p.M[a] > 0 && p.d == 0) {  // fixed grid: d must satisfy its k-space and spreading limits
-                    double kmax = 2 * M_PI * (M[a] / 2 - 1) / p.L[a];
-                    if (kmax * dd / 2 < std::sqrt(kconst)) ok = false;
-                    if (p.L[a] / M[a] * u > dd) ok = false;
-                }
+            const double c = consider(cand, dd);
+            if (c < cbest) {
+                cbest = c;
+                kbest = k;
             }
-            if (!ok && !(p.d > 0 && cands.size() == 1)) continue;
-            double rc = real_cut(dd);
-            double pairs = (double)R.n_tgt * p.n_src * (4 * M_PI / 3) * rc * rc * rc / tau;
-            double grid = (double)M[0] * M[1] * M[2];
-            double cost = C.pair * pairs + C.grid * grid * std::log2(std::max(grid, 2.0)) / 21.0 +
-                          C.support * (double)(p.n_src + R.n_tgt) * cand.P * cand.P * cand.P;
-            if ((R.flags & PB_KSPACE) == 0) cost = C.pair * pairs;
-            if (cost < best) {
-                best = cost;
-                d = dd;
-                sup = cand;
-            }
+        }
+        for (int k = std::max(0, kbest - 8); k <= std::min(159, kbest + 8); k++) {
+            const double dd = Lmin * std::pow(2.0, -1.0 - k * 0.0625);
+            if (dd >= 1e-6) consider(cand, dd);
         }
     }
     const int P = sup.P;
@@ -289,6 +314,8 @@ struct pb_plan_s {
     int4* items = nullptr;
     void *spos_a = nullptr, *spos_b = nullptr, *sfrc = nullptr, *tpos_a = nullptr, *tpos_b = nullptr;
     double *u_real = nullptr, *fsum = nullptr;
+    int* d_bad = nullptr;     // per instance: an input was not finite (set by the binning kernels)
+    int* h_bad = nullptr;     // pinned copy, written by plan_execute_parts
     int item_cap = 0;         // capacity of the real-space work item array
     void *u_k = nullptr, *grid = nullptr, *spec = nullptr;
 
@@ -369,7 +396,7 @@ size_t plan_layout(pb_plan_s* P, bool assign)
     }
     size_t o_ur = L.take<double>(3 * (size_t)nt);
     size_t o_uk = mixed ? L.take<float>(3 * (size_t)nt) : L.take<double>(3 * (size_t)nt);
-    size_t o_fsum = L.take<double>(3 * (size_t)q);
+    size_t o_fsum = L.take<double>(3 * (size_t)q), o_bad = L.take<int>(q);
     size_t esz = mixed ? 4 : 8;
     size_t o_grid = L.off;
     L.off += align_up(P->grid_elems * esz + 16);
@@ -429,6 +456,7 @@ size_t plan_layout(pb_plan_s* P, bool assign)
 
         P->u_k = A + o_uk;
         P->fsum = (double*)(A + o_fsum);
+        P->d_bad = (int*)(A + o_bad);
         P->grid = A + o_grid;
         P->spec = A + o_spec;
         for (size_t b = 0; b < P->buckets.size(); b++) {
@@ -617,6 +645,7 @@ void plan_free(pb_plan_s* P)
     if (P->gexec) cudaGraphExecDestroy(P->gexec);
     if (P->arena) cudaFree(P->arena);
     if (P->staging) cudaFreeHost(P->staging);
+    if (P->h_bad) cudaFreeHost(P->h_bad);
     if (P->ev_upload) cudaEventDestroy(P->ev_upload);
     if (P->ev_in) cudaEventDestroy(P->ev_in);
     if (P->ev_out) cudaEventDestroy(P->ev_out);
@@ -641,6 +670,8 @@ int plan_alloc(pb_plan_s* P)
     PB_CK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
     P->staging_bytes = (sizeof(PbInst) + sizeof(PbTables)) * (size_t)P->count + 4 * sizeof(int) * (P->count + 1);
     PB_CK(cudaMallocHost(&P->staging, P->staging_bytes));
+    PB_CK(cudaMallocHost(&P->h_bad, sizeof(int) * P->count));
+    std::memset(P->h_bad, 0, sizeof(int) * P->count);
     PB_CK(cudaEventCreateWithFlags(&P->ev_upload, cudaEventDisableTiming));
     PB_CK(cudaEventCreateWithFlags(&P->ev_in, cudaEventDisableTiming));
     PB_CK(cudaEventCreateWithFlags(&P->ev_out, cudaEventDisableTiming));
@@ -667,7 +698,7 @@ void bin_and_sort(pb_plan_s* P, const double* pos, int n, const int* d_off, int*
 {
     cudaMemsetAsync(cnt, 0, sizeof(int) * (P->ncell + 1), s);
     cudaMemsetAsync(fill, 0, sizeof(int) * (P->ncell + 1), s);
-    launch_bin(pos, n, d_off, P->d_inst, P->count, cell_of, cnt, s);
+    launch_bin(pos, n, d_off, P->d_inst, P->count, cell_of, cnt, P->d_bad, s);
     launch_exclusive_scan(cnt, start, P->ncell, P->scan_tmp, s, P->d_cell_off + P->count);
     launch_scatter(cell_of, n, d_off + P->count, start, fill, perm_tmp, s);
     launch_sort_cells(perm_tmp, perm, start, P->ncell, P->d_cell_off + P->count, P->nsm, s);
@@ -683,24 +714,25 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
 {
     const bool mixed = P->prec == PB_PREC_MIXED;
     record(P, 0, s);
+    cudaMemsetAsync(P->d_bad, 0, sizeof(int) * P->count, s);
     bin_and_sort(P, P->x, P->n_src, P->d_src_off, P->cell_of_s, P->cnt_s, P->start_s, P->fill_s, P->perm_tmp_s,
                  P->perm_s, s);
     if (mixed)
         launch_prepare_mixed(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count, (float4*)P->spos_a,
-                             (float4*)P->spos_b, (float4*)P->sfrc, s);
+                             (float4*)P->spos_b, (float4*)P->sfrc, P->d_bad, s);
     else
         launch_prepare_fp64(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count, (Dbl4*)P->spos_a,
-                            (Dbl4*)P->sfrc, s);
+                            (Dbl4*)P->sfrc, P->d_bad, s);
     if (!P->all_same) {
         launch_pack_targets(P->x, P->y, P->n_tgt, P->d_tgt_off, P->d_src_off, P->d_y_off, P->count, P->ypack, s);
         bin_and_sort(P, P->ypack, P->n_tgt, P->d_tgt_off, P->cell_of_t, P->cnt_t, P->start_t, P->fill_t,
                      P->perm_tmp_t, P->perm_t, s);
         if (mixed)
             launch_prepare_mixed(P->ypack, nullptr, P->perm_t, P->n_tgt, P->d_tgt_off, P->d_inst, P->count,
-                                 (float4*)P->tpos_a, (float4*)P->tpos_b, nullptr, s);
+                                 (float4*)P->tpos_a, (float4*)P->tpos_b, nullptr, P->d_bad, s);
         else
             launch_prepare_fp64(P->ypack, nullptr, P->perm_t, P->n_tgt, P->d_tgt_off, P->d_inst, P->count,
-                                (Dbl4*)P->tpos_a, nullptr, s);
+                                (Dbl4*)P->tpos_a, nullptr, P->d_bad, s);
     }
     launch_build_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items, P->item_cap,
                        P->counter + 1, P->nsm, s);
@@ -1013,6 +1045,7 @@ int plan_execute_parts(pb_plan P, const double* const* xs, const double* const* 
             PB_CK(cudaMemcpyAsync(Us[q], P->U + 3 * (size_t)P->tgt_off[q], sizeof(double) * 3 * R.n_tgt,
                                   cudaMemcpyDeviceToHost, s));
     }
+    PB_CK(cudaMemcpyAsync(P->h_bad, P->d_bad, sizeof(int) * P->count, cudaMemcpyDeviceToHost, s));
     P->exec_count++;
     PB_CK(cudaEventRecord(P->ev_out, s));
     PB_CK(cudaStreamWaitEvent(us, P->ev_out, 0));
@@ -1062,6 +1095,8 @@ int plan_bind_prepared(pb_plan P, const pb_solve_params* p, const PbTables* tabs
 {
     return bind_impl(P, p, tabs, count);
 }
+
+const int* plan_bad_flags(pb_plan P) { return P->h_bad; }
 
 int kspace_instance(const pb_solve_params& p, PbInst* inst)
 {

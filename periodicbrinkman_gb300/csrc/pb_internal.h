@@ -21,8 +21,13 @@ int prepare_instance(const pb_solve_params& p, int npoly_cap, PbTables* tab, pb_
 int plan_bind_prepared(pb_plan P, const pb_solve_params* p, const PbTables* tabs, int count);
 // Executes a bound plan with per-instance host buffers: instance q reads
 // xs[q], fs[q] (and ys[q] when it has its own targets) and writes Us[q].
-// Page-locked buffers are copied asynchronously; inputs must be finite.
+// Page-locked buffers are copied asynchronously; non-finite inputs are
+// reported by plan_bad_flags.
 int plan_execute_parts(pb_plan P, const double* const* xs, const double* const* fs, const double* const* ys,
                        double* const* Us, cudaStream_t stream);
+
+// After an execution by plan_execute_parts has completed: flags[q] != 0 when
+// instance q had a non-finite input (those inputs were computed as 0).
+const int* plan_bad_flags(pb_plan P);
 
 }  // namespace pb

@@ -13,8 +13,10 @@ namespace pb {
 // set of instances that fits the capacity.
 // cell_of[p] = global cell index of particle p (instance cell_off + local cell),
 // counts[cell] += 1.  pos: AoS doubles of all instances, offsets: ninst+1 prefix.
+// Non-finite coordinates (and forces, in the prepare kernels) are replaced by 0
+// and set bad[instance] = 1 (bad may be null).
 void launch_bin(const double* pos, int ncap, const int* offsets, const PbInst* inst, int ninst,
-                int* cell_of, int* counts, cudaStream_t s);
+                int* cell_of, int* counts, int* bad, cudaStream_t s);
 // Exclusive scan of n ints into out (out has n+1 entries; out[n] = total).
 // tmp must hold scan_tmp_ints(n) ints.  With n_act (device), only the first
 // *n_act entries may be nonzero and out is valid up to index *n_act.
@@ -28,10 +30,10 @@ void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap
                        cudaStream_t s);
 // Sorted particle records.  Mixed: pos_hi (x,y,z, w = instance bits), pos_lo, frc.
 void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
-                          const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out,
+                          const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out, int* bad,
                           cudaStream_t s);
 void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
-                         const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, cudaStream_t s);
+                         const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, int* bad, cudaStream_t s);
 // Work items: up to 32 consecutive targets of one cell row spanning <= 8 cells,
 // times csplit stencil column groups:
 // int4 {inst, first target, local row, count | za << 8 | zb << 16 | group << 24}.

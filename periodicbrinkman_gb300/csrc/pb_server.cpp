@@ -106,14 +106,16 @@ int grid_index(pb_server_s* S, int g)
 void finish_slot(pb_server_s* S, Slot& sl, int status)
 {
     size_t off = 0;
-    for (Req* r : sl.reqs) {
+    const int* bad = status == PB_OK ? pb::plan_bad_flags(sl.plan) : nullptr;
+    for (size_t k = 0; k < sl.reqs.size(); k++) {
+        Req* r = sl.reqs[k];
         size_t nb = 3 * (size_t)r->n_tgt_eff;
         if (status == PB_OK && !r->pin_out) std::memcpy(r->U, sl.U + off, nb * sizeof(double));
         off += nb;
-        r->status = status;
+        r->status = (bad && bad[k]) ? PB_ERR_INVALID : status;  // non-finite input, found on the device
         r->t_done = Clock::now();
         r->state.store(2);
-        if (status == PB_OK)
+        if (r->status == PB_OK)
             S->completed++;
         else
             S->failed++;
@@ -348,15 +350,18 @@ int pb_server_submit(pb_server S, const pb_solve_params* p, const double* x, con
     if (p->precision != S->cfg.precision) return PB_ERR_INVALID;
     if (p->n_src <= 0 || (p->n_tgt > 0 && !y) || !x || !f || !U) return PB_ERR_INVALID;
     // autotune and build the real-space tables here, in the caller's thread, so
-    // the scheduler only binds; inputs are checked here too
-    pb_instance_info info;
-    int rc = pb::resolve_info(*p, &info);
-    if (rc != PB_OK) return rc;
-    int need = std::max(info.M[0], std::max(info.M[1], info.M[2]));
-    int gi = grid_index(S, need);
-    // the instance runs on its slot's grid: resolve and build its tables for that grid
+    // the scheduler only binds.  The instance runs on its slot's grid: when the
+    // autotuned grid is not a provisioned one, resolve again for the slot's grid.
     Req* r = new Req();
-    if (gi >= 0) {
+    pb_instance_info info;
+    int rc = pb::prepare_instance(*p, S->npoly, &r->tab, &info);
+    if (rc != PB_OK) {
+        delete r;
+        return rc;
+    }
+    const int need = std::max(info.M[0], std::max(info.M[1], info.M[2]));
+    const int gi = grid_index(S, need);
+    if (gi >= 0 && !(info.M[0] == S->grids[gi] && info.M[1] == S->grids[gi] && info.M[2] == S->grids[gi])) {
         pb_solve_params pg = *p;
         pg.M[0] = pg.M[1] = pg.M[2] = S->grids[gi];
         rc = pb::prepare_instance(pg, S->npoly, &r->tab, &info);
@@ -364,14 +369,6 @@ int pb_server_submit(pb_server S, const pb_solve_params* p, const double* x, con
             delete r;
             return rc;
         }
-    }
-    const size_t n3 = 3 * (size_t)p->n_src, m3 = 3 * (size_t)std::max(p->n_tgt, 0);
-    bool finite = true;
-    for (size_t i = 0; i < n3 && finite; i++) finite = std::isfinite(x[i]) && std::isfinite(f[i]);
-    for (size_t i = 0; i < m3 && finite; i++) finite = std::isfinite(y[i]);
-    if (!finite) {
-        delete r;
-        return pb::api_error(PB_ERR_INVALID, "non-finite input");
     }
     int n_tgt_eff = p->n_tgt > 0 ? p->n_tgt : p->n_src;
     const long long cells = (long long)info.ncell[0] * info.ncell[1] * info.ncell[2];
@@ -386,7 +383,13 @@ int pb_server_submit(pb_server S, const pb_solve_params* p, const double* x, con
         return PB_ERR_BUDGET;
     }
     r->id = S->next_id++;
+    // the resolved splitting, support and grid go with the request, so that
+    // binding it reproduces the instance its tables were built for
     r->p = *p;
+    r->p.d = info.d;
+    r->p.rc = info.rc;
+    r->p.P = info.P;
+    for (int a = 0; a < 3; a++) r->p.M[a] = info.M[a];
     r->grid = gi;
     r->n_tgt_eff = n_tgt_eff;
     r->x = x;

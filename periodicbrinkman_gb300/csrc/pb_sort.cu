@@ -5,8 +5,17 @@
 
 namespace pb {
 
+// A non-finite coordinate is binned as 0 and flags its instance in bad[q].
+__device__ __forceinline__ double finite_or_flag(double v, int* bad, int q)
+{
+    if (isfinite(v)) return v;
+    if (bad) bad[q] = 1;
+    return 0.0;
+}
+
 __global__ void k_bin(const double* __restrict__ pos, const int* __restrict__ offsets,
-                      const PbInst* __restrict__ inst, int ninst, int* __restrict__ cell_of, int* __restrict__ counts)
+                      const PbInst* __restrict__ inst, int ninst, int* __restrict__ cell_of, int* __restrict__ counts,
+                      int* __restrict__ bad)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= offsets[ninst]) return;
@@ -15,7 +24,7 @@ __global__ void k_bin(const double* __restrict__ pos, const int* __restrict__ of
     int c[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        double w = wrap_coord_r(pos[3 * (size_t)p + a], I.L[a], I.iL[a]);
+        double w = wrap_coord_r(finite_or_flag(pos[3 * (size_t)p + a], bad, q), I.L[a], I.iL[a]);
         int ci = (int)(w * I.ih[a]);
         c[a] = ci >= I.nc[a] ? I.nc[a] - 1 : ci;
     }
@@ -25,10 +34,10 @@ __global__ void k_bin(const double* __restrict__ pos, const int* __restrict__ of
 }
 
 void launch_bin(const double* pos, int ncap, const int* offsets, const PbInst* inst, int ninst, int* cell_of,
-                int* counts, cudaStream_t s)
+                int* counts, int* bad, cudaStream_t s)
 {
     if (ncap <= 0) return;
-    k_bin<<<(ncap + 255) / 256, 256, 0, s>>>(pos, offsets, inst, ninst, cell_of, counts);
+    k_bin<<<(ncap + 255) / 256, 256, 0, s>>>(pos, offsets, inst, ninst, cell_of, counts, bad);
 }
 
 // ---- exclusive scan (reduce-then-scan, recursive over block sums) ----
@@ -181,7 +190,7 @@ void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap
 __global__ void k_prepare_mixed(const double* __restrict__ pos, const double* __restrict__ frc,
                                 const int* __restrict__ perm, const int* __restrict__ offsets,
                                 const PbInst* __restrict__ inst, int ninst, float4* __restrict__ pos_hi,
-                                float4* __restrict__ pos_lo, float4* __restrict__ frc_out)
+                                float4* __restrict__ pos_lo, float4* __restrict__ frc_out, int* __restrict__ bad)
 {
     int sidx = blockIdx.x * blockDim.x + threadIdx.x;
     if (sidx >= offsets[ninst]) return;
@@ -190,27 +199,29 @@ __global__ void k_prepare_mixed(const double* __restrict__ pos, const double* __
     const PbInst& I = inst[q];
     float hi[3], lo[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++) split_double(wrap_coord_r(pos[3 * (size_t)p + a], I.L[a], I.iL[a]), hi[a], lo[a]);
+    for (int a = 0; a < 3; a++)
+        split_double(wrap_coord_r(finite_or_flag(pos[3 * (size_t)p + a], bad, q), I.L[a], I.iL[a]), hi[a], lo[a]);
     pos_hi[sidx] = make_float4(hi[0], hi[1], hi[2], __int_as_float(q));
     pos_lo[sidx] = make_float4(lo[0], lo[1], lo[2], 0.f);
     if (frc)
-        frc_out[sidx] = make_float4((float)frc[3 * (size_t)p], (float)frc[3 * (size_t)p + 1],
-                                    (float)frc[3 * (size_t)p + 2], 0.f);
+        frc_out[sidx] = make_float4((float)finite_or_flag(frc[3 * (size_t)p], bad, q),
+                                    (float)finite_or_flag(frc[3 * (size_t)p + 1], bad, q),
+                                    (float)finite_or_flag(frc[3 * (size_t)p + 2], bad, q), 0.f);
 }
 
 void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
-                          const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out,
+                          const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out, int* bad,
                           cudaStream_t s)
 {
     if (ncap <= 0) return;
     k_prepare_mixed<<<(ncap + 255) / 256, 256, 0, s>>>(pos, frc, perm, offsets, inst, ninst, pos_hi, pos_lo,
-                                                        frc_out);
+                                                        frc_out, bad);
 }
 
 __global__ void k_prepare_fp64(const double* __restrict__ pos, const double* __restrict__ frc,
                                const int* __restrict__ perm, const int* __restrict__ offsets,
                                const PbInst* __restrict__ inst, int ninst, Dbl4* __restrict__ pos_out,
-                               Dbl4* __restrict__ frc_out)
+                               Dbl4* __restrict__ frc_out, int* __restrict__ bad)
 {
     int sidx = blockIdx.x * blockDim.x + threadIdx.x;
     if (sidx >= offsets[ninst]) return;
@@ -219,16 +230,20 @@ __global__ void k_prepare_fp64(const double* __restrict__ pos, const double* __r
     const PbInst& I = inst[q];
     double w[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++) w[a] = wrap_coord_r(pos[3 * (size_t)p + a], I.L[a], I.iL[a]);
+    for (int a = 0; a < 3; a++) w[a] = wrap_coord_r(finite_or_flag(pos[3 * (size_t)p + a], bad, q), I.L[a], I.iL[a]);
     pos_out[sidx] = make_dbl4(w[0], w[1], w[2], (double)q);
-    if (frc) frc_out[sidx] = make_dbl4(frc[3 * (size_t)p], frc[3 * (size_t)p + 1], frc[3 * (size_t)p + 2], 0.0);
+    if (frc)
+        frc_out[sidx] = make_dbl4(finite_or_flag(frc[3 * (size_t)p], bad, q),
+                                  finite_or_flag(frc[3 * (size_t)p + 1], bad, q),
+                                  finite_or_flag(frc[3 * (size_t)p + 2], bad, q), 0.0);
 }
 
 void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
-                         const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, cudaStream_t s)
+                         const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, int* bad, cudaStream_t s)
 {
     if (ncap <= 0) return;
-    k_prepare_fp64<<<(ncap + 255) / 256, 256, 0, s>>>(pos, frc, perm, offsets, inst, ninst, pos_out, frc_out);
+    k_prepare_fp64<<<(ncap + 255) / 256, 256, 0, s>>>(pos, frc, perm, offsets, inst, ninst, pos_out, frc_out,
+                                                       bad);
 }
 
 // Work items of the real-space kernel: each cell row (c0, c1) of an instance

@@ -9,7 +9,7 @@ import pytest
 import oracle
 import periodicbrinkman_gb300 as pb
 from periodicbrinkman_gb300 import _lib
-from periodicbrinkman_gb300.api import estimate_bytes, make_params
+from periodicbrinkman_gb300.api import estimate_bytes, make_params, resolve
 
 
 def test_library_exports_header_symbols():
@@ -58,6 +58,17 @@ def test_autotuner_resolves_consistent_parameters():
                                                                              "mixed")]:
         b = estimate_bytes(make_params(n, L, a, e, tol=tol, precision=prec))
         assert b > 0
+
+
+@pytest.mark.parametrize("n,L,a,e,M", [(1000, 1.0, 10.0, 0.01, 0), (20000, 1.0, 20.0, 0.005, 0),
+                                       (3000, (0.5, 1.0, 2.0), 3.0, 0.005, 0), (2000, 1.0, 10.0, 0.01, 32)])
+def test_resolved_parameters_are_a_fixed_point(n, L, a, e, M):
+    """Resolving again with the resolved splitting, cutoff, support and grid
+    given explicitly reproduces the instance (the serving path binds requests
+    this way, with tables built at submission)."""
+    r = resolve(make_params(n, L, a, e, tol=1e-6, M=(M, M, M)))
+    r2 = resolve(make_params(n, L, a, e, tol=1e-6, d=r["d"], rc=r["rc"], P=r["P"], M=tuple(r["M"])))
+    assert r2 == r
 
 
 def test_kernel_tables_match_oracle():

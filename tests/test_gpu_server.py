@@ -100,3 +100,23 @@ def test_server_rejects_and_validates():
         U, _ = srv.result(t)
         assert np.isfinite(U).all()
         assert srv.stats()["rejected"] >= 1
+
+
+def test_server_non_finite_request_fails_alone():
+    """A request with a NaN position or force is found on the device and fails
+    with PB_ERR_INVALID; the requests batched with it are unaffected."""
+    with Server(precision="mixed", budget_bytes=2 << 30, max_batch=4, slots_per_grid=1, grids=(16, 32),
+                max_src=2000, linger_us=50000) as srv:
+        rng = np.random.default_rng(34)
+        xs = [rng.random((300, 3)) for _ in range(3)]
+        fs = [rng.standard_normal((300, 3)) for _ in range(3)]
+        fs[1][7, 2] = np.nan
+        tickets = [srv.submit(xs[k], fs[k], 1.0, 10.0, 0.01, tol=1e-6) for k in range(3)]
+        for k in (0, 2):
+            U, _ = srv.result(tickets[k])
+            alone = pb.solve(_cuda(xs[k]), _cuda(fs[k]), 1.0, 10.0, 0.01, tol=1e-6).cpu().numpy()
+            assert np.abs(U - alone).max() <= 2 * MIX_TOL * np.abs(alone).max(), k
+        with pytest.raises(pb.PbError) as ei:
+            srv.result(tickets[1])
+        assert ei.value.code == _lib.PB_ERR_INVALID
+        assert srv.stats()["failed"] >= 1
