@@ -247,42 +247,30 @@ void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, 
 }
 
 // Work items of the real-space kernel: each cell row (c0, c1) of an instance
-// is walked along z and cut into row items of <= 32 consecutive targets
-// spanning <= 8 cells (a cell with more than 32 targets gives items of its
-// own).  Each row item becomes `G` = csplit work items, one per group of
-// stencil columns, so that small instances still fill the GPU.  One thread
-// per row start: a counting walk, then the emitting walk into its range.
+// is walked along z and cut into row items of 32 consecutive targets (cells
+// may be split between items, so warps stay full), fewer where the row ends
+// or where 32 targets would span more than 8 cells.  Each row item becomes
+// `G` = csplit work items, one per group of stencil columns, so that small
+// instances still fill the GPU.  One thread per row start: a counting walk,
+// then the emitting walk into its range.  A row gives at most
+// targets/32 + cells items.
 // Item = {instance, first target, local row, count | za << 8 | zb << 16 | group << 24}.
 template <bool EMIT>
 __device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q, int rowl, int G, int4* items,
                          int k0, int cap, int& nitems)
 {
-    int z = 0, k = 0;
-    auto emit = [&](int first, int count, int za, int zb) {
+    int k = 0, z = 0;
+    int t = start[row0];
+    const int end = start[row0 + nz];
+    while (t < end) {
+        while (start[row0 + z + 1] <= t) z++;  // za: the cell of target t
+        const int za = z;
+        const int lim = min(min(t + 32, end), start[row0 + min(za + 8, nz)]);
+        while (start[row0 + z + 1] <= lim - 1) z++;  // zb: the cell of target lim - 1
         for (int g = 0; g < G; g++, k++)
             if (EMIT && k0 + k < cap)
-                items[k0 + k] = make_int4(q, first, rowl, count | (za << 8) | (zb << 16) | (g << 24));
-    };
-    while (z < nz) {
-        int n = start[row0 + z + 1] - start[row0 + z];
-        if (n == 0) {
-            z++;
-            continue;
-        }
-        if (n > 32) {
-            int b = start[row0 + z];
-            for (int c = 0; c * 32 < n; c++) emit(b + 32 * c, min(32, n - 32 * c), z, z);
-            z++;
-            continue;
-        }
-        int za = z, tot = 0;
-        while (z < nz && z - za < 8) {
-            int m = start[row0 + z + 1] - start[row0 + z];
-            if (tot + m > 32) break;
-            tot += m;
-            z++;
-        }
-        emit(start[row0 + za], tot, za, z - 1);
+                items[k0 + k] = make_int4(q, t, rowl, (lim - t) | (za << 8) | (z << 16) | (g << 24));
+        t = lim;
     }
     nitems = k;
 }
