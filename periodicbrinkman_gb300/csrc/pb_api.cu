@@ -263,9 +263,11 @@ int resolve(const pb_solve_params& p, Resolved& R)
         if (Pa > R.M[a]) return fail(PB_ERR_UNSUPPORTED, "support %d exceeds grid M[%d]=%d", Pa, a, R.M[a]);
         R.Pa[a] = Pa;
     }
-    // cell list: cells at least rc/2 wide (two-cell reach), capped at 128 per axis
+    // cell list: cells at least rc/2 wide across (two-cell reach) and rc/4 along z,
+    // where each stencil column is cut to the part of the cutoff ball it meets;
+    // capped at 128 per axis
     for (int a = 0; a < 3; a++) {
-        int nc = (int)std::floor(2.0 * p.L[a] / R.rc);
+        int nc = (int)std::floor((a == 2 ? 4.0 : 2.0) * p.L[a] / R.rc);
         nc = std::max(1, std::min(128, nc));
         R.nc[a] = nc;
         R.h[a] = p.L[a] / nc;
@@ -704,7 +706,7 @@ void bin_and_sort(pb_plan_s* P, const double* pos, int n, const int* d_off, int*
     launch_bin(pos, n, d_off, P->d_inst, P->count, cell_of, cnt, P->d_bad, s);
     launch_exclusive_scan(cnt, start, P->ncell, P->scan_tmp, s, P->d_cell_off + P->count);
     launch_scatter(cell_of, n, d_off + P->count, start, fill, perm_tmp, s);
-    launch_sort_cells(perm_tmp, perm, start, P->ncell, P->d_cell_off + P->count, P->nsm, s);
+    launch_sort_cells(perm_tmp, perm, start, P->ncell, P->d_cell_off, P->d_inst, P->count, pos, P->nsm, s);
 }
 
 void record(pb_plan_s* P, int k, cudaStream_t s)

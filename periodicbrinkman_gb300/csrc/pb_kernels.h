@@ -25,9 +25,9 @@ void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_
 // perm[start[c] + k] = particle, fill must be zeroed.
 void launch_scatter(const int* cell_of, int ncap, const int* ntot, const int* start, int* fill, int* perm,
                     cudaStream_t s);
-// Sort each cell's perm entries ascending (deterministic order); *ncell = actual cells.
-void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap, const int* ncell, int nsm,
-                       cudaStream_t s);
+// Sort each cell's perm entries by (wrapped z as FP32, index); cell_offsets[ninst] = actual cells.
+void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap, const int* cell_offsets,
+                       const PbInst* inst, int ninst, const double* pos, int nsm, cudaStream_t s);
 // Sorted particle records.  Mixed: pos_hi (x,y,z, w = instance bits), pos_lo, frc.
 void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                           const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out, int* bad,

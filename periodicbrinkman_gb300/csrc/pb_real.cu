@@ -138,29 +138,50 @@ __device__ __forceinline__ float horner_g(const float* __restrict__ c, int n, fl
 }
 
 // Per-warp shared memory of the mixed-precision kernel.
+constexpr int kSeg = 64;   // candidate segments gathered before they are streamed
+constexpr int kNear = 64;  // deferred near pairs (evaluated 32 at a time; <= 31 wait)
+
 struct __align__(16) RealWarpSmem {
-    float4 s_hi[32], s_lo[32], s_f[32];  // staged sources: frame-relative hi, lo; force
-    float4 t_hi[32], t_lo[32];           // the item's targets: frame-relative hi, lo
-    float c_x[32], c_y[32], c_z[32];     // staged sources, hi parts by axis (classification)
-    float acc[3][32];                    // per-target partial sums of the current chunk
-    double acc64[3][32];                 // per-target FP64 sums of series pairs
-    unsigned short q[3][1024];           // pair queues (t << 5 | j): screened, blob region, series
-    float2 tn[kMaxCheb];                 // near piece (T1, T2) of the current instance
-    float2 tb[kMaxCheb];                 // blob piece (H1, r^2 H2) of the current instance
-    FrameTabs ft;                        // the current item's frame tables
+    float4 s_hi[32], s_lo[32], s_f[32];     // staged sources: frame-relative hi, lo; force
+    float4 t_hi[32], t_lo[32];              // the item's targets: frame-relative hi, lo
+    float4 nq_h[kNear], nq_l[kNear], nq_f[kNear];  // deferred near pairs: displacement hi (target in w), lo; force
+    float c_x[32], c_y[32], c_z[32];        // staged sources, hi parts by axis (classification)
+    float acc[3][32];                       // per-target partial sums of the current chunk
+    float ks[6][32];                        // per-target Kahan sums (3) and compensations (3) of the item
+    double acc64[3][32];                    // per-target FP64 sums of series pairs
+    unsigned selfm[32];                     // per target: the staged candidate that is its own source
+    int sg_b[kSeg], sg_n[kSeg], sg_pre[kSeg], sg_meta[kSeg];  // segments: first source, count, prefix, frame
+    float box[6];                           // the item's targets: frame-relative bounding box (hi parts)
+    int nq_n;                               // deferred near pairs waiting
+    unsigned short q[1024];                 // in-cutoff pairs of a chunk, target-major (t << 5 | j)
+    float2 tn[kMaxCheb];                    // near piece (T1, T2) of the current instance
+    float2 tb[kMaxCheb];                    // blob piece (H1, r^2 H2) of the current instance
+    FrameTabs ft;                           // the current item's frame tables
+    struct {
+        float rtiny2, rs2, tbs, tbo, tns, tno;
+        int nbp, nnp;
+    } rk;                                   // constants of the rare pieces of the current instance
 };
 
-// Warp-wide exclusive prefix sum (64-bit, three packed 16-bit counters).
-__device__ __forceinline__ unsigned long long warp_excl_scan64(unsigned long long v, int lane)
+// Warp-wide exclusive prefix sum.
+__device__ __forceinline__ int warp_excl_scan(int v, int lane)
 {
-    unsigned long long x = v;
+    int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        unsigned long long y = __shfl_up_sync(kFull, x, o);
+        int y = __shfl_up_sync(kFull, x, o);
         if (lane >= o) x += y;
     }
     return x - v;
 }
+
+// Order-preserving map of floats to ints (for warp min/max reductions).
+__device__ __forceinline__ int float_key(float f)
+{
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float key_float(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
 // Segmented (by target) warp reduction of the contributions of one round of
 // a target-major queue; segment ends add into the per-target accumulators.
@@ -184,13 +205,308 @@ __device__ __forceinline__ void segment_reduce_add(float v0, float v1, float v2,
     }
 }
 
+// The instance's constants of the common path, held by each lane.
+struct MixedConsts {
+    float tds, tdo, rc2, rare2;
+};
+
+// A pair below r_mid: the blob piece (R_eps - R_d itself) inside the blob
+// region, else the near piece of S - R_d; below r_tiny (or at r = 0) the FP64
+// series, summed into the target's FP64 accumulator (then v = 0).
+__device__ __forceinline__ void rare_pair(RealWarpSmem& S, const PbTables& T, float4 h, float4 l, float4 f, int t,
+                                          float& v0, float& v1, float& v2)
+{
+    const auto& K = S.rk;
+    const float dx = h.x + l.x, dy = h.y + l.y, dz = h.z + l.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    v0 = v1 = v2 = 0.f;
+    if ((r2 < K.rtiny2) | (r2 == 0.f)) {
+        const double ddx = (double)h.x + (double)l.x, ddy = (double)h.y + (double)l.y, ddz = (double)h.z + (double)l.z;
+        const double rr = ddx * ddx + ddy * ddy + ddz * ddz;
+        double H1, H2;
+        if (T.blob) {
+            series_H(T, rr, H1, H2);
+        } else if (rr == 0.0) {
+            H1 = T.self1;  // coincident points, eps = 0: the reference's r -> 0 limit
+            H2 = 0;
+        } else {  // eps = 0, nearly coincident: singular kernel from the near piece
+            float r2f = (float)rr, ri = rsqrtf(r2f);
+            ri = ri * fmaf(-0.5f * r2f * ri, ri, 1.5f);
+            const float2 T12 = cheb2(S.tn, K.nnp, fmaf(r2f * ri, K.tns, K.tno));
+            H1 = (double)(T12.x * ri);
+            H2 = (double)(T12.y * (ri * ri * ri));
+        }
+        const double fd = f.x * ddx + f.y * ddy + f.z * ddz;
+        atomicAdd(&S.acc64[0][t], H1 * f.x + H2 * fd * ddx);
+        atomicAdd(&S.acc64[1][t], H1 * f.y + H2 * fd * ddy);
+        atomicAdd(&S.acc64[2][t], H1 * f.z + H2 * fd * ddz);
+        return;
+    }
+    float ri = rsqrtf(r2);
+    ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
+    const float r = r2 * ri;
+    float H1, H2;
+    if (r2 < K.rs2) {
+        const float2 b = cheb2(S.tb, K.nbp, fmaf(r, K.tbs, K.tbo));
+        H1 = b.x;
+        H2 = b.y * (ri * ri);
+    } else {
+        const float2 T12 = cheb2(S.tn, K.nnp, fmaf(r, K.tns, K.tno));
+        H1 = T12.x * ri;
+        H2 = T12.y * (ri * ri * ri);
+    }
+    const float g = H2 * fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
+    v0 = fmaf(H1, f.x, g * dx);
+    v1 = fmaf(H1, f.y, g * dy);
+    v2 = fmaf(H1, f.z, g * dz);
+}
+
+// Evaluate the `n` (<= 32) deferred near pairs [end - n, end), one per lane,
+// into the per-target accumulators: each lane writes its pair's contribution
+// over the entry, then lane t sums the entries of target t (no atomics).
+__device__ __forceinline__ void near_flush(RealWarpSmem& S, const PbTables& T, int end, int n, int lane)
+{
+    const int e0 = end - n;
+    if (lane < n) {
+        const int e = e0 + lane;
+        const float4 h = S.nq_h[e];
+        const int t = __float_as_int(h.w);
+        float v0, v1, v2;
+        rare_pair(S, T, h, S.nq_l[e], S.nq_f[e], t, v0, v1, v2);
+        S.nq_h[e] = make_float4(v0, v1, v2, h.w);
+    }
+    __syncwarp();
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    for (int i = 0; i < n; i++) {
+        const float4 w = S.nq_h[e0 + i];
+        if (__float_as_int(w.w) == lane) {
+            a0 += w.x;
+            a1 += w.y;
+            a2 += w.z;
+        }
+    }
+    S.acc[0][lane] += a0;
+    S.acc[1][lane] += a1;
+    S.acc[2][lane] += a2;
+    __syncwarp();
+}
+
+// Kahan-add the chunk's per-target sums into the item's sums; clear them.
+__device__ __forceinline__ void chunk_sums(RealWarpSmem& S, int lane)
+{
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float sc = S.ks[c][lane], kc = S.ks[3 + c][lane];
+        kahan_add(sc, kc, S.acc[c][lane]);
+        S.ks[c][lane] = sc;
+        S.ks[3 + c][lane] = kc;
+        S.acc[c][lane] = 0.f;
+    }
+}
+
+// Stream the gathered candidate segments through the warp 32 sources at a
+// time: stage, classify against the item's targets, queue the pairs inside
+// the cutoff target-major and evaluate them (far polynomial; pairs below
+// r_mid are deferred to the near queue).
+template <int NP>
+__device__ __forceinline__ void stream_segments(RealWarpSmem& S, const PbInst& I, const PbTables& T,
+                                                const MixedConsts& K, const float2 (&c12)[NP], const ItemFrame& F,
+                                                int nseg, int lane, const float4* __restrict__ spos_hi,
+                                                const float4* __restrict__ spos_lo, const float4* __restrict__ sfrc)
+{
+    // exclusive prefix of the segment counts (two segments per lane)
+    int total;
+    {
+        const int a = 2 * lane, b = 2 * lane + 1;
+        const int n0 = a < nseg ? S.sg_n[a] : 0, n1 = b < nseg ? S.sg_n[b] : 0;
+        const int ex = warp_excl_scan(n0 + n1, lane);
+        if (a < nseg) S.sg_pre[a] = ex;
+        if (b < nseg) S.sg_pre[b] = ex + n0;
+        total = __shfl_sync(kFull, ex + n0 + n1, 31);
+    }
+    __syncwarp();
+    const int self_shift = I.same ? I.tgt_off - I.src_off - F.first : 0;
+    for (int base = 0; base < total; base += 32) {
+        const int ncand = min(32, total - base);
+        if (lane < ncand) {
+            const int p = base + lane;
+            int lo = 0, hi = nseg - 1;  // the last segment starting at or before p
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (S.sg_pre[mid] <= p)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const int j = S.sg_b[lo] + (p - S.sg_pre[lo]);
+            const int meta = S.sg_meta[lo];
+            const int i0 = meta & 31, i1 = (meta >> 5) & 31, i2 = meta >> 10;
+            const float2 qx = S.ft.qx[i0], qy = S.ft.qy[i1], qz = S.ft.qz[i2];
+            const float qh[3] = {qx.x, qy.x, qz.x}, ql[3] = {qx.y, qy.y, qz.y};
+            const float4 ph = spos_hi[j], pl = spos_lo[j];
+            const float xh[3] = {ph.x, ph.y, ph.z}, xl[3] = {pl.x, pl.y, pl.z};
+            float p3[3], l3[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                float s, er;
+                two_sum(xh[a], -qh[a], s, er);
+                p3[a] = s;
+                l3[a] = er + (xl[a] - ql[a]);
+            }
+            S.s_hi[lane] = make_float4(p3[0], p3[1], p3[2], 0.f);
+            S.s_lo[lane] = make_float4(l3[0], l3[1], l3[2], 0.f);
+            S.s_f[lane] = sfrc[j];
+            S.c_x[lane] = p3[0];
+            S.c_y[lane] = p3[1];
+            S.c_z[lane] = p3[2];
+            if (I.same && S.ft.zx[i0] && S.ft.zy[i1] && S.ft.zz[i2]) {  // a target's own source (added by the combine kernel)
+                const int ts = j + self_shift;
+                if (ts >= 0 && ts < F.count) S.selfm[ts] = 1u << lane;
+            }
+        } else {  // padding: far from every target, active (finite) or not (+3e30)
+            S.c_x[lane] = -3.0e30f;
+            S.c_y[lane] = -3.0e30f;
+            S.c_z[lane] = -3.0e30f;
+        }
+        __syncwarp();
+        // candidate pairs of this lane's target inside the cutoff and below r_mid (two per
+        // packed FP32x2 operation)
+        unsigned mi = 0, mr = 0;
+        {
+            const float4 tt = S.t_hi[lane];
+            const float2 ntx = make_float2(-tt.x, -tt.x), nty = make_float2(-tt.y, -tt.y),
+                         ntz = make_float2(-tt.z, -tt.z);
+#pragma unroll
+            for (int jj = 0; jj < 32; jj += 2) {
+                const float2 dx = __fadd2_rn(*reinterpret_cast<const float2*>(&S.c_x[jj]), ntx);
+                const float2 dy = __fadd2_rn(*reinterpret_cast<const float2*>(&S.c_y[jj]), nty);
+                const float2 dz = __fadd2_rn(*reinterpret_cast<const float2*>(&S.c_z[jj]), ntz);
+                float2 r2 = __fmul2_rn(dx, dx);
+                r2 = __ffma2_rn(dy, dy, r2);
+                r2 = __ffma2_rn(dz, dz, r2);
+                if (r2.x < K.rc2) mi |= 1u << jj;
+                if (r2.y < K.rc2) mi |= 2u << jj;
+                if (r2.x < K.rare2) mr |= 1u << jj;
+                if (r2.y < K.rare2) mr |= 2u << jj;
+            }
+        }
+        mi &= ~S.selfm[lane];
+        mr &= ~S.selfm[lane];
+        S.selfm[lane] = 0u;
+        mi &= ~mr;
+        // target-major queues: pairs inside the cutoff from the front of q, pairs
+        // below r_mid from its back (the two are disjoint pairs of the chunk)
+        const int cnt = __popc(mi) | (__popc(mr) << 16);
+        int ex = warp_excl_scan(cnt, lane);
+        const int tot = __shfl_sync(kFull, ex + cnt, 31);
+        const int nn = tot & 0xffff, nr = tot >> 16;
+        {
+            const unsigned short tag = (unsigned short)(lane << 5);
+            int pn = ex & 0xffff, pr = 1023 - (ex >> 16);
+            for (unsigned m = mi; m; m &= m - 1) S.q[pn++] = tag | (__ffs(m) - 1);
+            for (unsigned m = mr; m; m &= m - 1) S.q[pr--] = tag | (__ffs(m) - 1);
+        }
+        __syncwarp();
+        // pairs below r_mid join the near queue (<= 31 waiting), which is
+        // evaluated whenever it holds 32
+        for (int r0 = 0; r0 < nr;) {
+            const int nq = S.nq_n;
+            const int k = min(nr - r0, kNear - nq);
+            __syncwarp();
+            for (int i = lane; i < k; i += 32) {
+                const int qv = S.q[1023 - (r0 + i)], t = qv >> 5, jj = qv & 31;
+                const float4 p = S.s_hi[jj], pl = S.s_lo[jj], a = S.t_hi[t], al = S.t_lo[t];
+                S.nq_h[nq + i] = make_float4(a.x - p.x, a.y - p.y, a.z - p.z, __int_as_float(t));
+                S.nq_l[nq + i] = make_float4(al.x - pl.x, al.y - pl.y, al.z - pl.z, 0.f);
+                S.nq_f[nq + i] = S.s_f[jj];
+            }
+            __syncwarp();
+            int n = nq + k;
+            while (n >= 32) {
+                near_flush(S, T, n, 32, lane);
+                n -= 32;
+            }
+            if (lane == 0) S.nq_n = n;
+            __syncwarp();
+            r0 += k;
+        }
+        // Lane l takes the contiguous block [l K, (l+1) K) of the queue and sums runs
+        // of one target in registers: a target that starts inside the block is added
+        // by this lane alone; the block's first target (which may continue from
+        // earlier lanes) goes through one segmented reduction.
+        {
+            const int KB = (nn + 31) >> 5;
+            const int eb = min(lane * KB, nn), ee = min(eb + KB, nn);
+            int cur = -1, first = -1;
+            float a0 = 0, a1 = 0, a2 = 0, f0 = 0, f1 = 0, f2 = 0;
+            for (int ei = eb; ei < ee; ei++) {
+                const int qv = S.q[ei], t = qv >> 5, jj = qv & 31;
+                const float4 p = S.s_hi[jj], pl = S.s_lo[jj], f = S.s_f[jj];
+                const float4 a = S.t_hi[t], al = S.t_lo[t];
+                const float dx = (a.x - p.x) + (al.x - pl.x);
+                const float dy = (a.y - p.y) + (al.y - pl.y);
+                const float dz = (a.z - p.z) + (al.z - pl.z);
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                float ri = rsqrtf(r2);
+                ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
+                const float r = r2 * ri;
+                const float2 T12 = horner2<NP>(c12, fmaf(r, K.tds, K.tdo));
+                const float H1 = T12.x * ri, H2 = T12.y * (ri * ri * ri);
+                const float g = H2 * fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
+                const float v0 = fmaf(H1, f.x, g * dx);
+                const float v1 = fmaf(H1, f.y, g * dy);
+                const float v2 = fmaf(H1, f.z, g * dz);
+                if (t != cur) {
+                    if (cur >= 0) {
+                        if (first < 0) {
+                            first = cur;
+                            f0 = a0;
+                            f1 = a1;
+                            f2 = a2;
+                        } else {
+                            S.acc[0][cur] += a0;
+                            S.acc[1][cur] += a1;
+                            S.acc[2][cur] += a2;
+                        }
+                    }
+                    cur = t;
+                    a0 = v0;
+                    a1 = v1;
+                    a2 = v2;
+                } else {
+                    a0 += v0;
+                    a1 += v1;
+                    a2 += v2;
+                }
+            }
+            if (cur >= 0) {
+                if (first < 0) {
+                    first = cur;
+                    f0 = a0;
+                    f1 = a1;
+                    f2 = a2;
+                } else {
+                    S.acc[0][cur] += a0;
+                    S.acc[1][cur] += a1;
+                    S.acc[2][cur] += a2;
+                }
+            }
+            __syncwarp();
+            if (nn > 0) segment_reduce_add(f0, f1, f2, first >= 0 ? first : -1 - lane, lane, S.acc);
+        }
+        __syncwarp();
+
+        chunk_sums(S, lane);
+        __syncwarp();
+    }
+}
+
 template <int NP>
 __global__ void __launch_bounds__(kRealWarps * 32, 4)
     k_real_mixed(const PbInst* __restrict__ inst, const PbTables* __restrict__ tab, const int4* __restrict__ items,
                  const int* __restrict__ nitems_ptr, const float4* __restrict__ spos_hi, const float4* __restrict__ spos_lo,
-                 const float4* __restrict__ sfrc, const int* __restrict__ src_start, const float4* __restrict__ tpos_hi,
-                 const float4* __restrict__ tpos_lo, double* __restrict__ u_real, int* __restrict__ counter,
-                 int item_cap)
+                 const float4* __restrict__ sfrc, const int* __restrict__ src_start, const float4* __restrict__ tpos_hi, const float4* __restrict__ tpos_lo, double* __restrict__ u_real,
+                 int* __restrict__ counter, int item_cap)
 {
     __shared__ RealWarpSmem smem_all[kRealWarps];
     RealWarpSmem& S = smem_all[threadIdx.x >> 5];
@@ -200,13 +516,15 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
     const int nitems = min(*nitems_ptr, item_cap);
     float2 c12[NP];
     int cur_q = -1;
-    float tds = 0, tdo = 0, rc2 = 0, rare2 = 0, rtiny2 = 0, tbs = 0, tbo = 0, tns = 0, tno = 0, rs2 = 0;
-    int nbp = 1, nnp = 1;
+    MixedConsts K{};
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         S.acc[c][lane] = 0.f;
         S.acc64[c][lane] = 0.0;
     }
+    S.selfm[lane] = 0u;
+    if (lane == 0) S.nq_n = 0;
+    __syncwarp();
 
     while (true) {
         int item = 0;
@@ -220,19 +538,20 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
             cur_q = it.x;
 #pragma unroll
             for (int k = 0; k < NP; k++) c12[k] = make_float2(T.pd1[k], T.pd2[k]);
-            tds = T.td_scale;
-            tdo = T.td_off;
-            rc2 = T.rc2;
-            // rare pairs: the blob region (eps > 0), else coincident points only
-            rare2 = T.rm2;  // near piece (holds the blob region and r = 0)
-            rs2 = T.rs2;
-            tns = T.tn_scale;
-            tno = T.tn_off;
-            nnp = T.nn > 0 ? T.nn : 1;
-            rtiny2 = T.rtiny2f;
-            tbs = T.tb_scale;
-            tbo = T.tb_off;
-            nbp = T.nb > 0 ? T.nb : 1;
+            K.tds = T.td_scale;
+            K.tdo = T.td_off;
+            K.rc2 = T.rc2;
+            K.rare2 = T.rm2;  // below r_mid: the near and blob pieces (and r = 0)
+            if (lane == 0) {
+                S.rk.rs2 = T.rs2;
+                S.rk.tns = T.tn_scale;
+                S.rk.tno = T.tn_off;
+                S.rk.nnp = T.nn > 0 ? T.nn : 1;
+                S.rk.rtiny2 = T.rtiny2f;
+                S.rk.tbs = T.tb_scale;
+                S.rk.tbo = T.tb_off;
+                S.rk.nbp = T.nb > 0 ? T.nb : 1;
+            }
             for (int k = lane; k < kMaxCheb; k += 32) {
                 S.tn[k] = make_float2(T.cn1[k], T.cn2[k]);
                 S.tb[k] = make_float2(T.cb1[k], T.cb2[k]);
@@ -243,11 +562,10 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
         fill_frame_tabs(I, F, S.ft, lane);
         const bool active = lane < F.count;
         const int tidx = F.first + (active ? lane : 0);
-        const int self_src = I.same ? tidx - I.tgt_off + I.src_off : -1;
-        float th[3], tl[3];
+        float th[3];
         {
             float4 ph = tpos_hi[tidx], pl = tpos_lo[tidx];
-            float xh[3] = {ph.x, ph.y, ph.z}, xl[3] = {pl.x, pl.y, pl.z};
+            float xh[3] = {ph.x, ph.y, ph.z}, xl[3] = {pl.x, pl.y, pl.z}, tl[3];
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 float oh, ol, s, e;
@@ -256,269 +574,107 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
                 th[a] = active ? s : 3.0e30f;  // inactive lanes pair with nothing
                 tl[a] = e + (xl[a] - ol);
             }
-        }
-        S.t_hi[lane] = make_float4(th[0], th[1], th[2], 0.f);
-        S.t_lo[lane] = make_float4(tl[0], tl[1], tl[2], 0.f);
-        __syncwarp();
-        float s0 = 0, s1 = 0, s2 = 0, k0 = 0, k1 = 0, k2 = 0;
-        const int nzt = F.zb - F.za + 2 * I.S[2] + 1;
-
-        const int ny1 = 2 * I.S[1] + 1, ncol = (2 * I.S[0] + 1) * ny1;
-        const int csplit = max(1, I.csplit);
-        for (int col = F.group; col < ncol; col += csplit) {
-            const int i0 = col / ny1, i1 = col - i0 * ny1;
-            {
-                const float2 qx = S.ft.qx[i0];
-                const int w0 = S.ft.wx[i0], z0 = S.ft.zx[i0];
-                const float2 qy = S.ft.qy[i1];
-                const int w1 = S.ft.wy[i1], z1 = S.ft.zy[i1];
-                const int row = I.cell_off + (w0 * I.nc[1] + w1) * I.nc[2];
-                int i2 = 0;
-                while (i2 < nzt) {
-                    // maximal run of z cells sharing one image shift (contiguous wrapped cells)
-                    const int w2 = S.ft.wz[i2];
-                    const int run = min(nzt - i2, I.nc[2] - w2);
-                    const float2 qz = S.ft.qz[i2];
-                    const bool zero_shift = z0 && z1 && S.ft.zz[i2];
-                    const int b = src_start[row + w2], e = src_start[row + w2 + run];
-                    i2 += run;
-                    const float qh[3] = {qx.x, qy.x, qz.x}, ql[3] = {qx.y, qy.y, qz.y};
-                    for (int base = b; base < e; base += 32) {
-                        const int j = base + lane;
-                        const int ncand = min(32, e - base);
-                        if (lane < ncand) {
-                            float4 ph = spos_hi[j], pl = spos_lo[j];
-                            float xh[3] = {ph.x, ph.y, ph.z}, xl[3] = {pl.x, pl.y, pl.z};
-                            float p3[3], l3[3];
+            S.t_hi[lane] = make_float4(th[0], th[1], th[2], 0.f);
+            S.t_lo[lane] = make_float4(tl[0], tl[1], tl[2], 0.f);
+            // bounding box of the item's targets (hi parts; the margin below covers the rest)
 #pragma unroll
-                            for (int a = 0; a < 3; a++) {
-                                float s, er;
-                                two_sum(xh[a], -qh[a], s, er);
-                                p3[a] = s;
-                                l3[a] = er + (xl[a] - ql[a]);
-                            }
-                            S.s_hi[lane] = make_float4(p3[0], p3[1], p3[2], 0.f);
-                            S.s_lo[lane] = make_float4(l3[0], l3[1], l3[2], 0.f);
-                            S.s_f[lane] = sfrc[j];
-                            S.c_x[lane] = p3[0];
-                            S.c_y[lane] = p3[1];
-                            S.c_z[lane] = p3[2];
-                        } else {  // padding: far from every target, active (finite) or not (+3e30)
-                            S.c_x[lane] = -3.0e30f;
-                            S.c_y[lane] = -3.0e30f;
-                            S.c_z[lane] = -3.0e30f;
-                        }
-                        __syncwarp();
-                        // classify candidate pairs of this lane's target: screened / blob region / series
-                        // (two candidates per packed FP32x2 operation; padded to 32)
-                        unsigned mi = 0, mr = 0;
-                        {
-                            const float2 ntx = make_float2(-th[0], -th[0]), nty = make_float2(-th[1], -th[1]),
-                                         ntz = make_float2(-th[2], -th[2]);
-#pragma unroll
-                            for (int jj = 0; jj < 32; jj += 2) {
-                                const float2 dx = __fadd2_rn(*reinterpret_cast<const float2*>(&S.c_x[jj]), ntx);
-                                const float2 dy = __fadd2_rn(*reinterpret_cast<const float2*>(&S.c_y[jj]), nty);
-                                const float2 dz = __fadd2_rn(*reinterpret_cast<const float2*>(&S.c_z[jj]), ntz);
-                                float2 r2 = __fmul2_rn(dx, dx);
-                                r2 = __ffma2_rn(dy, dy, r2);
-                                r2 = __ffma2_rn(dz, dz, r2);
-                                if (r2.x < rc2) mi |= 1u << jj;
-                                if (r2.y < rc2) mi |= 2u << jj;
-                                if (r2.x < rare2) mr |= 1u << jj;
-                                if (r2.y < rare2) mr |= 2u << jj;
-                            }
-                        }
-                        unsigned mn = mi & ~mr, mb = 0, ms = 0;
-                        for (unsigned m = mr; m; m &= m - 1) {  // rare: blob region or series
-                            const int jj = __ffs(m) - 1;
-                            float4 p = S.s_hi[jj];
-                            float dx = th[0] - p.x, dy = th[1] - p.y, dz = th[2] - p.z;
-                            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                            if ((r2 < rtiny2) | (r2 == 0.f))
-                                ms |= 1u << jj;
-                            else
-                                mb |= 1u << jj;
-                        }
-                        if (zero_shift && self_src >= base && self_src < base + ncand)
-                            ms &= ~(1u << (self_src - base));  // self pair: added in FP64 by the combine kernel
-                        // target-major queues
-                        unsigned long long cnt = (unsigned long long)__popc(mn) |
-                                                 ((unsigned long long)__popc(mb) << 16) |
-                                                 ((unsigned long long)__popc(ms) << 32);
-                        unsigned long long ex = warp_excl_scan64(cnt, lane);
-                        unsigned long long tot = __shfl_sync(kFull, ex + cnt, 31);
-                        {
-                            int pn = (int)(ex & 0xffff), pb = (int)((ex >> 16) & 0xffff), ps = (int)(ex >> 32);
-                            unsigned short tag = (unsigned short)(lane << 5);
-                            unsigned m = mn;
-                            while (m) {
-                                int jj = __ffs(m) - 1;
-                                m &= m - 1;
-                                S.q[0][pn++] = tag | jj;
-                            }
-                            m = mb;
-                            while (m) {
-                                int jj = __ffs(m) - 1;
-                                m &= m - 1;
-                                S.q[1][pb++] = tag | jj;
-                            }
-                            m = ms;
-                            while (m) {
-                                int jj = __ffs(m) - 1;
-                                m &= m - 1;
-                                S.q[2][ps++] = tag | jj;
-                            }
-                        }
-                        __syncwarp();
-                        const int nn = (int)(tot & 0xffff), nbq = (int)((tot >> 16) & 0xffff), nsq = (int)(tot >> 32);
-                        // screened pairs: T(r) polynomial of S - R_d only.  Lane l takes the
-                        // contiguous block [l K, (l+1) K) of the target-major queue and sums
-                        // runs of one target in registers: a target that starts inside the
-                        // block is added by this lane alone; the block's first target (which
-                        // may continue from earlier lanes) goes through one segmented reduction.
-                        {
-                            const int K = (nn + 31) >> 5;
-                            const int eb = min(lane * K, nn), ee = min(eb + K, nn);
-                            int cur = -1, first = -1;
-                            float a0 = 0, a1 = 0, a2 = 0, f0 = 0, f1 = 0, f2 = 0;
-                            for (int ei = eb; ei < ee; ei++) {
-                                const int qv = S.q[0][ei], t = qv >> 5, jj = qv & 31;
-                                float4 p = S.s_hi[jj], pl = S.s_lo[jj], f = S.s_f[jj];
-                                float4 a = S.t_hi[t], al = S.t_lo[t];
-                                float dx = (a.x - p.x) + (al.x - pl.x);
-                                float dy = (a.y - p.y) + (al.y - pl.y);
-                                float dz = (a.z - p.z) + (al.z - pl.z);
-                                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                                float ri = rsqrtf(r2);
-                                ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
-                                float r = r2 * ri;
-                                const float2 T12 = horner2<NP>(c12, fmaf(r, tds, tdo));
-                                float H1 = T12.x * ri, H2 = T12.y * (ri * ri * ri);
-                                float g = H2 * fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
-                                const float v0 = fmaf(H1, f.x, g * dx);
-                                const float v1 = fmaf(H1, f.y, g * dy);
-                                const float v2 = fmaf(H1, f.z, g * dz);
-                                if (t != cur) {
-                                    if (cur >= 0) {
-                                        if (first < 0) {
-                                            first = cur;
-                                            f0 = a0;
-                                            f1 = a1;
-                                            f2 = a2;
-                                        } else {
-                                            S.acc[0][cur] += a0;
-                                            S.acc[1][cur] += a1;
-                                            S.acc[2][cur] += a2;
-                                        }
-                                    }
-                                    cur = t;
-                                    a0 = v0;
-                                    a1 = v1;
-                                    a2 = v2;
-                                } else {
-                                    a0 += v0;
-                                    a1 += v1;
-                                    a2 += v2;
-                                }
-                            }
-                            if (cur >= 0) {
-                                if (first < 0) {
-                                    first = cur;
-                                    f0 = a0;
-                                    f1 = a1;
-                                    f2 = a2;
-                                } else {
-                                    S.acc[0][cur] += a0;
-                                    S.acc[1][cur] += a1;
-                                    S.acc[2][cur] += a2;
-                                }
-                            }
-                            __syncwarp();
-                            if (nn > 0) segment_reduce_add(f0, f1, f2, first >= 0 ? first : -1 - lane, lane, S.acc);
-                        }
-                        // near pairs (r < r_mid): the blob piece (R_eps - R_d itself) inside the
-                        // blob region, else the near piece of S - R_d
-                        for (int e0 = 0; e0 < nbq; e0 += 32) {
-                            const int ei = e0 + lane;
-                            float v0 = 0, v1 = 0, v2 = 0;
-                            int key = -1 - lane;
-                            if (ei < nbq) {
-                                const int qv = S.q[1][ei], t = qv >> 5, jj = qv & 31;
-                                key = t;
-                                float4 p = S.s_hi[jj], pl = S.s_lo[jj], f = S.s_f[jj];
-                                float4 a = S.t_hi[t], al = S.t_lo[t];
-                                float dx = (a.x - p.x) + (al.x - pl.x);
-                                float dy = (a.y - p.y) + (al.y - pl.y);
-                                float dz = (a.z - p.z) + (al.z - pl.z);
-                                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                                float ri = rsqrtf(r2);
-                                ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
-                                float r = r2 * ri;
-                                float H1, H2;
-                                if (r2 < rs2) {
-                                    const float2 h = cheb2(S.tb, nbp, fmaf(r, tbs, tbo));
-                                    H1 = h.x;
-                                    H2 = h.y * (ri * ri);
-                                } else {
-                                    const float2 T12 = cheb2(S.tn, nnp, fmaf(r, tns, tno));
-                                    H1 = T12.x * ri;
-                                    H2 = T12.y * (ri * ri * ri);
-                                }
-                                float g = H2 * fmaf(f.x, dx, fmaf(f.y, dy, f.z * dz));
-                                v0 = fmaf(H1, f.x, g * dx);
-                                v1 = fmaf(H1, f.y, g * dy);
-                                v2 = fmaf(H1, f.z, g * dz);
-                            }
-                            segment_reduce_add(v0, v1, v2, key, lane, S.acc);
-                        }
-                        // series pairs (r < r_tiny): FP64 series of R_eps - R_d, FP64 sums
-                        for (int e0 = 0; e0 < nsq; e0 += 32) {
-                            const int ei = e0 + lane;
-                            if (ei < nsq) {
-                                const int qv = S.q[2][ei], t = qv >> 5, jj = qv & 31;
-                                float4 p = S.s_hi[jj], pl = S.s_lo[jj], f = S.s_f[jj];
-                                float4 a = S.t_hi[t], al = S.t_lo[t];
-                                double dx = (double)(a.x - p.x) + (double)(al.x - pl.x);
-                                double dy = (double)(a.y - p.y) + (double)(al.y - pl.y);
-                                double dz = (double)(a.z - p.z) + (double)(al.z - pl.z);
-                                double rr = dx * dx + dy * dy + dz * dz;
-                                double H1, H2;
-                                if (T.blob) {
-                                    series_H(T, rr, H1, H2);
-                                } else if (rr == 0.0) {
-                                    H1 = T.self1;  // coincident points, eps = 0: the reference's r -> 0 limit
-                                    H2 = 0;
-                                } else {  // eps = 0, nearly coincident: singular kernel from the near piece
-                                    float r2f = (float)rr, ri = rsqrtf(r2f);
-                                    ri = ri * fmaf(-0.5f * r2f * ri, ri, 1.5f);
-                                    const float2 T12 = cheb2(S.tn, nnp, fmaf(r2f * ri, tns, tno));
-                                    H1 = (double)(T12.x * ri);
-                                    H2 = (double)(T12.y * (ri * ri * ri));
-                                }
-                                double fd = f.x * dx + f.y * dy + f.z * dz;
-                                atomicAdd(&S.acc64[0][t], H1 * f.x + H2 * fd * dx);
-                                atomicAdd(&S.acc64[1][t], H1 * f.y + H2 * fd * dy);
-                                atomicAdd(&S.acc64[2][t], H1 * f.z + H2 * fd * dz);
-                            }
-                        }
-                        __syncwarp();
-                        kahan_add(s0, k0, S.acc[0][lane]);
-                        kahan_add(s1, k1, S.acc[1][lane]);
-                        kahan_add(s2, k2, S.acc[2][lane]);
-                        S.acc[0][lane] = 0.f;
-                        S.acc[1][lane] = 0.f;
-                        S.acc[2][lane] = 0.f;
-                        __syncwarp();
-                    }
+            for (int a = 0; a < 3; a++) {
+                const int kmin = __reduce_min_sync(kFull, float_key(active ? th[a] : 3.0e30f));
+                const int kmax = __reduce_max_sync(kFull, float_key(active ? th[a] : -3.0e30f));
+                if (lane == 0) {
+                    S.box[a] = key_float(kmin);
+                    S.box[3 + a] = key_float(kmax);
                 }
             }
         }
+#pragma unroll
+        for (int c = 0; c < 6; c++) S.ks[c][lane] = 0.f;
+        __syncwarp();
+
+        // The item's stencil columns, 32 at a time (a lane per column): the
+        // column's part of the cutoff ball around the targets' box is a z-range;
+        // its cells are cut into runs at the periodic wrap and each run is
+        // narrowed to that z-range by binary search (sources are sorted by z
+        // within their cells).  The runs are gathered as segments and streamed
+        // through the warp in full chunks of 32 sources.
+        const int ny1 = 2 * I.S[1] + 1, ncol = (2 * I.S[0] + 1) * ny1;
+        const int csplit = max(1, I.csplit);
+        const int ncg = (ncol - F.group + csplit - 1) / csplit;
+        const float h0 = (float)I.h[0], h1 = (float)I.h[1], ih2 = (float)(1.0 / I.h[2]);
+        const float marg = 4e-6f * (float)fmax(I.L[0], fmax(I.L[1], I.L[2]));
+        const int nzt = F.zb - F.za + 2 * I.S[2] + 1;
+        // gather segments until the list could overflow in the next round, stream
+        // them (one call site keeps the hot loop once in the instruction cache),
+        // repeat; per-lane column cursors persist across the streaming
+        int nseg = 0, kb = 0;
+        bool open = false;
+        int i0 = 0, i1 = 0, i2 = 1, i2b = 0, row = 0;
+        while (true) {
+            while (true) {
+                if (!open) {
+                    if (kb >= ncg) break;
+                    i2 = 1;
+                    i2b = 0;
+                    if (kb + lane < ncg) {
+                        const int col = F.group + (kb + lane) * csplit;
+                        i0 = col / ny1;
+                        i1 = col - i0 * ny1;
+                        const float o0 = (float)(i0 - I.S[0]), o1 = (float)(i1 - I.S[1]);
+                        const float dx = fmaxf(0.f, fmaxf(o0 * h0 - S.box[3], S.box[0] - (o0 + 1.f) * h0) - marg);
+                        const float dy = fmaxf(0.f, fmaxf(o1 * h1 - S.box[4], S.box[1] - (o1 + 1.f) * h1) - marg);
+                        const float d2 = fmaf(dx, dx, dy * dy);
+                        if (d2 < K.rc2) {
+                            const float rz = sqrtf(K.rc2 - d2) + 2.f * marg;
+                            i2 = max(0, (int)floorf((S.box[2] - rz) * ih2) + I.S[2]);
+                            i2b = min(nzt - 1, (int)floorf((S.box[5] + rz) * ih2) + I.S[2]);
+                            row = I.cell_off + (S.ft.wx[i0] * I.nc[1] + S.ft.wy[i1]) * I.nc[2];
+                        }
+                    }
+                    kb += 32;
+                    open = true;
+                }
+                if (!__any_sync(kFull, i2 <= i2b)) {
+                    open = false;
+                    continue;
+                }
+                if (nseg > kSeg - 32) break;  // a round adds up to 32 segments
+                int sb = 0, sn = 0, meta = 0;
+                if (i2 <= i2b) {
+                    const int w2 = S.ft.wz[i2];
+                    const int run = min(i2b - i2 + 1, I.nc[2] - w2);
+                    sb = src_start[row + w2];
+                    sn = src_start[row + w2 + run] - sb;
+                    meta = i0 | (i1 << 5) | (i2 << 10);
+                    i2 += run;
+                }
+                const unsigned bal = __ballot_sync(kFull, sn > 0);
+                if (sn > 0) {
+                    const int pos = nseg + __popc(bal & lt);
+                    S.sg_b[pos] = sb;
+                    S.sg_n[pos] = sn;
+                    S.sg_meta[pos] = meta;
+                }
+                nseg += __popc(bal);
+            }
+            if (nseg == 0) break;
+            __syncwarp();
+            stream_segments<NP>(S, I, T, K, c12, F, nseg, lane, spos_hi, spos_lo, sfrc);
+            nseg = 0;
+        }
+        // the rest of the near queue, then the item's sums
+        {
+            const int nq = S.nq_n;
+            __syncwarp();
+            if (nq > 0) near_flush(S, T, nq, nq, lane);
+            if (lane == 0) S.nq_n = 0;
+        }
+        __syncwarp();
+        chunk_sums(S, lane);
         if (active) {  // the item's part of the target's sum (other column groups add theirs)
             size_t o = 3 * (size_t)tidx;
-            atomicAdd(u_real + o, ((double)s0 - (double)k0) + S.acc64[0][lane]);
-            atomicAdd(u_real + o + 1, ((double)s1 - (double)k1) + S.acc64[1][lane]);
-            atomicAdd(u_real + o + 2, ((double)s2 - (double)k2) + S.acc64[2][lane]);
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+                atomicAdd(u_real + o + c, ((double)S.ks[c][lane] - (double)S.ks[3 + c][lane]) + S.acc64[c][lane]);
         }
         S.acc64[0][lane] = 0.0;
         S.acc64[1][lane] = 0.0;
@@ -530,8 +686,8 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
 void launch_real_mixed(int npoly, const PbInst* inst, const PbTables* tab, const int4* items, const int* nitems_ptr,
                        int nitems_max,
                        const float4* spos_hi, const float4* spos_lo, const float4* sfrc, const int* src_start,
-                       const float4* tpos_hi, const float4* tpos_lo, int ntgt_cap, double* u_real, int* counter,
-                       int nsm, cudaStream_t s)
+                       const float4* tpos_hi, const float4* tpos_lo, int ntgt_cap,
+                       double* u_real, int* counter, int nsm, cudaStream_t s)
 {
     if (nitems_max <= 0) return;
     cudaMemsetAsync(counter, 0, sizeof(int), s);
@@ -541,8 +697,8 @@ void launch_real_mixed(int npoly, const PbInst* inst, const PbTables* tab, const
     if (blocks > need) blocks = need;
 #define PB_LAUNCH_REAL(NP)                                                                                            \
     k_real_mixed<NP><<<blocks, kRealWarps * 32, 0, s>>>(inst, tab, items, nitems_ptr, spos_hi, spos_lo, sfrc,        \
-                                                         src_start,                                                  \
-                                                         tpos_hi, tpos_lo, u_real, counter, nitems_max)
+                                                         src_start, tpos_hi, tpos_lo, u_real, counter,               \
+                                                         nitems_max)
     if (npoly <= 16)
         PB_LAUNCH_REAL(16);
     else if (npoly <= 20)

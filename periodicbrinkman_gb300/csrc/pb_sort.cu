@@ -151,13 +151,18 @@ void launch_scatter(const int* cell_of, int ncap, const int* ntot, const int* st
     k_scatter<<<(ncap + 255) / 256, 256, 0, s>>>(cell_of, ntot, start, fill, perm);
 }
 
-// Rank sort of each cell's entries (a warp per cell, persistent over the
-// actual cells): entry v goes to slot start + #{u in cell : u < v}.  Entries
-// are distinct particle indices.
+// Rank sort of each cell's entries by (z, index) (a warp per cell, persistent
+// over the actual cells): entry v goes to slot start + #{u in cell : (z_u, u) <
+// (z_v, v)}, z the coordinate wrapped in FP32.  Consecutive targets
+// then lie close in z, which narrows the z-range of a real-space work item.
+// Cells of more than kSortMax entries keep the (index) scatter order.
+constexpr int kSortMax = 1024;
+
 __global__ void k_sort_cells(const int* __restrict__ perm_in, int* __restrict__ perm_out,
-                             const int* __restrict__ start, const int* __restrict__ ncell_p)
+                             const int* __restrict__ start, const int* __restrict__ cell_offsets,
+                             const PbInst* __restrict__ inst, int ninst, const double* __restrict__ pos)
 {
-    const int ncell = *ncell_p;
+    const int ncell = cell_offsets[ninst];
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < ncell; cell += nwarps) {
@@ -166,25 +171,47 @@ __global__ void k_sort_cells(const int* __restrict__ perm_in, int* __restrict__ 
             if (n == 1 && lane == 0) perm_out[b] = perm_in[b];
             continue;
         }
-        if (n > 4096) {  // very large cells keep the scatter order
+        const int q = find_instance(cell_offsets, ninst, cell);
+        if (n > kSortMax) {
             for (int i = lane; i < n; i += 32) perm_out[b + i] = perm_in[b + i];
             continue;
         }
-        for (int i = lane; i < n; i += 32) {
-            int v = perm_in[b + i], rank = 0;
-            for (int j = 0; j < n; j++) rank += (perm_in[b + j] < v);
-            perm_out[b + rank] = v;
+        const PbInst& I = inst[q];
+        // FP32 key (the order only shapes the work items; FP64 would cost the GPU's slow FP64 pipe)
+        const float Lz = (float)I.L[2], iLz = (float)I.iL[2];
+        auto zkey = [&](int v) {
+            float z = (float)pos[3 * (size_t)v + 2];
+            z -= Lz * floorf(z * iLz);
+            return (z == z) ? z : 0.f;
+        };
+        for (int ib = 0; ib < n; ib += 32) {
+            const int i = ib + lane;
+            const int v = i < n ? perm_in[b + i] : 0;
+            const float z = i < n ? zkey(v) : 0.f;
+            int rank = 0;
+            for (int jb = 0; jb < n; jb += 32) {
+                const int j = jb + lane;
+                const int u = j < n ? perm_in[b + j] : 0;
+                const float zu = j < n ? zkey(u) : 0.f;
+                const int m = min(32, n - jb);
+                for (int k = 0; k < m; k++) {
+                    const int uk = __shfl_sync(kFull, u, k);
+                    const float zk = __shfl_sync(kFull, zu, k);
+                    rank += (zk < z) || (zk == z && uk < v);
+                }
+            }
+            if (i < n) perm_out[b + rank] = v;
         }
     }
 }
 
-void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap, const int* ncell, int nsm,
-                       cudaStream_t s)
+void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap, const int* cell_offsets,
+                       const PbInst* inst, int ninst, const double* pos, int nsm, cudaStream_t s)
 {
     if (ncell_cap <= 0) return;
     long long blocks = ((long long)ncell_cap * 32 + 255) / 256;
     if (blocks > (long long)nsm * 16) blocks = (long long)nsm * 16;
-    k_sort_cells<<<(int)blocks, 256, 0, s>>>(perm, perm_tmp, start, ncell);
+    k_sort_cells<<<(int)blocks, 256, 0, s>>>(perm, perm_tmp, start, cell_offsets, inst, ninst, pos);
 }
 
 __global__ void k_prepare_mixed(const double* __restrict__ pos, const double* __restrict__ frc,
