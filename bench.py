@@ -451,9 +451,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="serve", choices=["serve", "single"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", nargs="?", const="single", choices=["single", "slot"],
-                    help="for ncu: run the single-solve plan twice (eager, then capture+replay), or (slot) one "
-                         "128^3 serving slot holding two requests of the stream three times, and exit")
+    ap.add_argument("--profile", nargs="?", const="single", choices=["single", "slot", "serve"],
+                    help="for ncu: run the single-solve plan twice (eager, then capture+replay), (slot) one "
+                         "128^3 serving slot holding two requests of the stream three times, or (serve) the "
+                         "first 300 requests of the serving stream through the server, and exit")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -468,6 +469,9 @@ def main():
     torch.cuda.set_device(local)
     if args.profile == "slot":
         profile_slot(torch)
+        return
+    if args.profile == "serve":
+        profile_serve(torch)
         return
     if args.profile:
         w = SINGLE
@@ -574,6 +578,26 @@ def profile_slot(torch):
     print(json.dumps({"profile": "slot_128_two_stream_requests", "n_src": [int(N[k]) for k in ks],
                       "kernels_per_execution": slot.kernel_count}))
     slot.close()
+
+
+def profile_serve(torch, nreq=300):
+    """The first `nreq` requests of the serving stream submitted at once (for an ncu launch list)."""
+    w = SERVE
+    arrive, N, alpha, eps, tol = gen_stream(w)
+    pool = InputPool(w["nmax"], sets=4, pinned=True)
+    srv = serve_server(w)
+    outs, tickets = [], []
+    for k in range(nreq):
+        x, f, y = pool.get(k, int(N[k]))
+        U = host_array((y.shape[0], 3), True)
+        outs.append(U)
+        tickets.append(srv.submit(x, f, 1.0, float(alpha[k]), float(eps[k]), y=y, out=U, tol=float(tol[k])))
+    for t in tickets:
+        srv.result(t)
+    st = srv.stats()
+    srv.close()
+    print(json.dumps({"profile": "serve_stream_first_%d" % nreq, "batches": st["batches"],
+                      "kernels": st["kernels"], "mean_batch": st["mean_batch"]}))
 
 
 def _cpu_single():

@@ -288,12 +288,28 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const size_t M12 = (size_t)I.M[1] * I.M[2];
     const float4* g4 = reinterpret_cast<const float4*>(grid + I.grid_off);
     float s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0;
+    // quotients by multiply and shift (exact for id < 2^15): no integer division in the loop
+    const unsigned inv_p2 = ((1u << 20) + P2 - 1) / P2, inv_pz = ((1u << 20) + Pz - 1) / Pz;
     for (int id = lane; id < P2 * R; id += 32) {
-        const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
+        const int xs = (int)(((unsigned)id * inv_p2) >> 20), yz = id - xs * P2;
+        const int py = (int)(((unsigned)yz * inv_pz) >> 20), pz = yz - py * Pz;
         const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
-        // one x row of the window in plain FP32 (<= 32 same-sign-weighted terms), rows Kahan-summed
+        // one x row of the window in plain FP32 (<= 32 same-sign-weighted terms), rows Kahan-summed;
+        // the first 16 points of the row are loaded together (predicated), so that many loads
+        // are in flight at once
         float r0 = 0, r1 = 0, r2 = 0;
-        for (int px = xs; px < Px; px += R) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const int px = xs + k * R;
+            if (px < Px) {
+                const float wx = wgt[w][0][px];
+                const float4 v = __ldg(g4 + (size_t)gidx[w][0][px] * M12 + oyz);
+                r0 = fmaf(wx, v.x, r0);
+                r1 = fmaf(wx, v.y, r1);
+                r2 = fmaf(wx, v.z, r2);
+            }
+        }
+        for (int px = xs + 16 * R; px < Px; px += R) {
             const float wx = wgt[w][0][px];
             const float4 v = __ldg(g4 + (size_t)gidx[w][0][px] * M12 + oyz);
             r0 = fmaf(wx, v.x, r0);

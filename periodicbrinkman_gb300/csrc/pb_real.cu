@@ -600,8 +600,8 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
         const int ny1 = 2 * I.S[1] + 1, ncol = (2 * I.S[0] + 1) * ny1;
         const int csplit = max(1, I.csplit);
         const int ncg = (ncol - F.group + csplit - 1) / csplit;
-        const float h0 = (float)I.h[0], h1 = (float)I.h[1], ih2 = (float)(1.0 / I.h[2]);
-        const float marg = 4e-6f * (float)fmax(I.L[0], fmax(I.L[1], I.L[2]));
+        const float h0 = (float)I.h[0], h1 = (float)I.h[1], ih2 = 1.f / (float)I.h[2];
+        const float marg = 4e-6f * fmaxf((float)I.L[0], fmaxf((float)I.L[1], (float)I.L[2]));
         const int nzt = F.zb - F.za + 2 * I.S[2] + 1;
         // gather segments until the list could overflow in the next round, stream
         // them (one call site keeps the hot loop once in the instruction cache),
