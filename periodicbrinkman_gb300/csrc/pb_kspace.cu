@@ -832,6 +832,491 @@ __global__ void k_fft_x_green(typename Cx<T>::t* __restrict__ spec, const PbInst
     }
 }
 
+// ---------------------------------------------------------------------------
+// Register FFT passes (FP32 grids, line lengths 4..256)
+// ---------------------------------------------------------------------------
+// A line of length N = N1 N2 is transformed by T threads, each holding N/T
+// values in registers: N2 FFTs of length N1 over x[N2 n1 + n2] (thread t takes
+// n2 = t, t + T, ...), the twiddles W_N^(n2 k1), one exchange through shared
+// memory, then N1 FFTs of length N2 (thread t takes k1 = t, t + T, ...); the
+// result X[k1 + N1 k2] stays in the registers of the thread that owns k1.
+// Lengths up to 16 are radix-2 butterflies on named registers with constant
+// twiddles.  Forward uses W = exp(-2 pi i / N), inverse its conjugate, both
+// unnormalised, as the shared-memory passes above.
+
+// cos and sin of 2 pi m / 16
+__host__ __device__ constexpr float c16(int m)
+{
+    return m == 0 ? 1.f : m == 1 ? 0.92387953251128674f : m == 2 ? 0.70710678118654752f
+         : m == 3 ? 0.38268343236508977f : m == 4 ? 0.f : m == 5 ? -0.38268343236508977f
+         : m == 6 ? -0.70710678118654752f : -0.92387953251128674f;
+}
+__host__ __device__ constexpr float s16(int m)
+{
+    return m == 0 ? 0.f : m == 1 ? 0.38268343236508977f : m == 2 ? 0.70710678118654752f
+         : m == 3 ? 0.92387953251128674f : m == 4 ? 1.f : m == 5 ? 0.92387953251128674f
+         : m == 6 ? 0.70710678118654752f : 0.38268343236508977f;
+}
+
+// x * W_16^m (m < 8 and known at compile time after unrolling)
+template <bool INV>
+__device__ __forceinline__ float2 w16_mul(float2 x, int m)
+{
+    if (m == 0) return x;
+    if (m == 4) return INV ? make_float2(-x.y, x.x) : make_float2(x.y, -x.x);
+    const float c = c16(m), s = INV ? s16(m) : -s16(m);
+    return make_float2(fmaf(x.x, c, -x.y * s), fmaf(x.x, s, x.y * c));
+}
+
+__host__ __device__ constexpr int bitrev(int i, int bits)
+{
+    int r = 0;
+    for (int b = 0; b < bits; b++) r |= ((i >> b) & 1) << (bits - 1 - b);
+    return r;
+}
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
+
+// In-register FFT of R <= 16 values, natural order in and out.
+template <int R, bool INV>
+__device__ __forceinline__ void fft_reg(float2 (&v)[R])
+{
+    constexpr int L = ilog2(R);
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        const int j = bitrev(i, L);
+        if (j > i) {
+            const float2 t = v[i];
+            v[i] = v[j];
+            v[j] = t;
+        }
+    }
+#pragma unroll
+    for (int h = 1; h < R; h <<= 1) {
+#pragma unroll
+        for (int k = 0; k < h; k++) {
+            const int m = k * (8 / h);  // W_{2h}^k = W_16^(8 k / h)
+#pragma unroll
+            for (int j = k; j < R; j += 2 * h) {
+                const float2 b = w16_mul<INV>(v[j + h], m), a = v[j];
+                v[j] = make_float2(a.x + b.x, a.y + b.y);
+                v[j + h] = make_float2(a.x - b.x, a.y - b.y);
+            }
+        }
+    }
+}
+
+// x * W_N^m from the table of W_N^k, k < N/2 (conjugated for the inverse)
+template <bool INV>
+__device__ __forceinline__ float2 twN_mul(float2 x, int m, int N, const float2* __restrict__ tw)
+{
+    const int h = N >> 1;
+    float2 w = __ldg(tw + (m < h ? m : m - h));
+    if (m >= h) w = make_float2(-w.x, -w.y);
+    if (INV) w.y = -w.y;
+    return cmul(x, w);
+}
+
+// Four-step line transform: A (stage-1 layout, A[a][n1] = x[N2 n1 + t + T a]) ->
+// B (stage-2 layout, B[b][k2] = X[t + T b + N1 k2]).  `ex` holds N elements of
+// this line at stride LS (ex[e * LS]); the caller synchronises before the
+// exchange buffer is reused.
+// Shared-memory slot of element e of a line: ex[e * LS] for the passes
+// whose lines sit in the lanes of a warp (y, x); for the z passes, where a
+// warp holds 32/T lines times the T threads of each, the line index `ll` is
+// rotated within its aligned group of 32 by (32/T) ((e + e/N1) mod T), so
+// that the T threads of a line, which differ in n2 (stage 1) or in k1
+// (stage 2), hit different banks.
+template <int T, int N1>
+__device__ __forceinline__ int zslot(int e, int ll, int LS)
+{
+    const int s = (e + e / N1) & (T - 1);
+    return e * LS + (ll & ~31) + ((ll + (32 / T) * s) & 31);
+}
+
+template <int N1, int N2, int T, bool INV, bool ZSW = false>
+__device__ __forceinline__ void line_fft(float2 (&A)[N2 / T][N1], float2 (&B)[N1 / T][N2], float2* ex, int LS, int t,
+                                         const float2* __restrict__ tw, int ll = 0)
+{
+    constexpr int N = N1 * N2;
+#pragma unroll
+    for (int a = 0; a < N2 / T; a++) {
+        fft_reg<N1, INV>(A[a]);
+        const int n2 = t + T * a;
+        if (N2 > 1) {
+#pragma unroll
+            for (int k1 = 1; k1 < N1; k1++) A[a][k1] = twN_mul<INV>(A[a][k1], n2 * k1, N, tw);
+        }
+    }
+    if (N2 == 1) {
+#pragma unroll
+        for (int b = 0; b < N1 / T; b++) B[b][0] = A[0][b];
+        return;
+    }
+#pragma unroll
+    for (int a = 0; a < N2 / T; a++) {
+        const int n2 = t + T * a;
+#pragma unroll
+        for (int k1 = 0; k1 < N1; k1++) {
+            const int e = n2 * N1 + k1;
+            ex[ZSW ? zslot<T, N1>(e, ll, LS) : e * LS] = A[a][k1];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < N1 / T; b++) {
+        const int k1 = t + T * b;
+#pragma unroll
+        for (int n2 = 0; n2 < N2; n2++) {
+            const int e = n2 * N1 + k1;
+            B[b][n2] = ex[ZSW ? zslot<T, N1>(e, ll, LS) : e * LS];
+        }
+        fft_reg<N2, INV>(B[b]);
+    }
+}
+
+// y pass: lines along y (stride Mzh) of the spectrum volumes; a block is 32
+// consecutive z' lines (lanes) times T threads per line (warps).
+template <int N1, int N2, int T, bool INV>
+__global__ void __launch_bounds__(32 * T)
+    k_fft_y_reg(float2* __restrict__ spec, int Mx, int Mzh, const float2* __restrict__ tw,
+                const PbInst* __restrict__ inst, const int* __restrict__ bucket_inst)
+{
+    constexpr int N = N1 * N2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* ex = (float2*)smem_raw;
+    const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
+    const int ntile = (Mzh + 31) >> 5;
+    const long long blk = blockIdx.x;
+    const int tile = (int)(blk % ntile);
+    const long long vx = blk / ntile;  // volume * Mx + x
+    if (!fft_live(inst, bucket_inst, vx / Mx / 3)) return;
+    const int z = tile * 32 + lane;
+    const bool ok = z < Mzh;
+    float2* base = spec + (size_t)vx * N * Mzh + (ok ? z : 0);
+    float2 A[N2 / T][N1], B[N1 / T][N2];
+#pragma unroll
+    for (int a = 0; a < N2 / T; a++)
+#pragma unroll
+        for (int n1 = 0; n1 < N1; n1++)
+            A[a][n1] = ok ? base[(size_t)(N2 * n1 + t + T * a) * Mzh] : make_float2(0.f, 0.f);
+    line_fft<N1, N2, T, INV>(A, B, ex + lane, 32, t, tw);
+#pragma unroll
+    for (int b = 0; b < N1 / T; b++)
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++)
+            if (ok) base[(size_t)(t + T * b + N1 * k2) * Mzh] = B[b][k2];
+}
+
+// x pass fused with the Green multiply: for 32 consecutive z' lines of one
+// (instance, y), the three components' forward x transforms are kept in
+// shared memory (SP[c][k][line]), multiplied by the Green tensor and
+// transformed back.  The Green multiply is the one of k_fft_x_green.
+template <int N1, int N2, int T>
+__global__ void __launch_bounds__(32 * T)
+    k_fft_x_green_reg(float2* __restrict__ spec, const PbInst* __restrict__ inst, const int* __restrict__ bucket_inst,
+                      long long base_off, int My, int Mzh, int Mz, const float2* __restrict__ tw)
+{
+    constexpr int N = N1 * N2;  // Mx
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* SP = (float2*)smem_raw;  // [3][N][32]
+    const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
+    const int ntile = (Mzh + 31) >> 5;
+    const long long blk = blockIdx.x;
+    const int tile = (int)(blk % ntile);
+    const long long r = blk / ntile;
+    const int y = (int)(r % My);
+    const int qi = (int)(r / My);
+    if (!fft_live(inst, bucket_inst, qi)) return;
+    const PbInst& I = inst[bucket_inst[qi]];
+    const int z = tile * 32 + lane;
+    const bool ok = z < Mzh;
+    const size_t vol = (size_t)N * My * Mzh, xs = (size_t)My * Mzh;
+    float2* base = spec + (I.spec_off - base_off) + (size_t)y * Mzh + (ok ? z : 0);
+    float2 A[N2 / T][N1], B[N1 / T][N2];
+#pragma unroll 1
+    for (int c = 0; c < 3; c++) {
+        float2* ex = SP + (size_t)c * N * 32 + lane;
+#pragma unroll
+        for (int a = 0; a < N2 / T; a++)
+#pragma unroll
+            for (int n1 = 0; n1 < N1; n1++)
+                A[a][n1] = ok ? base[c * vol + (size_t)(N2 * n1 + t + T * a) * xs] : make_float2(0.f, 0.f);
+        line_fft<N1, N2, T, false>(A, B, ex, 32, t, tw);
+        __syncthreads();
+#pragma unroll
+        for (int b = 0; b < N1 / T; b++)
+#pragma unroll
+            for (int k2 = 0; k2 < N2; k2++) ex[(size_t)(t + T * b + N1 * k2) * 32] = B[b][k2];
+    }
+    __syncthreads();
+    // Green multiply (as k_fft_x_green, in FP32)
+    {
+        const float tpx = (float)(2 * kPiD / I.L[0]), tpy = (float)(2 * kPiD / I.L[1]),
+                    tpz = (float)(2 * kPiD / I.L[2]);
+        const double a2d = I.alpha * I.alpha;
+        const float a2 = (float)a2d;
+        const float a1oa2 = (float)(-expm1(-a2d * I.d * I.d / 4) / a2d);
+        const float gexp = (float)(I.d * I.d / 4 - I.eta / 2);
+        const float kfac = (float)I.kfac;
+        const int ny = (y < My / 2) ? y : y - My;
+        const bool ynyq = (2 * y == My);
+        const float ky = tpy * (float)ny, kzv = tpz * (float)z;
+#pragma unroll 4
+        for (int i = t; i < N; i += T) {
+            float2* v0 = SP + (size_t)i * 32 + lane;
+            float2* v1 = v0 + (size_t)N * 32;
+            float2* v2 = v1 + (size_t)N * 32;
+            const int nx = (i < N / 2) ? i : i - N;
+            const bool zero = (2 * i == N) || ynyq || (2 * z == Mz) || (nx == 0 && ny == 0 && z == 0);
+            if (zero) {
+                *v0 = make_float2(0.f, 0.f);
+                *v1 = make_float2(0.f, 0.f);
+                *v2 = make_float2(0.f, 0.f);
+                continue;
+            }
+            const float kx = tpx * (float)nx;
+            const float kn = kx * kx + ky * ky + kzv * kzv;
+            const float sc = kfac * (1.f + a1oa2 * kn) * expf(-kn * gexp) / (kn * (kn + a2));
+            const float2 A0 = *v0, A1 = *v1, A2 = *v2;
+            const float dr = kx * A0.x + ky * A1.x + kzv * A2.x;
+            const float di = kx * A0.y + ky * A1.y + kzv * A2.y;
+            *v0 = make_float2(sc * (kn * A0.x - kx * dr), sc * (kn * A0.y - kx * di));
+            *v1 = make_float2(sc * (kn * A1.x - ky * dr), sc * (kn * A1.y - ky * di));
+            *v2 = make_float2(sc * (kn * A2.x - kzv * dr), sc * (kn * A2.y - kzv * di));
+        }
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int c = 0; c < 3; c++) {
+        float2* ex = SP + (size_t)c * N * 32 + lane;
+#pragma unroll
+        for (int a = 0; a < N2 / T; a++)
+#pragma unroll
+            for (int n1 = 0; n1 < N1; n1++) A[a][n1] = ex[(size_t)(N2 * n1 + t + T * a) * 32];
+        __syncthreads();
+        line_fft<N1, N2, T, true>(A, B, ex, 32, t, tw);
+#pragma unroll
+        for (int b = 0; b < N1 / T; b++)
+#pragma unroll
+            for (int k2 = 0; k2 < N2; k2++)
+                if (ok) base[c * vol + (size_t)(t + T * b + N1 * k2) * xs] = B[b][k2];
+    }
+}
+
+// z pass, forward, FP32 float4 grid lines (instance, x, y) of length Mz = 2 Nh:
+// the packed half-length transform of the three components, then the split
+// into the Nh + 1 half-spectrum values of each.  256 threads: 256 / T lines.
+template <int N1, int N2, int T>
+__global__ void __launch_bounds__(256)
+    k_fft_z_fwd_reg(const float4* __restrict__ grid, float2* __restrict__ spec, long long nlines, int Mx, int My,
+                    const float2* __restrict__ tw, const float2* __restrict__ rt, const PbInst* __restrict__ inst,
+                    const int* __restrict__ bucket_inst)
+{
+    constexpr int Nh = N1 * N2, Mzh = Nh + 1, LPC = 256 / T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* ex = (float2*)smem_raw;  // [3][Nh][LPC]
+    const int t = threadIdx.x % T, ll = threadIdx.x / T;
+    const long long l0 = (long long)blockIdx.x * LPC;
+    const long long xy = (long long)Mx * My;
+    const long long lastl = min(l0 + LPC, nlines) - 1;
+    if (!fft_live(inst, bucket_inst, l0 / xy) && !fft_live(inst, bucket_inst, lastl / xy)) return;
+    const long long line = l0 + ll;
+    const bool ok = line < nlines;
+    const float4* src = grid + (size_t)(ok ? line : 0) * (2 * Nh);
+    float2 A0[N2 / T][N1], A1[N2 / T][N1], A2[N2 / T][N1];
+#pragma unroll
+    for (int a = 0; a < N2 / T; a++)
+#pragma unroll
+        for (int n1 = 0; n1 < N1; n1++) {
+            const int n = N2 * n1 + t + T * a;
+            const float4 p = ok ? src[2 * n] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 q = ok ? src[2 * n + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+            A0[a][n1] = make_float2(p.x, q.x);
+            A1[a][n1] = make_float2(p.y, q.y);
+            A2[a][n1] = make_float2(p.z, q.z);
+        }
+    float2 B0[N1 / T][N2], B1[N1 / T][N2], B2[N1 / T][N2];
+    line_fft<N1, N2, T, false, true>(A0, B0, ex, LPC, t, tw, ll);
+    line_fft<N1, N2, T, false, true>(A1, B1, ex + (size_t)Nh * LPC, LPC, t, tw, ll);
+    line_fft<N1, N2, T, false, true>(A2, B2, ex + (size_t)2 * Nh * LPC, LPC, t, tw, ll);
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < N1 / T; b++)
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) {
+            const int k = t + T * b + N1 * k2, o = zslot<T, N1>(k, ll, LPC);
+            ex[o] = B0[b][k2];
+            ex[(size_t)Nh * LPC + o] = B1[b][k2];
+            ex[(size_t)2 * Nh * LPC + o] = B2[b][k2];
+        }
+    __syncthreads();
+    if (!ok) return;
+    const long long bi = line / xy, rest = line - bi * xy;
+    for (int k = t; k < Mzh; k += T) {
+        const float2 w = __ldg(rt + k);
+        const int ok_ = zslot<T, N1>(k == Nh ? 0 : k, ll, LPC), om = zslot<T, N1>(k == 0 ? 0 : Nh - k, ll, LPC);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const float2* Z = ex + (size_t)c * Nh * LPC;
+            const float2 zk = Z[ok_];
+            const float2 zm = Z[om];
+            const float2 E = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            const float2 Od = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+            const float2 wo = cmul(w, Od);
+            spec[((size_t)(3 * bi + c) * xy + rest) * Mzh + k] = make_float2(E.x + wo.x, E.y + wo.y);
+        }
+    }
+}
+
+// z pass, inverse: Nh + 1 half-spectrum values of each component -> one real
+// float4 grid line (three components interleaved, fourth zero).
+template <int N1, int N2, int T>
+__global__ void __launch_bounds__(256)
+    k_fft_z_inv_reg(const float2* __restrict__ spec, float4* __restrict__ grid, long long nlines, int Mx, int My,
+                    const float2* __restrict__ tw, const float2* __restrict__ rt, const PbInst* __restrict__ inst,
+                    const int* __restrict__ bucket_inst)
+{
+    constexpr int Nh = N1 * N2, Mzh = Nh + 1, LPC = 256 / T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* ex = (float2*)smem_raw;  // [3][Nh][LPC]
+    const int t = threadIdx.x % T, ll = threadIdx.x / T;
+    const long long l0 = (long long)blockIdx.x * LPC;
+    const long long xy = (long long)Mx * My;
+    const long long lastl = min(l0 + LPC, nlines) - 1;
+    if (!fft_live(inst, bucket_inst, l0 / xy) && !fft_live(inst, bucket_inst, lastl / xy)) return;
+    const long long line = l0 + ll;
+    const bool ok = line < nlines;
+    const long long bi = (ok ? line : 0) / xy, rest = (ok ? line : 0) - bi * xy;
+    float2 A[3][N2 / T][N1];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const float2* src = spec + ((size_t)(3 * bi + c) * xy + rest) * Mzh;
+#pragma unroll
+        for (int a = 0; a < N2 / T; a++)
+#pragma unroll
+            for (int n1 = 0; n1 < N1; n1++) {
+                const int k = N2 * n1 + t + T * a;
+                float2 Z = make_float2(0.f, 0.f);
+                if (ok) {
+                    const float2 xk = src[k], xm = src[Nh - k];
+                    const float2 e = make_float2(xk.x + xm.x, xk.y - xm.y);
+                    const float2 dlt = make_float2(xk.x - xm.x, xk.y + xm.y);
+                    float2 wc = __ldg(rt + k);
+                    wc.y = -wc.y;
+                    const float2 od = cmul(wc, dlt);
+                    Z = make_float2(e.x - od.y, e.y + od.x);
+                }
+                A[c][a][n1] = Z;
+            }
+    }
+    float2 B0[N1 / T][N2], B1[N1 / T][N2], B2[N1 / T][N2];
+    line_fft<N1, N2, T, true, true>(A[0], B0, ex, LPC, t, tw, ll);
+    line_fft<N1, N2, T, true, true>(A[1], B1, ex + (size_t)Nh * LPC, LPC, t, tw, ll);
+    line_fft<N1, N2, T, true, true>(A[2], B2, ex + (size_t)2 * Nh * LPC, LPC, t, tw, ll);
+    if (!ok) return;
+    float4* dst = grid + (size_t)line * (2 * Nh);
+#pragma unroll
+    for (int b = 0; b < N1 / T; b++)
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) {
+            const int k = t + T * b + N1 * k2;
+            dst[2 * k] = make_float4(B0[b][k2].x, B1[b][k2].x, B2[b][k2].x, 0.f);
+            dst[2 * k + 1] = make_float4(B0[b][k2].y, B1[b][k2].y, B2[b][k2].y, 0.f);
+        }
+}
+
+// Four-step shape (N1, N2, T) of the register passes for a line length; 0 when
+// the length has no register pass (the shared-memory passes are used).
+struct RegShape {
+    int n1, n2, t;
+};
+static RegShape reg_shape(int N, bool z)
+{
+    switch (N) {
+        case 4: return {4, 1, 1};
+        case 8: return {4, 2, 2};
+        case 16: return {4, 4, 4};
+        case 32: return {8, 4, 4};
+        case 64: return {8, 8, 8};
+        case 128: return z ? RegShape{0, 0, 0} : RegShape{16, 8, 8};
+        case 256: return z ? RegShape{0, 0, 0} : RegShape{16, 16, 16};
+        default: return {0, 0, 0};
+    }
+}
+
+template <int N1, int N2, int T>
+static void launch_y_reg(float2* spec, int nvol, int Mx, int Mzh, const float2* tw, bool inverse, const PbInst* inst,
+                         const int* bucket, cudaStream_t s)
+{
+    const size_t sm = (size_t)N1 * N2 * 32 * sizeof(float2);
+    const long long nb = (long long)nvol * Mx * ((Mzh + 31) / 32);
+    if (inverse) {
+        cudaFuncSetAttribute(k_fft_y_reg<N1, N2, T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_fft_y_reg<N1, N2, T, true><<<(unsigned)nb, 32 * T, sm, s>>>(spec, Mx, Mzh, tw, inst, bucket);
+    } else {
+        cudaFuncSetAttribute(k_fft_y_reg<N1, N2, T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_fft_y_reg<N1, N2, T, false><<<(unsigned)nb, 32 * T, sm, s>>>(spec, Mx, Mzh, tw, inst, bucket);
+    }
+}
+
+template <int N1, int N2, int T>
+static void launch_x_reg(float2* spec, int nb, int My, int Mzh, int Mz, long long base_off, const float2* tw,
+                         const PbInst* inst, const int* bucket, cudaStream_t s)
+{
+    const size_t sm = (size_t)3 * N1 * N2 * 32 * sizeof(float2);
+    cudaFuncSetAttribute(k_fft_x_green_reg<N1, N2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const long long nblk = (long long)nb * My * ((Mzh + 31) / 32);
+    k_fft_x_green_reg<N1, N2, T><<<(unsigned)nblk, 32 * T, sm, s>>>(spec, inst, bucket, base_off, My, Mzh, Mz, tw);
+}
+
+template <int N1, int N2, int T>
+static void launch_z_reg(const float4* grid_in, float4* grid_out, float2* spec, bool inverse, long long nlines,
+                         int Mx, int My, const float2* tw, const float2* rt, const PbInst* inst, const int* bucket,
+                         cudaStream_t s)
+{
+    constexpr int LPC = 256 / T;
+    const size_t sm = (size_t)3 * N1 * N2 * LPC * sizeof(float2);
+    const unsigned nblk = (unsigned)((nlines + LPC - 1) / LPC);
+    if (inverse) {
+        cudaFuncSetAttribute(k_fft_z_inv_reg<N1, N2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_fft_z_inv_reg<N1, N2, T><<<nblk, 256, sm, s>>>(spec, grid_out, nlines, Mx, My, tw, rt, inst, bucket);
+    } else {
+        cudaFuncSetAttribute(k_fft_z_fwd_reg<N1, N2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_fft_z_fwd_reg<N1, N2, T><<<nblk, 256, sm, s>>>(grid_in, spec, nlines, Mx, My, tw, rt, inst, bucket);
+    }
+}
+
+#define PB_REG_SHAPES(X) X(4, 1, 1) X(4, 2, 2) X(4, 4, 4) X(8, 4, 4) X(8, 8, 8) X(16, 8, 8) X(16, 16, 16)
+#define PB_REG_SHAPES_Z(X) X(4, 1, 1) X(4, 2, 2) X(4, 4, 4) X(8, 4, 4) X(8, 8, 8)
+
+static void y_reg(RegShape r, float2* spec, int nvol, int Mx, int Mzh, const float2* tw, bool inverse,
+                  const PbInst* inst, const int* bucket, cudaStream_t s)
+{
+#define PB_Y(a, b, c) \
+    if (r.n1 == a && r.n2 == b && r.t == c) return launch_y_reg<a, b, c>(spec, nvol, Mx, Mzh, tw, inverse, inst, bucket, s);
+    PB_REG_SHAPES(PB_Y)
+#undef PB_Y
+}
+
+static void x_reg(RegShape r, float2* spec, int nb, int My, int Mzh, int Mz, long long base_off, const float2* tw,
+                  const PbInst* inst, const int* bucket, cudaStream_t s)
+{
+#define PB_X(a, b, c) \
+    if (r.n1 == a && r.n2 == b && r.t == c) return launch_x_reg<a, b, c>(spec, nb, My, Mzh, Mz, base_off, tw, inst, bucket, s);
+    PB_REG_SHAPES(PB_X)
+#undef PB_X
+}
+
+static void z_reg(RegShape r, const float4* gin, float4* gout, float2* spec, bool inverse, long long nlines, int Mx,
+                  int My, const float2* tw, const float2* rt, const PbInst* inst, const int* bucket, cudaStream_t s)
+{
+#define PB_Z(a, b, c) \
+    if (r.n1 == a && r.n2 == b && r.t == c) \
+        return launch_z_reg<a, b, c>(gin, gout, spec, inverse, nlines, Mx, My, tw, rt, inst, bucket, s);
+    PB_REG_SHAPES_Z(PB_Z)
+#undef PB_Z
+}
+
 static int pick_tw(int N, int mult, size_t csize, int maxbytes)
 {
     int tw = 16;
@@ -849,6 +1334,21 @@ void launch_kspace_fft(const PbInst* inst_dev, const int* bucket_inst, int nb, l
     const int Mx = M[0], My = M[1], Mz = M[2], Nh = Mz / 2, Mzh = Nh + 1;
     const int nvol = 3 * nb;
     TwOff o = tw_offsets(M);
+    if (sizeof(T) == 4) {  // register passes where every axis has one
+        const RegShape rz = reg_shape(Nh, true), ry = reg_shape(My, false), rx = reg_shape(Mx, false);
+        if (rz.n1 && ry.n1 && rx.n1) {
+            const float2* tw2 = (const float2*)tw_v;
+            float2* sp2 = (float2*)spec_v;
+            float4* g4 = (float4*)grid;
+            const long long nlines4 = (long long)nb * Mx * My;
+            z_reg(rz, g4, nullptr, sp2, false, nlines4, Mx, My, tw2 + o.zh, tw2 + o.r, inst_dev, bucket_inst, s);
+            y_reg(ry, sp2, nvol, Mx, Mzh, tw2 + o.y, false, inst_dev, bucket_inst, s);
+            x_reg(rx, sp2, nb, My, Mzh, Mz, base_off, tw2 + o.x, inst_dev, bucket_inst, s);
+            y_reg(ry, sp2, nvol, Mx, Mzh, tw2 + o.y, true, inst_dev, bucket_inst, s);
+            z_reg(rz, nullptr, g4, sp2, true, nlines4, Mx, My, tw2 + o.zh, tw2 + o.r, inst_dev, bucket_inst, s);
+            return;
+        }
+    }
     const size_t cs = sizeof(T2);
     const int smax = 64 * 1024;
     // z forward
