@@ -985,13 +985,14 @@ __global__ void __launch_bounds__(32 * T)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* ex = (float2*)smem_raw;
     const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
-    const int ntile = (Mzh + 31) >> 5;
+    const int nz = Mzh - 1;  // the z Nyquist plane is zeroed by the Green multiply: not transformed
+    const int ntile = (nz + 31) >> 5;
     const long long blk = blockIdx.x;
     const int tile = (int)(blk % ntile);
     const long long vx = blk / ntile;  // volume * Mx + x
     if (!fft_live(inst, bucket_inst, vx / Mx / 3)) return;
     const int z = tile * 32 + lane;
-    const bool ok = z < Mzh;
+    const bool ok = z < nz;
     float2* base = spec + (size_t)vx * N * Mzh + (ok ? z : 0);
     float2 A[N2 / T][N1], B[N1 / T][N2];
 #pragma unroll
@@ -1020,7 +1021,8 @@ __global__ void __launch_bounds__(32 * T)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* SP = (float2*)smem_raw;  // [3][N][32]
     const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
-    const int ntile = (Mzh + 31) >> 5;
+    const int nz = Mzh - 1;  // z' < Mz/2; the Nyquist plane z' = Mz/2 is zero after the Green multiply
+    const int ntile = (nz + 31) >> 5;
     const long long blk = blockIdx.x;
     const int tile = (int)(blk % ntile);
     const long long r = blk / ntile;
@@ -1029,9 +1031,14 @@ __global__ void __launch_bounds__(32 * T)
     if (!fft_live(inst, bucket_inst, qi)) return;
     const PbInst& I = inst[bucket_inst[qi]];
     const int z = tile * 32 + lane;
-    const bool ok = z < Mzh;
+    const bool ok = z < nz;
     const size_t vol = (size_t)N * My * Mzh, xs = (size_t)My * Mzh;
     float2* base = spec + (I.spec_off - base_off) + (size_t)y * Mzh + (ok ? z : 0);
+    if (tile == 0) {  // the Nyquist line of this (instance, y), for the inverse y and z passes
+        float2* nyq = spec + (I.spec_off - base_off) + (size_t)y * Mzh + nz;
+        for (int i = threadIdx.x; i < 3 * N; i += 32 * T)
+            nyq[(size_t)(i / N) * vol + (size_t)(i % N) * xs] = make_float2(0.f, 0.f);
+    }
     float2 A[N2 / T][N1], B[N1 / T][N2];
 #pragma unroll 1
     for (int c = 0; c < 3; c++) {
@@ -1249,7 +1256,7 @@ static void launch_y_reg(float2* spec, int nvol, int Mx, int Mzh, const float2* 
                          const int* bucket, cudaStream_t s)
 {
     const size_t sm = (size_t)N1 * N2 * 32 * sizeof(float2);
-    const long long nb = (long long)nvol * Mx * ((Mzh + 31) / 32);
+    const long long nb = (long long)nvol * Mx * ((Mzh - 1 + 31) / 32);
     if (inverse) {
         cudaFuncSetAttribute(k_fft_y_reg<N1, N2, T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_fft_y_reg<N1, N2, T, true><<<(unsigned)nb, 32 * T, sm, s>>>(spec, Mx, Mzh, tw, inst, bucket);
@@ -1265,7 +1272,7 @@ static void launch_x_reg(float2* spec, int nb, int My, int Mzh, int Mz, long lon
 {
     const size_t sm = (size_t)3 * N1 * N2 * 32 * sizeof(float2);
     cudaFuncSetAttribute(k_fft_x_green_reg<N1, N2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    const long long nblk = (long long)nb * My * ((Mzh + 31) / 32);
+    const long long nblk = (long long)nb * My * ((Mzh - 1 + 31) / 32);
     k_fft_x_green_reg<N1, N2, T><<<(unsigned)nblk, 32 * T, sm, s>>>(spec, inst, bucket, base_off, My, Mzh, Mz, tw);
 }
 
