@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
 // No FP64 division: the FP64 pipe of this GPU runs at a small fraction of
 // the FP32 rate.
 __device__ __forceinline__ void window_f32(const PbInst& I, float4 h4, float4 l4, int lane, float (*wgt)[kMaxP],
-                                           int (*idx)[kMaxP])
+                                           int (*idx)[kMaxP], int* g0out = nullptr)
 {
     int g0 = 0;
     float base = 0.f;
@@ -227,6 +227,7 @@ __device__ __forceinline__ void window_f32(const PbInst& I, float4 h4, float4 l4
         const int c = min(max((int)floor(xa * I.gih[lane]), 0), I.M[lane] - 1);
         g0 = c - I.Pa[lane] / 2 + 1;
         base = (float)fma(-(double)g0, I.gh[lane], xa);
+        if (g0out) g0out[lane] = g0;
     }
     const float inv_eta = (float)(1.0 / I.eta);
 #pragma unroll
@@ -266,6 +267,157 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
         for (int px = xs; px < Px; px += R) {
             const float wx = wgt[w][0][px];
             atomicAdd(g4 + (size_t)gidx[w][0][px] * M12 + oyz, make_float4(h0 * wx, h1 * wx, h2 * wx, 0.f));
+        }
+    }
+}
+
+// Grouped spreading: a warp takes kSpreadGroup consecutive (cell-sorted, so
+// nearby) points and adds their windows together over the box that holds
+// them all, one vector L2 atomic per box point instead of one per point and
+// window point (about half the atomics for points of one cell).  Each box
+// point sums the points' contributions in registers; per-point weights are
+// laid out along the box (zero outside the point's window), so the box loops
+// need no bounds tests.  Points of another instance, or a box wider than
+// kBoxMax along an axis, are spread one point at a time through the same loops.
+constexpr int kSpreadGroup = 4;
+constexpr int kBoxMax = 48;
+
+__global__ void __launch_bounds__(kSpreadWarps * 32)
+    k_spread_f4g(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
+                 const float4* __restrict__ pb, const float4* __restrict__ frc, float* __restrict__ grid)
+{
+    constexpr int G = kSpreadGroup;
+    __shared__ float wgt[kSpreadWarps][3][kMaxP];
+    __shared__ int gidx[kSpreadWarps][3][kMaxP];
+    __shared__ float raw[kSpreadWarps][G][3][kMaxP];
+    __shared__ float pw[kSpreadWarps][G][3][kBoxMax];
+    __shared__ int gs[kSpreadWarps][G][3];
+    __shared__ float4 fs[kSpreadWarps][G];
+    const int ntot = *ntot_p;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int ngroups = (ntot + G - 1) / G;
+    const int gi = spread_order(blockIdx.x * kSpreadWarps + w, ngroups);
+    if (gi < 0) return;
+    const int sb = gi * G, cnt = min(G, ntot - sb);
+    const int q0 = __float_as_int(pa[sb].w);
+    const PbInst& I = inst[q0];
+    bool same = true;
+    for (int p = 0; p < cnt; p++) {
+        const float4 h4 = pa[sb + p], l4 = pb[sb + p];
+        if (__float_as_int(h4.w) != q0) {
+            same = false;
+            continue;
+        }
+        window_f32(I, h4, l4, lane, wgt[w], gidx[w], gs[w][p]);
+        __syncwarp();
+        for (int i = lane; i < 3 * kMaxP; i += 32) raw[w][p][i / kMaxP][i % kMaxP] = wgt[w][i / kMaxP][i % kMaxP];
+        if (lane == 0) fs[w][p] = frc[sb + p];
+        __syncwarp();
+    }
+    const int Pa[3] = {I.Pa[0], I.Pa[1], I.Pa[2]};
+    int b0[3], B[3];
+    bool fits = same;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        int lo = 1 << 30, hi = -(1 << 30);
+        for (int p = 0; p < cnt; p++) {
+            lo = min(lo, gs[w][p][a]);
+            hi = max(hi, gs[w][p][a] + Pa[a]);
+        }
+        b0[a] = lo;
+        B[a] = hi - lo;
+        fits = fits && B[a] <= kBoxMax;
+    }
+    const size_t M12 = (size_t)I.M[1] * I.M[2];
+    const int mx = I.M[0] - 1, my = I.M[1] - 1, mz = I.M[2] - 1;
+    float4* g4 = reinterpret_cast<float4*>(grid + I.grid_off);
+    // boxes: the whole group when it fits, else each point of instance q0 alone
+    // (points of another instance go through the one-point kernel's path below)
+    const int nbox = fits ? 1 : cnt;
+    for (int bi = 0; bi < nbox; bi++) {
+        int p0 = 0, p1 = cnt;
+        int o[3] = {b0[0], b0[1], b0[2]}, L[3] = {B[0], B[1], B[2]};
+        if (!fits) {
+            p0 = bi;
+            p1 = bi + 1;
+            if (__float_as_int(pa[sb + bi].w) != q0) continue;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                o[a] = gs[w][bi][a];
+                L[a] = Pa[a];
+            }
+        }
+        __syncwarp();
+        for (int i = lane; i < G * 3 * kBoxMax; i += 32) {
+            const int p = i / (3 * kBoxMax), r = i - p * 3 * kBoxMax, a = r / kBoxMax, x = r - a * kBoxMax;
+            float v = 0.f;
+            if (p >= p0 && p < p1) {
+                const int k = o[a] + x - gs[w][p][a];
+                if (x < L[a] && k >= 0 && k < Pa[a]) v = raw[w][p][a][k];
+            }
+            pw[w][p][a][x] = v;
+        }
+        __syncwarp();
+        float fx[G], fy[G], fz[G];
+#pragma unroll
+        for (int p = 0; p < G; p++) {
+            const float4 f = fs[w][p];
+            const bool in = p >= p0 && p < p1;
+            fx[p] = in ? f.x : 0.f;
+            fy[p] = in ? f.y : 0.f;
+            fz[p] = in ? f.z : 0.f;
+        }
+        const int Byz = L[1] * L[2];
+        for (int yz = lane; yz < Byz; yz += 32) {
+            const int y = yz / L[2], z = yz - y * L[2];
+            float c0[G], c1[G], c2[G];
+            bool any = false;
+#pragma unroll
+            for (int p = 0; p < G; p++) {
+                const float wyz = pw[w][p][1][y] * pw[w][p][2][z];
+                any = any || wyz != 0.f;
+                c0[p] = fx[p] * wyz;
+                c1[p] = fy[p] * wyz;
+                c2[p] = fz[p] * wyz;
+            }
+            if (!any) continue;
+            const size_t oyz = (size_t)((o[1] + y) & my) * I.M[2] + ((o[2] + z) & mz);
+            for (int x = 0; x < L[0]; x++) {
+                float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+#pragma unroll
+                for (int p = 0; p < G; p++) {
+                    const float wx = pw[w][p][0][x];
+                    v0 = fmaf(c0[p], wx, v0);
+                    v1 = fmaf(c1[p], wx, v1);
+                    v2 = fmaf(c2[p], wx, v2);
+                }
+                if (v0 != 0.f || v1 != 0.f || v2 != 0.f)
+                    atomicAdd(g4 + (size_t)((o[0] + x) & mx) * M12 + oyz, make_float4(v0, v1, v2, 0.f));
+            }
+        }
+    }
+    if (same) return;
+    // points of other instances than the group's first: one at a time
+    for (int p = 1; p < cnt; p++) {
+        const float4 h4 = pa[sb + p], l4 = pb[sb + p], fv = frc[sb + p];
+        const int qp = __float_as_int(h4.w);
+        if (qp == q0) continue;
+        const PbInst& J = inst[qp];
+        __syncwarp();
+        window_f32(J, h4, l4, lane, wgt[w], gidx[w]);
+        __syncwarp();
+        const int Px = J.Pa[0], Py = J.Pa[1], Pz = J.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
+        const size_t JM12 = (size_t)J.M[1] * J.M[2];
+        float4* j4 = reinterpret_cast<float4*>(grid + J.grid_off);
+        for (int id = lane; id < P2 * R; id += 32) {
+            const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
+            const float wyz = wgt[w][1][py] * wgt[w][2][pz];
+            const float h0 = fv.x * wyz, h1 = fv.y * wyz, h2 = fv.z * wyz;
+            const size_t oyz = (size_t)gidx[w][1][py] * J.M[2] + gidx[w][2][pz];
+            for (int px = xs; px < Px; px += R) {
+                const float wx = wgt[w][0][px];
+                atomicAdd(j4 + (size_t)gidx[w][0][px] * JM12 + oyz, make_float4(h0 * wx, h1 * wx, h2 * wx, 0.f));
+            }
         }
     }
 }
@@ -344,9 +496,11 @@ void launch_spread(const PbInst* inst, int ninst, const int* src_offsets, int nc
     if (ncap <= 0) return;
     int blocks = (ncap + 63 + kSpreadWarps - 1) / kSpreadWarps;  // spread_order covers up to 64 R >= ntot
     const int* ntot = src_offsets + ninst;
-    if (sizeof(T) == 4)
-        k_spread_f4<<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const float4*)pos_a, (const float4*)pos_b,
-                                                         (const float4*)frc, (float*)grid);
+    if (sizeof(T) == 4) {
+        const int ng = (ncap + kSpreadGroup - 1) / kSpreadGroup;
+        k_spread_f4g<<<(ng + 63 + kSpreadWarps - 1) / kSpreadWarps, kSpreadWarps * 32, 0, s>>>(
+            inst, ntot, (const float4*)pos_a, (const float4*)pos_b, (const float4*)frc, (float*)grid);
+    }
     else
         k_spread<T, Dbl4, Dbl4><<<blocks, kSpreadWarps * 32, 0, s>>>(
             inst, ntot, (const Dbl4*)pos_a, (const Dbl4*)pos_b, (const Dbl4*)frc, grid);
