@@ -242,35 +242,6 @@ __device__ __forceinline__ void window_f32(const PbInst& I, float4 h4, float4 l4
     }
 }
 
-__global__ void __launch_bounds__(kSpreadWarps * 32)
-    k_spread_f4(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
-                const float4* __restrict__ pb, const float4* __restrict__ frc, float* __restrict__ grid)
-{
-    __shared__ float wgt[kSpreadWarps][3][kMaxP];
-    __shared__ int gidx[kSpreadWarps][3][kMaxP];
-    const int ntot = *ntot_p;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int s = spread_order(blockIdx.x * kSpreadWarps + w, ntot);
-    if (s < 0) return;
-    const float4 h4 = pa[s], l4 = pb[s], fv = frc[s];
-    const PbInst& I = inst[__float_as_int(h4.w)];
-    window_f32(I, h4, l4, lane, wgt[w], gidx[w]);
-    __syncwarp();
-    const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
-    const size_t M12 = (size_t)I.M[1] * I.M[2];
-    float4* g4 = reinterpret_cast<float4*>(grid + I.grid_off);
-    for (int id = lane; id < P2 * R; id += 32) {
-        const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
-        const float wyz = wgt[w][1][py] * wgt[w][2][pz];
-        const float h0 = fv.x * wyz, h1 = fv.y * wyz, h2 = fv.z * wyz;
-        const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
-        for (int px = xs; px < Px; px += R) {
-            const float wx = wgt[w][0][px];
-            atomicAdd(g4 + (size_t)gidx[w][0][px] * M12 + oyz, make_float4(h0 * wx, h1 * wx, h2 * wx, 0.f));
-        }
-    }
-}
-
 // Grouped spreading: a warp takes kSpreadGroup consecutive (cell-sorted, so
 // nearby) points and adds their windows together over the box that holds
 // them all, one vector L2 atomic per box point instead of one per point and
@@ -280,6 +251,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
 // need no bounds tests.  Points of another instance, or a box wider than
 // kBoxMax along an axis, are spread one point at a time through the same loops.
 constexpr int kSpreadGroup = 4;
+constexpr int kGatherGroup = 1;  // measured: 1 -> 0.22 ms, 2 -> 0.26, 3 -> 0.29, 4 -> 0.32 at N = 1e5
 constexpr int kBoxMax = 48;
 
 __global__ void __launch_bounds__(kSpreadWarps * 32)
@@ -422,19 +394,11 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     }
 }
 
-__global__ void __launch_bounds__(kSpreadWarps * 32)
-    k_gather_f4(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
-                const float4* __restrict__ pb, const float* __restrict__ grid, float* __restrict__ u_k)
+// One target's window sum (the whole warp), written to out[0..2] by lane 0.
+__device__ __forceinline__ void gather_point(const PbInst& I, float4 h4, float4 l4, int lane, float (*wgt)[kMaxP],
+                                             int (*gidx)[kMaxP], const float* __restrict__ grid, float* out)
 {
-    __shared__ float wgt[kSpreadWarps][3][kMaxP];
-    __shared__ int gidx[kSpreadWarps][3][kMaxP];
-    const int ntot = *ntot_p;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int s = blockIdx.x * kSpreadWarps + w;
-    if (s >= ntot) return;
-    const float4 h4 = pa[s], l4 = pb[s];
-    const PbInst& I = inst[__float_as_int(h4.w)];
-    window_f32(I, h4, l4, lane, wgt[w], gidx[w]);
+    window_f32(I, h4, l4, lane, wgt, gidx);
     __syncwarp();
     const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
     const size_t M12 = (size_t)I.M[1] * I.M[2];
@@ -445,30 +409,18 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     for (int id = lane; id < P2 * R; id += 32) {
         const int xs = (int)(((unsigned)id * inv_p2) >> 20), yz = id - xs * P2;
         const int py = (int)(((unsigned)yz * inv_pz) >> 20), pz = yz - py * Pz;
-        const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
-        // one x row of the window in plain FP32 (<= 32 same-sign-weighted terms), rows Kahan-summed;
-        // the first 16 points of the row are loaded together (predicated), so that many loads
-        // are in flight at once
+        const size_t oyz = (size_t)gidx[1][py] * I.M[2] + gidx[2][pz];
+        // one x row of the window in plain FP32 (<= 32 same-sign-weighted terms), rows Kahan-summed
         float r0 = 0, r1 = 0, r2 = 0;
-#pragma unroll
-        for (int k = 0; k < 16; k++) {
-            const int px = xs + k * R;
-            if (px < Px) {
-                const float wx = wgt[w][0][px];
-                const float4 v = __ldg(g4 + (size_t)gidx[w][0][px] * M12 + oyz);
-                r0 = fmaf(wx, v.x, r0);
-                r1 = fmaf(wx, v.y, r1);
-                r2 = fmaf(wx, v.z, r2);
-            }
-        }
-        for (int px = xs + 16 * R; px < Px; px += R) {
-            const float wx = wgt[w][0][px];
-            const float4 v = __ldg(g4 + (size_t)gidx[w][0][px] * M12 + oyz);
+#pragma unroll 4
+        for (int px = xs; px < Px; px += R) {
+            const float wx = wgt[0][px];
+            const float4 v = __ldg(g4 + (size_t)gidx[0][px] * M12 + oyz);
             r0 = fmaf(wx, v.x, r0);
             r1 = fmaf(wx, v.y, r1);
             r2 = fmaf(wx, v.z, r2);
         }
-        const float wyz = wgt[w][1][py] * wgt[w][2][pz];
+        const float wyz = wgt[1][py] * wgt[2][pz];
         kahan_add(s0, c0, wyz * r0);
         kahan_add(s1, c1, wyz * r1);
         kahan_add(s2, c2, wyz * r2);
@@ -483,10 +435,127 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
         s2 += __shfl_xor_sync(kFull, s2, o);
     }
     if (lane == 0) {
-        u_k[3 * (size_t)s] = s0;
-        u_k[3 * (size_t)s + 1] = s1;
-        u_k[3 * (size_t)s + 2] = s2;
+        out[0] = s0;
+        out[1] = s1;
+        out[2] = s2;
     }
+}
+
+// Gathering over boxes: a warp takes kGatherGroup consecutive (nearby)
+// targets and reads each point of their common box once, accumulating every
+// target's weighted sum from it.  With one target per warp (the measured
+// best: more targets per warp cost registers and occupancy) the box is the
+// window, walked with per-axis weights laid out along it (no index tables,
+// no divisions in the loops).  Targets of another instance, or a box wider
+// than kBoxMax, are gathered one at a time.
+__global__ void __launch_bounds__(kSpreadWarps * 32)
+    k_gather_f4g(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
+                 const float4* __restrict__ pb, const float* __restrict__ grid, float* __restrict__ u_k)
+{
+    constexpr int G = kGatherGroup;
+    __shared__ float wgt[kSpreadWarps][3][kMaxP];
+    __shared__ int gidx[kSpreadWarps][3][kMaxP];
+    __shared__ float raw[kSpreadWarps][G][3][kMaxP];
+    __shared__ float pw[kSpreadWarps][G][3][kBoxMax];
+    __shared__ int gs[kSpreadWarps][G][3];
+    const int ntot = *ntot_p;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int sb = (blockIdx.x * kSpreadWarps + w) * G;
+    if (sb >= ntot) return;
+    const int cnt = min(G, ntot - sb);
+    const int q0 = __float_as_int(pa[sb].w);
+    const PbInst& I = inst[q0];
+    bool same = true;
+    for (int p = 0; p < cnt; p++) same = same && __float_as_int(pa[sb + p].w) == q0;
+    int b0[3] = {0, 0, 0}, B[3] = {0, 0, 0};
+    bool fits = same;
+    if (same) {
+        for (int p = 0; p < cnt; p++) {
+            window_f32(I, pa[sb + p], pb[sb + p], lane, wgt[w], gidx[w], gs[w][p]);
+            __syncwarp();
+            for (int i = lane; i < 3 * kMaxP; i += 32) raw[w][p][i / kMaxP][i % kMaxP] = wgt[w][i / kMaxP][i % kMaxP];
+            __syncwarp();
+        }
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            int lo = 1 << 30, hi = -(1 << 30);
+            for (int p = 0; p < cnt; p++) {
+                lo = min(lo, gs[w][p][a]);
+                hi = max(hi, gs[w][p][a] + I.Pa[a]);
+            }
+            b0[a] = lo;
+            B[a] = hi - lo;
+            fits = fits && B[a] <= kBoxMax;
+        }
+    }
+    if (!fits) {
+        for (int p = 0; p < cnt; p++) {
+            const float4 h4 = pa[sb + p];
+            __syncwarp();
+            gather_point(inst[__float_as_int(h4.w)], h4, pb[sb + p], lane, wgt[w], gidx[w], grid,
+                         u_k + 3 * (size_t)(sb + p));
+        }
+        return;
+    }
+    for (int i = lane; i < G * 3 * kBoxMax; i += 32) {
+        const int p = i / (3 * kBoxMax), r = i - p * 3 * kBoxMax, a = r / kBoxMax, x = r - a * kBoxMax;
+        float v = 0.f;
+        if (p < cnt) {
+            const int k = b0[a] + x - gs[w][p][a];
+            if (x < B[a] && k >= 0 && k < I.Pa[a]) v = raw[w][p][a][k];
+        }
+        pw[w][p][a][x] = v;
+    }
+    __syncwarp();
+    const size_t M12 = (size_t)I.M[1] * I.M[2];
+    const int mx = I.M[0] - 1, my = I.M[1] - 1, mz = I.M[2] - 1;
+    const float4* g4 = reinterpret_cast<const float4*>(grid + I.grid_off);
+    float s[G][3], c[G][3];
+#pragma unroll
+    for (int p = 0; p < G; p++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) s[p][k] = c[p][k] = 0.f;
+    const int Byz = B[1] * B[2];
+    for (int yz = lane; yz < Byz; yz += 32) {
+        const int y = yz / B[2], z = yz - y * B[2];
+        float wyz[G];
+        bool any = false;
+#pragma unroll
+        for (int p = 0; p < G; p++) {
+            wyz[p] = pw[w][p][1][y] * pw[w][p][2][z];
+            any = any || wyz[p] != 0.f;
+        }
+        if (!any) continue;
+        const size_t oyz = (size_t)((b0[1] + y) & my) * I.M[2] + ((b0[2] + z) & mz);
+        // rows in plain FP32 (<= kBoxMax same-sign-weighted terms), rows Kahan-summed
+        float r[G][3];
+#pragma unroll
+        for (int p = 0; p < G; p++) r[p][0] = r[p][1] = r[p][2] = 0.f;
+#pragma unroll 4
+        for (int x = 0; x < B[0]; x++) {
+            const float4 v = __ldg(g4 + (size_t)((b0[0] + x) & mx) * M12 + oyz);
+#pragma unroll
+            for (int p = 0; p < G; p++) {
+                const float wx = pw[w][p][0][x];
+                r[p][0] = fmaf(wx, v.x, r[p][0]);
+                r[p][1] = fmaf(wx, v.y, r[p][1]);
+                r[p][2] = fmaf(wx, v.z, r[p][2]);
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < G; p++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) kahan_add(s[p][k], c[p][k], wyz[p] * r[p][k]);
+    }
+#pragma unroll
+    for (int p = 0; p < G; p++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            float v = s[p][k] - c[p][k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+            if (lane == 0 && p < cnt) u_k[3 * (size_t)(sb + p) + k] = v;
+        }
 }
 
 template <class T>
@@ -514,8 +583,9 @@ void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int nc
     int blocks = (ncap + kSpreadWarps - 1) / kSpreadWarps;
     const int* ntot = tgt_offsets + ninst;
     if (sizeof(T) == 4)
-        k_gather_f4<<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const float4*)pos_a, (const float4*)pos_b,
-                                                         (const float*)grid, (float*)u_k);
+        k_gather_f4g<<<(ncap + kSpreadWarps * kGatherGroup - 1) / (kSpreadWarps * kGatherGroup), kSpreadWarps * 32, 0,
+                       s>>>(inst, ntot, (const float4*)pos_a, (const float4*)pos_b, (const float*)grid,
+                            (float*)u_k);
     else
         k_gather<T, Dbl4><<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const Dbl4*)pos_a,
                                                                     (const Dbl4*)pos_b, grid, u_k);
@@ -1101,30 +1171,30 @@ __device__ __forceinline__ void line_fft(float2 (&A)[N2 / T][N1], float2 (&B)[N1
             for (int k1 = 1; k1 < N1; k1++) A[a][k1] = twN_mul<INV>(A[a][k1], n2 * k1, N, tw);
         }
     }
-    if (N2 == 1) {
+    if constexpr (N2 == 1) {
 #pragma unroll
         for (int b = 0; b < N1 / T; b++) B[b][0] = A[0][b];
-        return;
-    }
+    } else {
 #pragma unroll
-    for (int a = 0; a < N2 / T; a++) {
-        const int n2 = t + T * a;
+        for (int a = 0; a < N2 / T; a++) {
+            const int n2 = t + T * a;
 #pragma unroll
-        for (int k1 = 0; k1 < N1; k1++) {
-            const int e = n2 * N1 + k1;
-            ex[ZSW ? zslot<T, N1>(e, ll, LS) : e * LS] = A[a][k1];
+            for (int k1 = 0; k1 < N1; k1++) {
+                const int e = n2 * N1 + k1;
+                ex[ZSW ? zslot<T, N1>(e, ll, LS) : e * LS] = A[a][k1];
+            }
         }
-    }
-    __syncthreads();
+        __syncthreads();
 #pragma unroll
-    for (int b = 0; b < N1 / T; b++) {
-        const int k1 = t + T * b;
+        for (int b = 0; b < N1 / T; b++) {
+            const int k1 = t + T * b;
 #pragma unroll
-        for (int n2 = 0; n2 < N2; n2++) {
-            const int e = n2 * N1 + k1;
-            B[b][n2] = ex[ZSW ? zslot<T, N1>(e, ll, LS) : e * LS];
+            for (int n2 = 0; n2 < N2; n2++) {
+                const int e = n2 * N1 + k1;
+                B[b][n2] = ex[ZSW ? zslot<T, N1>(e, ll, LS) : e * LS];
+            }
+            fft_reg<N2, INV>(B[b]);
         }
-        fft_reg<N2, INV>(B[b]);
     }
 }
 
