@@ -70,6 +70,10 @@ struct CostModel {
 // Per-unit device times measured on a GB300 (N = 1e5, 128^3, P = 12): mixed
 // precision 0.65 ms / 42e6 pairs, 0.26 ms per 128^3 FFT round trip of three
 // components, 0.79 ms / (2e5 x 1728) window points spread plus gathered.
+// (The kernels have since become faster: 0.50 ms, 0.093 ms and 0.53 ms.  A
+// model refitted to those figures picks finer grids for the serving stream
+// and served 4% fewer solves/s with a higher p99, since grid clears, launch
+// overhead and batching are not in it; the earlier constants are kept.)
 CostModel cost_model(int prec)
 {
     if (prec == PB_PREC_MIXED) return {1.5e-11, 1.2e-10, 2.3e-12};

@@ -1469,7 +1469,7 @@ static RegShape reg_shape(int N, bool z)
         case 16: return {4, 4, 4};
         case 32: return {8, 4, 4};
         case 64: return {8, 8, 8};
-        case 128: return z ? RegShape{0, 0, 0} : RegShape{16, 8, 8};
+        case 128: return RegShape{16, 8, 8};
         case 256: return z ? RegShape{0, 0, 0} : RegShape{16, 16, 16};
         default: return {0, 0, 0};
     }
@@ -1518,7 +1518,7 @@ static void launch_z_reg(const float4* grid_in, float4* grid_out, float2* spec, 
 }
 
 #define PB_REG_SHAPES(X) X(4, 1, 1) X(4, 2, 2) X(4, 4, 4) X(8, 4, 4) X(8, 8, 8) X(16, 8, 8) X(16, 16, 16)
-#define PB_REG_SHAPES_Z(X) X(4, 1, 1) X(4, 2, 2) X(4, 4, 4) X(8, 4, 4) X(8, 8, 8)
+#define PB_REG_SHAPES_Z(X) X(4, 1, 1) X(4, 2, 2) X(4, 4, 4) X(8, 4, 4) X(8, 8, 8) X(16, 8, 8)
 
 static void y_reg(RegShape r, float2* spec, int nvol, int Mx, int Mzh, const float2* tw, bool inverse,
                   const PbInst* inst, const int* bucket, cudaStream_t s)

@@ -165,6 +165,24 @@ def test_config1_parameters_error_reported():
     assert oracle.rel_errors(umx, u64)[0] < 1e-6
 
 
+@pytest.mark.parametrize("M,L,d,rc,P", [(8, 1.0, 0.25, 0.45, 4), (16, 1.0, 0.15, 0.4, 6), (32, 1.0, 0.1, 0.3, 8),
+                                        (128, 1.0, 0.03, 0.11, 10), (256, 1.0, 0.02, 0.075, 12),
+                                        ((32, 64, 16), (1.0, 2.0, 0.5), 0.08, 0.25, 8)])
+def test_mixed_matches_fp64_on_every_fft_length(M, L, d, rc, P):
+    """The FP32 k-space path (register FFT passes for lines of 4..256 points,
+    anisotropic grids included) agrees with the FP64 path on the same
+    splitting, cutoff, grid and support."""
+    Ls = L if isinstance(L, tuple) else (L, L, L)
+    Ms = M if isinstance(M, tuple) else (M, M, M)
+    rng = np.random.default_rng(sum(Ms))
+    x = rng.random((400, 3)) * np.array(Ls)
+    f = rng.standard_normal((400, 3))
+    kw = dict(d=d, rc=rc, M=Ms, P=P, tol=1e-6)
+    u64 = pb.solve(cuda(x), cuda(f), L, 10.0, 0.01, precision="fp64", **kw).cpu().numpy()
+    umx = pb.solve(cuda(x), cuda(f), L, 10.0, 0.01, precision="mixed", **kw).cpu().numpy()
+    assert np.abs(umx - u64).max() <= 2e-6 * np.abs(u64).max()
+
+
 def test_empty_and_invalid():
     x, f, _ = _case(10, 1.0, 18)
     with pytest.raises(pb.PbError):
