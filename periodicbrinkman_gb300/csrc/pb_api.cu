@@ -158,7 +158,10 @@ int resolve(const pb_solve_params& p, Resolved& R)
     R.n_tgt = R.same ? p.n_src : p.n_tgt;
     // error budgets aim at tol/2 so that the sum of the parts stays below tol
     const double kconst = std::log(20.0 / tol);      // k-space truncation exponent
-    const double ealias = std::log(2.0 / tol) + 1.0; // aliasing exponent
+    // aliasing exponent; measured as the cutoff margin below: an offset of +1
+    // gives 2.4e-7 (tol 1e-6) and 1.5e-5 (tol 1e-4) on the serving stream, 0
+    // gives 2.9e-7 and 3.4e-5, -1 gives 2.5e-6 (above tol)
+    const double ealias = std::log(2.0 / tol);
     const double etrunc = std::max(4.0, ealias - 3.0);
     // rc = zeta d.  Measured on the serving stream and the N = 1e5 solve (max
     // relative error of sampled requests against the FP64 oracle): an offset
