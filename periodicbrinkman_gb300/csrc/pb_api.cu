@@ -529,11 +529,11 @@ int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved&
 // Real-space work items per row item (csplit) of the first `count` instances.
 // A row item of a small instance carries a long candidate loop; splitting its
 // stencil columns into groups gives the GPU enough items to stay busy and
-// evens out the end of the dynamic item schedule.  The target is about 38912
-// items' worth of equal work (sixteen per resident warp of a GB300: with two
-// per warp, warps that draw a second item finish well after the rest; at
-// N = 1e5 the real-space sum takes 0.54 ms instead of 0.74 ms), bounded by the
-// stencil columns and by the item array's capacity.
+// evens out the end of the dynamic item schedule.  The target is about 12160
+// items' worth of equal work (five per resident warp of a GB300), bounded by
+// the stencil columns and by the item array's capacity.  Measured on the
+// N = 1e5 solve (real-space sum): 4864 items 0.40 ms, 7296 0.35, 12160 0.345,
+// 19456 0.36, 38912 0.38 ms.
 void assign_splits(pb_plan_s* P, int count)
 {
     double W = 0;
@@ -545,7 +545,7 @@ void assign_splits(pb_plan_s* P, int count)
         const Resolved& R = P->res[q];
         const int ncol = (2 * R.S[0] + 1) * (2 * R.S[1] + 1);
         const double per_item = 24.0 * std::max(1.0, (double)R.pairs_est) / std::max(1, R.n_tgt);
-        long long g = std::llround(per_item * 38912.0 / W);
+        long long g = std::llround(per_item * 12160.0 / W);
         G[q] = (int)std::max(1LL, std::min<long long>(g, std::min(ncol, 255)));
         // items of an instance <= min(targets, cells + targets/32 + 1) row items
         const long long nc = (long long)R.nc[0] * R.nc[1] * R.nc[2];
