@@ -302,24 +302,52 @@ __device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q,
     nitems = k;
 }
 
-// Row items of every row start cell (persistent over the actual cells); each
-// row reserves its range of the item array with one atomic.
-__global__ void k_build_items(const int* __restrict__ start, const int* __restrict__ cell_offsets,
-                              const PbInst* __restrict__ inst, int ninst, int4* __restrict__ items, int cap,
-                              int* __restrict__ nitems)
+// Row items of every row start cell: a warp looks at 32 cells at a time, and
+// for each row start among them stages the row's cell starts in shared memory
+// (coalesced) and lets one lane walk the row there (the walk's dependent
+// loads then cost shared-memory latency); each row reserves its range of the
+// item array with one atomic.
+constexpr int kItemWarps = 8;
+
+__global__ void __launch_bounds__(kItemWarps * 32)
+    k_build_items(const int* __restrict__ start, const int* __restrict__ cell_offsets,
+                  const PbInst* __restrict__ inst, int ninst, int4* __restrict__ items, int cap,
+                  int* __restrict__ nitems)
 {
+    __shared__ int st[kItemWarps][129];  // nc[2] <= 128
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int ncell = cell_offsets[ninst];
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
-        const int q = find_instance(cell_offsets, ninst, c);
-        const PbInst& I = inst[q];
-        const int local = c - I.cell_off;
-        if (local >= I.ncell || local % I.nc[2] != 0) continue;
-        const int G = max(1, I.csplit);
-        int n = 0;
-        walk_row<false>(start, c, I.nc[2], q, local / I.nc[2], G, nullptr, 0, 0, n);
-        if (n == 0) continue;
-        const int k0 = atomicAdd(nitems, n);
-        walk_row<true>(start, c, I.nc[2], q, local / I.nc[2], G, items, k0, cap, n);
+    const int nwarps = gridDim.x * kItemWarps;
+    for (int cb = (blockIdx.x * kItemWarps + w) * 32; cb < ncell; cb += nwarps * 32) {
+        const int c = cb + lane;
+        int q = 0, local = 0;
+        bool rs = false;
+        if (c < ncell) {
+            q = find_instance(cell_offsets, ninst, c);
+            local = c - inst[q].cell_off;
+            rs = local < inst[q].ncell && local % inst[q].nc[2] == 0;
+        }
+        unsigned m = __ballot_sync(kFull, rs);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const int rc = __shfl_sync(kFull, c, src), rq = __shfl_sync(kFull, q, src),
+                      rl = __shfl_sync(kFull, local, src);
+            const PbInst& I = inst[rq];
+            const int nz = I.nc[2];
+            __syncwarp();
+            for (int z = lane; z <= nz; z += 32) st[w][z] = start[rc + z];
+            __syncwarp();
+            if (lane == 0) {
+                const int G = max(1, I.csplit);
+                int n = 0;
+                walk_row<false>(st[w], 0, nz, rq, rl / nz, G, nullptr, 0, 0, n);
+                if (n > 0) {
+                    const int k0 = atomicAdd(nitems, n);
+                    walk_row<true>(st[w], 0, nz, rq, rl / nz, G, items, k0, cap, n);
+                }
+            }
+        }
     }
 }
 
@@ -328,9 +356,9 @@ void launch_build_items(const int* start, int ncell_cap, const int* cell_offsets
 {
     cudaMemsetAsync(nitems, 0, sizeof(int), s);
     if (ncell_cap <= 0) return;
-    long long blocks = ((long long)ncell_cap + 255) / 256;
+    long long blocks = ((long long)ncell_cap + 32 * kItemWarps - 1) / (32 * kItemWarps);
     if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
-    k_build_items<<<(int)blocks, 256, 0, s>>>(start, cell_offsets, inst, ninst, items, cap, nitems);
+    k_build_items<<<(int)blocks, kItemWarps * 32, 0, s>>>(start, cell_offsets, inst, ninst, items, cap, nitems);
 }
 
 }  // namespace pb
