@@ -326,44 +326,78 @@ __device__ __forceinline__ void stream_segments(RealWarpSmem& S, const PbInst& I
     }
     __syncwarp();
     const int self_shift = I.same ? I.tgt_off - I.src_off - F.first : 0;
-    for (int base = 0; base < total; base += 32) {
-        const int ncand = min(32, total - base);
-        if (lane < ncand) {
-            const int p = base + lane;
-            int lo = 0, hi = nseg - 1;  // the last segment starting at or before p
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (S.sg_pre[mid] <= p)
-                    lo = mid;
-                else
-                    hi = mid - 1;
+    const unsigned lt = (1u << lane) - 1u;
+    const float keep2 = K.rc2 * 1.0001f;
+    // Chunks of 32 sources that lie within rc of the targets' box: candidates
+    // are fetched 32 at a time and the others (about 30% of a column's cells)
+    // are dropped before any pair is tested.
+    int pos = 0;
+    while (pos < total) {
+        int fill = 0;
+        while (fill < 32 && pos < total) {
+            const int p = pos + lane;
+            // segment of candidate p without a search: the segment holding `pos`
+            // plus the segment starts in (pos, p] (at most 64 segments, two per lane)
+            int seg;
+            {
+                const int ka = lane, kb = lane + 32;
+                const int pa = ka < nseg ? S.sg_pre[ka] : 0x7fffffff, pb = kb < nseg ? S.sg_pre[kb] : 0x7fffffff;
+                const int k0 = __popc(__ballot_sync(kFull, pa <= pos)) + __popc(__ballot_sync(kFull, pb <= pos)) - 1;
+                const unsigned bits = (pa > pos && pa - pos < 32 ? 1u << (pa - pos) : 0u) |
+                                      (pb > pos && pb - pos < 32 ? 1u << (pb - pos) : 0u);
+                const unsigned starts = __reduce_or_sync(kFull, bits);
+                seg = k0 + __popc(starts & ((2u << lane) - 2u));
             }
-            const int j = S.sg_b[lo] + (p - S.sg_pre[lo]);
-            const int meta = S.sg_meta[lo];
-            const int i0 = meta & 31, i1 = (meta >> 5) & 31, i2 = meta >> 10;
-            const float2 qx = S.ft.qx[i0], qy = S.ft.qy[i1], qz = S.ft.qz[i2];
-            const float qh[3] = {qx.x, qy.x, qz.x}, ql[3] = {qx.y, qy.y, qz.y};
-            const float4 ph = spos_hi[j], pl = spos_lo[j];
-            const float xh[3] = {ph.x, ph.y, ph.z}, xl[3] = {pl.x, pl.y, pl.z};
-            float p3[3], l3[3];
+            bool keep = false, zs = false;
+            int j = 0;
+            float p3[3] = {0.f, 0.f, 0.f}, l3[3] = {0.f, 0.f, 0.f};
+            float4 fj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (p < total) {
+                j = S.sg_b[seg] + (p - S.sg_pre[seg]);
+                const int meta = S.sg_meta[seg];
+                const int i0 = meta & 31, i1 = (meta >> 5) & 31, i2 = meta >> 10;
+                const float2 qx = S.ft.qx[i0], qy = S.ft.qy[i1], qz = S.ft.qz[i2];
+                const float qh[3] = {qx.x, qy.x, qz.x}, ql[3] = {qx.y, qy.y, qz.y};
+                const float4 ph = spos_hi[j], pl = spos_lo[j];
+                fj = sfrc[j];  // loaded with the position (not after the test): one round of latency
+                const float xh[3] = {ph.x, ph.y, ph.z}, xl[3] = {pl.x, pl.y, pl.z};
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                float s, er;
-                two_sum(xh[a], -qh[a], s, er);
-                p3[a] = s;
-                l3[a] = er + (xl[a] - ql[a]);
+                for (int a = 0; a < 3; a++) {
+                    float sv, er;
+                    two_sum(xh[a], -qh[a], sv, er);
+                    p3[a] = sv;
+                    l3[a] = er + (xl[a] - ql[a]);
+                }
+                float d2 = 0.f;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    const float da = fmaxf(0.f, fmaxf(S.box[a] - p3[a], p3[a] - S.box[3 + a]));
+                    d2 = fmaf(da, da, d2);
+                }
+                keep = d2 < keep2;
+                zs = I.same && S.ft.zx[i0] && S.ft.zy[i1] && S.ft.zz[i2];
             }
-            S.s_hi[lane] = make_float4(p3[0], p3[1], p3[2], 0.f);
-            S.s_lo[lane] = make_float4(l3[0], l3[1], l3[2], 0.f);
-            S.s_f[lane] = sfrc[j];
-            S.c_x[lane] = p3[0];
-            S.c_y[lane] = p3[1];
-            S.c_z[lane] = p3[2];
-            if (I.same && S.ft.zx[i0] && S.ft.zy[i1] && S.ft.zz[i2]) {  // a target's own source (added by the combine kernel)
-                const int ts = j + self_shift;
-                if (ts >= 0 && ts < F.count) S.selfm[ts] = 1u << lane;
+            const unsigned bal = __ballot_sync(kFull, keep);
+            const int need = 32 - fill, k = __popc(bal), rank = __popc(bal & lt);
+            int adv = min(32, total - pos);
+            if (k > need) adv = __ffs(__ballot_sync(kFull, keep && rank == need - 1));  // through the last one taken
+            if (keep && rank < need) {
+                const int slot = fill + rank;
+                S.s_hi[slot] = make_float4(p3[0], p3[1], p3[2], 0.f);
+                S.s_lo[slot] = make_float4(l3[0], l3[1], l3[2], 0.f);
+                S.s_f[slot] = fj;
+                S.c_x[slot] = p3[0];
+                S.c_y[slot] = p3[1];
+                S.c_z[slot] = p3[2];
+                if (zs) {  // a target's own source (added by the combine kernel)
+                    const int ts = j + self_shift;
+                    if (ts >= 0 && ts < F.count) S.selfm[ts] = 1u << slot;
+                }
             }
-        } else {  // padding: far from every target, active (finite) or not (+3e30)
+            fill += min(k, need);
+            pos += adv;
+        }
+        if (lane >= fill) {  // padding: far from every target, active (finite) or not (+3e30)
             S.c_x[lane] = -3.0e30f;
             S.c_y[lane] = -3.0e30f;
             S.c_z[lane] = -3.0e30f;
