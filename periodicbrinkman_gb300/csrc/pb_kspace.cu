@@ -254,7 +254,9 @@ constexpr int kSpreadGroup = 3;  // measured at N = 1e5: 2 -> 0.35 ms, 3 -> 0.31
 constexpr int kGatherGroup = 1;  // measured: 1 -> 0.22 ms, 2 -> 0.26, 3 -> 0.29, 4 -> 0.32 at N = 1e5
 constexpr int kBoxMax = 48;
 
-__global__ void __launch_bounds__(kSpreadWarps * 32)
+// 4 blocks per SM (64 registers, a few spilled): measured 0.286 ms vs 0.300 at
+// 3 blocks (80 registers) and 0.294 / 0.332 at 5 / 6 blocks (N = 1e5)
+__global__ void __launch_bounds__(kSpreadWarps * 32, 4)
     k_spread_f4g(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
                  const float4* __restrict__ pb, const float4* __restrict__ frc, float* __restrict__ grid)
 {
