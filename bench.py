@@ -50,6 +50,8 @@ SERVE = dict(name="serve_stream_20000req_2000per_s_N1e3-2e5_targets_N/2_alpha1-5
              nreq=20000, rate=2000.0, nmin=1000, nmax=200000, seed=5000, budget=150 << 30)
 SINGLE = dict(name="single_solve_N1e5_uniform_alpha20_eps0.005_grid128_P12_tol1e-6_mixed", n=100_000, L=1.0,
               alpha=20.0, eps=0.005, M=128, P=12, tol=1e-6, seed=2000)
+CLUSTERED = dict(name="clustered_N1e6_200clusters_sigma0.02_L2_alpha5_eps0.002_grid256_tol1e-6_mixed", n=1_000_000,
+                 L=2.0, alpha=5.0, eps=0.002, M=256, P=0, tol=1e-6, ncl=200, sigma=0.02, seed=3000)
 METRIC = "Brinkman solves/s + p50/p99 latency at <=1e-6 rel err, served vs plain FP64"
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_real_mixed launch of the N = 1e5 solve
 REAL_DRAM_BYTES = 8.06e6
@@ -282,6 +284,14 @@ def single_inputs(w):
     return rng.random((w["n"], 3)) * w["L"], rng.standard_normal((w["n"], 3))
 
 
+def clustered_inputs(w):
+    """Gaussian clusters (centres uniform in the box), positions wrapped into the box."""
+    rng = np.random.default_rng(w["seed"])
+    centres = rng.random((w["ncl"], 3)) * w["L"]
+    x = (centres[rng.integers(0, w["ncl"], w["n"])] + w["sigma"] * rng.standard_normal((w["n"], 3))) % w["L"]
+    return x, rng.standard_normal((w["n"], 3))
+
+
 def roofline_single(torch, local, steps_warm=3):
     """Stage times of the single N = 1e5 solve and the dominant kernel's roofline."""
     from periodicbrinkman_gb300.api import Plan, make_params
@@ -329,13 +339,13 @@ def roofline_single(torch, local, steps_warm=3):
     return roof, dict(zip(names, stages.tolist())), info
 
 
-def run_single(args, torch, local):
+def run_single(args, torch, local, w=SINGLE, inputs=single_inputs, nerr=96):
     from periodicbrinkman_gb300.api import Plan, make_params
 
-    w = SINGLE
-    x, f = single_inputs(w)
+    x, f = inputs(w)
     p = make_params(w["n"], w["L"], w["alpha"], w["eps"], tol=w["tol"], M=w["M"], P=w["P"], precision="mixed")
     plan = Plan(p)
+    info = plan.info(0)
     xd, fd = torch.from_numpy(x).cuda(), torch.from_numpy(f).cuda()
     Ud = torch.empty_like(xd)
     stream = torch.cuda.current_stream()
@@ -364,14 +374,17 @@ def run_single(args, torch, local):
     try:
         import oracle
 
-        idx = np.random.default_rng(5).choice(w["n"], 96, replace=False)
+        idx = np.random.default_rng(5).choice(w["n"], nerr, replace=False)
         err = oracle.rel_errors(Uh.numpy()[idx], oracle.ewald_velocity(x[idx], x, f, w["L"], w["alpha"], w["eps"]))
     except Exception:
         pass
     nk = plan.kernel_count
+    plan.set_timing(True)
+    plan.execute(xd, fd, U=Ud, stream=stream)
+    stages = dict(zip(["sort", "real", "spread", "fft_green", "gather", "combine"], plan.stage_ms()))
     plan.close()
     return dict(value=args.steps / t_dev, e2e=args.steps / t_e2e, t_dev=t_dev, nk=nk, err=err,
-                clocks=clk.summary())
+                clocks=clk.summary(), info=info, stages=stages)
 
 
 # ---------------------------------------------------------------- CPU / reference arm
@@ -449,7 +462,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="serve", choices=["serve", "single"])
+    ap.add_argument("--workload", default="serve", choices=["serve", "single", "clustered"],
+                    help="serve: the serving stream (default); single: the N = 1e5 solve; clustered: the N = 1e6 "
+                         "solve of 200 Gaussian clusters (L = 2, grid 256^3)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", nargs="?", const="single", choices=["single", "slot", "serve"],
                     help="for ncu: run the single-solve plan twice (eager, then capture+replay), (slot) one "
@@ -490,6 +505,26 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
+    if args.workload == "clustered":
+        w = CLUSTERED
+        r = run_single(args, torch, local, w, clustered_inputs, nerr=16)
+        if rank != 0:
+            return
+        info = r["info"]
+        line = {"metric": METRIC, "value": r["value"] * world, "unit": "solves/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["t_dev"] / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded numpy)",
+                "config": {"workload": w["name"], "grid": info["M"], "P": info["P"], "d": info["d"],
+                           "rc": info["rc"], "pairs_est_uniform": info["pairs_est"],
+                           "l2": "flushed (256 MB write) between steps", "parallelism": f"replicas x{world}"},
+                "e2e": {"value": r["e2e"] * world, "unit": "solves/s", "h2d_bytes_per_step": 2 * 3 * w["n"] * 8,
+                        "d2h_bytes_per_step": 3 * w["n"] * 8},
+                "gpu_launches": r["nk"] * args.steps, "stage_ms": r["stages"],
+                "max_rel_err": r["err"][0] if r["err"] else None, "err_sample": "16 targets vs the FP64 oracle",
+                "clocks": r["clocks"]}
+        print(json.dumps(line))
+        return
     roof, stages, info = roofline_single(torch, local)
     if args.workload == "single":
         r = run_single(args, torch, local)
