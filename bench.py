@@ -52,6 +52,8 @@ SINGLE = dict(name="single_solve_N1e5_uniform_alpha20_eps0.005_grid128_P12_tol1e
               alpha=20.0, eps=0.005, M=128, P=12, tol=1e-6, seed=2000)
 CLUSTERED = dict(name="clustered_N1e6_200clusters_sigma0.02_L2_alpha5_eps0.002_grid256_tol1e-6_mixed", n=1_000_000,
                  L=2.0, alpha=5.0, eps=0.002, M=256, P=0, tol=1e-6, ncl=200, sigma=0.02, seed=3000)
+BATCH = dict(name="batch_512_instances_N_logU100-2e4_L_U0.5-2_alpha_logU1-50_eps0.01L_tol1e-6_mixed", count=512,
+             nmin=100, nmax=20000, seed=4000)
 METRIC = "Brinkman solves/s + p50/p99 latency at <=1e-6 rel err, served vs plain FP64"
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_real_mixed launch of the N = 1e5 solve
 REAL_DRAM_BYTES = 8.06e6
@@ -292,6 +294,72 @@ def clustered_inputs(w):
     return x, rng.standard_normal((w["n"], 3))
 
 
+def batch_instances(w):
+    """The 512-instance batch: per instance (N, L, alpha, eps, x, f)."""
+    rng = np.random.default_rng(w["seed"])
+    out = []
+    for _ in range(w["count"]):
+        n = int(np.exp(rng.uniform(np.log(w["nmin"]), np.log(w["nmax"]))))
+        L = float(rng.uniform(0.5, 2.0))
+        alpha = float(np.exp(rng.uniform(0.0, np.log(50.0))))
+        out.append((n, L, alpha, 0.01 * L, rng.random((n, 3)) * L, rng.standard_normal((n, 3))))
+    return out
+
+
+def run_batch(args, torch, local):
+    """One plan holding all 512 instances (a captured graph per execution)."""
+    from periodicbrinkman_gb300.api import Plan, make_params
+
+    w = BATCH
+    inst = batch_instances(w)
+    params = [make_params(n, L, a, e, tol=1e-6, precision="mixed") for n, L, a, e, _, _ in inst]
+    plan = Plan(params)
+    X = torch.from_numpy(np.concatenate([i[4] for i in inst])).cuda()
+    F = torch.from_numpy(np.concatenate([i[5] for i in inst])).cuda()
+    U = torch.empty_like(X)
+    stream = torch.cuda.current_stream()
+    for _ in range(max(args.warmup, 3)):
+        plan.execute(X, F, U=U, stream=stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            plan.execute(X, F, U=U, stream=stream)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+    t_dev = float(np.sum([a.elapsed_time(b) for a, b in evs])) / 1e3
+    Xh, Fh = X.cpu().pin_memory(), F.cpu().pin_memory()
+    Uh = torch.empty_like(Xh).pin_memory()
+    plan.execute(Xh.numpy(), Fh.numpy(), U=Uh.numpy())
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plan.execute(Xh.numpy(), Fh.numpy(), U=Uh.numpy())
+    t_e2e = time.perf_counter() - t0
+    err = None
+    try:
+        import oracle
+
+        Un = Uh.numpy()
+        offs = np.cumsum([0] + [i[0] for i in inst])
+        worst = 0.0
+        for q in np.random.default_rng(6).choice(len(inst), 6, replace=False):
+            n, L, a, e, x, f = inst[q]
+            sel = np.arange(min(n, 8))
+            ref = oracle.ewald_velocity(x[sel], x, f, L, a, e)
+            worst = max(worst, oracle.rel_errors(Un[offs[q]:offs[q + 1]][sel], ref)[0])
+        err = worst
+    except Exception:
+        pass
+    nk = plan.kernel_count
+    nsrc = int(sum(i[0] for i in inst))
+    plan.close()
+    return dict(value=w["count"] * args.steps / t_dev, e2e=w["count"] * args.steps / t_e2e, t_dev=t_dev, nk=nk,
+                err=err, clocks=clk.summary(), nsrc=nsrc)
+
+
 def roofline_single(torch, local, steps_warm=3):
     """Stage times of the single N = 1e5 solve and the dominant kernel's roofline."""
     from periodicbrinkman_gb300.api import Plan, make_params
@@ -462,9 +530,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="serve", choices=["serve", "single", "clustered"],
+    ap.add_argument("--workload", default="serve", choices=["serve", "single", "clustered", "batch"],
                     help="serve: the serving stream (default); single: the N = 1e5 solve; clustered: the N = 1e6 "
-                         "solve of 200 Gaussian clusters (L = 2, grid 256^3)")
+                         "solve of 200 Gaussian clusters (L = 2, grid 256^3); batch: 512 instances in one plan")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", nargs="?", const="single", choices=["single", "slot", "serve"],
                     help="for ncu: run the single-solve plan twice (eager, then capture+replay), (slot) one "
@@ -505,6 +573,23 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
+    if args.workload == "batch":
+        w = BATCH
+        r = run_batch(args, torch, local)
+        if rank != 0:
+            return
+        line = {"metric": METRIC, "value": r["value"] * world, "unit": "solves/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["t_dev"] / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded numpy)",
+                "config": {"workload": w["name"], "instances": w["count"], "sources": r["nsrc"],
+                           "l2": "flushed (256 MB write) between steps", "parallelism": f"replicas x{world}"},
+                "e2e": {"value": r["e2e"] * world, "unit": "solves/s", "h2d_bytes_per_step": 2 * 3 * r["nsrc"] * 8,
+                        "d2h_bytes_per_step": 3 * r["nsrc"] * 8},
+                "gpu_launches": r["nk"] * args.steps, "max_rel_err": r["err"],
+                "err_sample": "8 targets of 6 instances vs the FP64 oracle", "clocks": r["clocks"]}
+        print(json.dumps(line))
+        return
     if args.workload == "clustered":
         w = CLUSTERED
         r = run_single(args, torch, local, w, clustered_inputs, nerr=16)
