@@ -1,16 +1,19 @@
 // Real-space Ewald sum over a device-built cell list.
 //
 // Work item = (instance, cell row (c0, c1), z-range [za, zb] of at most 8
-// cells, up to 32 consecutive sorted targets), one warp per item, items pulled
-// from a global counter by a persistent grid.  Each lane owns one target.  The
-// sources of the stencil (rows c0 +- S, c1 +- S; cells za - S .. zb + S) are
-// visited as contiguous z-runs of the cell-sorted source array, staged 32 at a
-// time in shared memory.  Mixed precision: each lane classifies its 32 candidate
-// pairs (inside the cutoff / inside the blob region / below r_tiny), the warp
-// compacts them into target-major queues in shared memory, and every lane then
-// evaluates one queued pair at a time, so the FMA pipe sees full warps and the
-// rare blob and series pairs never diverge the common path; per-target sums
-// of each round are formed by a segmented warp reduction (no atomics).
+// cells, up to 32 consecutive sorted targets, a group of the stencil's
+// columns), one warp per item, items pulled from a global counter by a
+// persistent grid.  Each lane owns one target.  Each stencil column is cut to
+// the part of the cutoff ball around the targets' box; its contiguous z-runs
+// of the cell-sorted source array are gathered as segments and streamed
+// through shared memory 32 sources at a time, dropping sources beyond rc of
+// the box.  Mixed precision: each lane classifies its 32 candidate pairs
+// (inside the cutoff / below r_mid), the warp compacts the pairs inside the
+// cutoff into a target-major queue, and every lane then evaluates a block of
+// it, so the FMA pipe sees full warps; per-target sums of each chunk are
+// formed by one segmented warp reduction (no atomics).  Pairs below r_mid
+// (blob, near and series pieces) are queued per warp and evaluated 32 at a
+// time.
 //
 // Mixed precision (k_real_mixed): positions are FP32 hi/lo pairs re-expressed
 // in the frame of the target cell (error-free TwoSum), so displacements carry
@@ -626,11 +629,10 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
         __syncwarp();
 
         // The item's stencil columns, 32 at a time (a lane per column): the
-        // column's part of the cutoff ball around the targets' box is a z-range;
-        // its cells are cut into runs at the periodic wrap and each run is
-        // narrowed to that z-range by binary search (sources are sorted by z
-        // within their cells).  The runs are gathered as segments and streamed
-        // through the warp in full chunks of 32 sources.
+        // column's part of the cutoff ball around the targets' box is a z-range,
+        // taken at cell granularity (cells are rc/4 along z); its cells are cut
+        // into runs at the periodic wrap.  The runs are gathered as segments and
+        // streamed through the warp in full chunks of 32 sources.
         const int ny1 = 2 * I.S[1] + 1, ncol = (2 * I.S[0] + 1) * ny1;
         const int csplit = max(1, I.csplit);
         const int ncg = (ncol - F.group + csplit - 1) / csplit;
