@@ -31,11 +31,12 @@ from ._lib import (  # noqa: F401
     lib,
     lib_path,
 )
-from .api import Plan, fftBrinkman, pair_kernel_tables, periodicBrinkman, solve, shell_counts  # noqa: F401
+from .api import Plan, Server, fftBrinkman, pair_kernel_tables, periodicBrinkman, solve, shell_counts  # noqa: F401
 
 __all__ = [
     "PbError",
     "Plan",
+    "Server",
     "SolveParams",
     "fftBrinkman",
     "periodicBrinkman",
