@@ -211,31 +211,37 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
 // FP32 grids interleave the three components of a point in one float4, so a
 // point costs one vector atomic (spread) or one 16-byte load (gather).
 // FP32-grid window of a point given as FP32 hi/lo pairs: lane a < 3 resolves
-// axis a in FP64 (the grid cell holding x by a multiply with the inverse
-// spacing, and the offset of x from the window start), the other lanes take
-// those by shuffle, and lane p < P computes weight p in FP32 from the offset.
-// No FP64 division: the FP64 pipe of this GPU runs at a small fraction of
-// the FP32 rate.
+// axis a (the grid cell holding x, by a multiply with the inverse spacing, and
+// the offset of x from the window start in double-float arithmetic: g0 h is
+// split exactly by an FMA), the other lanes take those by shuffle, and lane
+// p < P computes weight p from the offset.  No FP64: the FP64 pipe of this GPU
+// runs at a small fraction of the FP32 rate, and the FP64 window set-up had
+// kept it 35-40% busy in spreading and gathering.  Near a cell boundary the
+// cell may come out one lower or higher than exact arithmetic would give; the
+// window then still holds the point within half a spacing of its centre.
 __device__ __forceinline__ void window_f32(const PbInst& I, float4 h4, float4 l4, int lane, float (*wgt)[kMaxP],
                                            int (*idx)[kMaxP], int* g0out = nullptr)
 {
     int g0 = 0;
     float base = 0.f;
     if (lane < 3) {
-        const double xa = (double)(lane == 0 ? h4.x : lane == 1 ? h4.y : h4.z) +
-                          (double)(lane == 0 ? l4.x : lane == 1 ? l4.y : l4.z);
-        const int c = min(max((int)floor(xa * I.gih[lane]), 0), I.M[lane] - 1);
+        const float xh = lane == 0 ? h4.x : lane == 1 ? h4.y : h4.z;
+        const float xl = lane == 0 ? l4.x : lane == 1 ? l4.y : l4.z;
+        const float gi = I.gihf[lane];
+        const int c = min(max((int)floorf(fmaf(xh, gi, xl * gi)), 0), I.M[lane] - 1);
         g0 = c - I.Pa[lane] / 2 + 1;
-        base = (float)fma(-(double)g0, I.gh[lane], xa);
+        const float gf = (float)g0, hh = I.ghh[lane];
+        const float p = gf * hh, e = fmaf(gf, hh, -p);  // g0 hh = p + e exactly
+        base = ((xh - p) - e) + (xl - gf * I.ghl[lane]);
         if (g0out) g0out[lane] = g0;
     }
-    const float inv_eta = (float)(1.0 / I.eta);
+    const float inv_eta = I.inv_eta_f;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const int ga = __shfl_sync(kFull, g0, a);
         const float ba = __shfl_sync(kFull, base, a);
         if (lane < I.Pa[a]) {
-            const float dx = fmaf(-(float)lane, (float)I.gh[a], ba);
+            const float dx = fmaf(-(float)lane, I.ghh[a], ba);
             wgt[a][lane] = expf(-dx * dx * inv_eta);
             idx[a][lane] = (ga + lane) & (I.M[a] - 1);  // grids are powers of two
         }

@@ -61,6 +61,9 @@ struct PbInst {
     double iL[3];     // inverse box lengths
     double ih[3];     // inverse cell widths
     double eta;       // Gaussian spreading parameter: exp(-r^2/eta)
+    float ghh[3], ghl[3];  // grid spacings as FP32 hi + lo (window set-up without FP64)
+    float gihf[3];         // inverse grid spacings in FP32
+    float inv_eta_f;       // 1 / eta in FP32
     double kfac;      // spectral prefactor (normalisations of spread, FFT, gather)
     double zero_mode[3];  // k = 0 mean-flow velocity added to every target (or 0)
     int nc[3];        // cells per axis
