@@ -251,12 +251,12 @@ __device__ __forceinline__ void window_f32(const PbInst& I, float4 h4, float4 l4
 // Grouped spreading: a warp takes kSpreadGroup consecutive (cell-sorted, so
 // nearby) points and adds their windows together over the box that holds
 // them all, one vector L2 atomic per box point instead of one per point and
-// window point (about 40% fewer atomics for three points of one cell).  Each box
+// window point (about half the atomics for four points of one cell).  Each box
 // point sums the points' contributions in registers; per-point weights are
 // laid out along the box (zero outside the point's window), so the box loops
 // need no bounds tests.  Points of another instance, or a box wider than
 // kBoxMax along an axis, are spread one point at a time through the same loops.
-constexpr int kSpreadGroup = 3;  // measured at N = 1e5: 2 -> 0.35 ms, 3 -> 0.31, 4 -> 0.32, 6 -> 0.33, 8 -> 0.38
+constexpr int kSpreadGroup = 4;  // measured at N = 1e5: 2 -> 0.31 ms, 3 -> 0.26, 4 -> 0.24, 5 -> 0.244, 6 -> 0.276
 constexpr int kGatherGroup = 1;  // measured: 1 -> 0.22 ms, 2 -> 0.26, 3 -> 0.29, 4 -> 0.32 at N = 1e5
 constexpr int kBoxMax = 48;
 
