@@ -507,6 +507,12 @@ void set_inst_fields(PbInst& I, const pb_solve_params& p, const Resolved& R, int
         I.gihf[a] = (float)I.gih[a];
     }
     I.inv_eta_f = (float)(1.0 / R.eta);
+    for (int a = 0; a < 3; a++) {
+        I.hch[a] = (float)R.h[a];
+        I.hcl[a] = (float)(R.h[a] - (double)I.hch[a]);
+        I.Lh[a] = (float)p.L[a];
+        I.Ll[a] = (float)(p.L[a] - (double)I.Lh[a]);
+    }
     double Mtot = (double)R.M[0] * R.M[1] * R.M[2];
     I.kfac = I.gh[0] * I.gh[1] * I.gh[2] / (Mtot * std::pow(M_PI * R.eta, 3.0));
     I.P = std::max(R.Pa[0], std::max(R.Pa[1], R.Pa[2]));

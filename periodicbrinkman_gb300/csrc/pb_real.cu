@@ -66,6 +66,20 @@ struct __align__(8) FrameTabs {
     int zx[2 * kMaxReach + 1], zy[2 * kMaxReach + 1], zz[kZTab];
 };
 
+// c h - s L as an FP32 hi/lo pair (double-float arithmetic: the products are
+// split exactly by FMAs), for a cell index c and an image shift count s.
+__device__ __forceinline__ void frame_offset(const PbInst& I, int ax, int c, int sc, float& hi, float& lo)
+{
+    const float cf = (float)c, sf = (float)sc;
+    const float p1 = cf * I.hch[ax], e1 = fmaf(cf, I.hch[ax], -p1);
+    const float p2 = sf * I.Lh[ax], e2 = fmaf(sf, I.Lh[ax], -p2);
+    float s, er;
+    two_sum(p1, -p2, s, er);
+    const float l = er + ((e1 + cf * I.hcl[ax]) - (e2 + sf * I.Ll[ax]));
+    hi = s + l;
+    lo = l - (hi - s);
+}
+
 __device__ __forceinline__ void fill_frame_tabs(const PbInst& I, const ItemFrame& F, FrameTabs& T, int lane)
 {
     const int nx = 2 * I.S[0] + 1, ny = 2 * I.S[1] + 1, nz = F.zb - F.za + 2 * I.S[2] + 1;
@@ -87,9 +101,8 @@ __device__ __forceinline__ void fill_frame_tabs(const PbInst& I, const ItemFrame
         const int n = I.nc[ax];
         int w = ((g % n) + n) % n;
         int sc = (g - w) / n;  // image shift count
-        double Q = F.O[ax] - (double)sc * I.L[ax];
-        float hi, lo;
-        split_double(Q, hi, lo);
+        float hi, lo;  // Q = O - sc L, O = the frame cell's corner
+        frame_offset(I, ax, ax == 0 ? F.c0 : ax == 1 ? F.c1 : F.za, sc, hi, lo);
         if (ax == 0) {
             T.qx[k] = make_float2(hi, lo);
             T.wx[k] = w;
@@ -606,7 +619,7 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 float oh, ol, s, e;
-                split_double(F.O[a], oh, ol);
+                frame_offset(I, a, a == 0 ? F.c0 : a == 1 ? F.c1 : F.za, 0, oh, ol);
                 two_sum(xh[a], -oh, s, e);
                 th[a] = active ? s : 3.0e30f;  // inactive lanes pair with nothing
                 tl[a] = e + (xl[a] - ol);

@@ -64,6 +64,8 @@ struct PbInst {
     float ghh[3], ghl[3];  // grid spacings as FP32 hi + lo (window set-up without FP64)
     float gihf[3];         // inverse grid spacings in FP32
     float inv_eta_f;       // 1 / eta in FP32
+    float hch[3], hcl[3];  // cell widths as FP32 hi + lo (real-space frames without FP64)
+    float Lh[3], Ll[3];    // box lengths as FP32 hi + lo
     double kfac;      // spectral prefactor (normalisations of spread, FFT, gather)
     double zero_mode[3];  // k = 0 mean-flow velocity added to every target (or 0)
     int nc[3];        // cells per axis
