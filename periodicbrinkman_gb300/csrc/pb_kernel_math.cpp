@@ -117,18 +117,25 @@ static void scaled_moments(double b, int nj, double* Kt)
     }
     std::sort(edges.begin(), edges.end());
     for (int j = 0; j < nj; j++) Kt[j] = 0;
+    // per interval, the 16 nodes' weighted powers advance together (independent
+    // lanes), so the power chain is not one serial multiply per node and moment
+    double g[16], k2[16];
     for (size_t p = 0; p + 1 < edges.size(); p++) {
         double lo = edges[p], hi = edges[p + 1];
         if (hi - lo < 1e-15) continue;
         double mid = 0.5 * (lo + hi), h = 0.5 * (hi - lo);
         for (int q = 0; q < 16; q++) {
-            double k = mid + h * gx[q], k2 = k * k;
-            double g = (1.0 + c * k2 / (b * b)) * std::exp(-k2 / 4) / (k2 + b * b) * gw[q] * h;
-            double pw = 1;
-            for (int j = 0; j < nj; j++) {
-                Kt[j] += g * pw;
-                pw *= k2;
+            double k = mid + h * gx[q];
+            k2[q] = k * k;
+            g[q] = (1.0 + c * k2[q] / (b * b)) * std::exp(-k2[q] / 4) / (k2[q] + b * b) * gw[q] * h;
+        }
+        for (int j = 0; j < nj; j++) {
+            double s = 0;
+            for (int q = 0; q < 16; q++) {
+                s += g[q];
+                g[q] *= k2[q];
             }
+            Kt[j] += s;
         }
     }
 }
@@ -199,15 +206,57 @@ void scaled_diffH(double r, double a, double delta, const double* ser1, const do
 
 namespace {
 
+// The matrix C[j][k] = cos(pi j (2k + 1) / (2 nodes)) of the Chebyshev
+// transform, as cos(pi q / (2 nodes)) at q = j (2k + 1) mod 4 nodes; built once
+// per node count for the two counts the fits use, else per call.
+const double* cos_matrix(int nodes, std::vector<double>& own)
+{
+    static std::once_flag once;
+    static std::vector<double> m40, m64;
+    auto fill = [](std::vector<double>& m, int n) {
+        std::vector<double> ct(4 * n);
+        for (int q = 0; q < 4 * n; q++) ct[q] = std::cos(kPi * q / (2.0 * n));
+        m.resize((size_t)n * n);
+        for (int j = 0; j < n; j++)
+            for (int k = 0; k < n; k++) m[(size_t)j * n + k] = ct[(j * (2 * k + 1)) % (4 * n)];
+    };
+    std::call_once(once, [&] {
+        fill(m40, 40);
+        fill(m64, 64);
+    });
+    if (nodes == 40) return m40.data();
+    if (nodes == 64) return m64.data();
+    fill(own, nodes);
+    return own.data();
+}
+
 // Chebyshev coefficients of samples v[k] = f(node k) (c[0] halved, untruncated).
+// Four coefficients are summed side by side (independent addition chains, each
+// in the order k = 0, 1, ...).
 std::vector<double> cheb_coeffs(const std::vector<double>& v)
 {
     const int nodes = (int)v.size();
-    std::vector<double> c(nodes), ct(4 * nodes);
-    for (int q = 0; q < 4 * nodes; q++) ct[q] = std::cos(kPi * q / (2.0 * nodes));  // cos(pi q / (2 nodes))
-    for (int j = 0; j < nodes; j++) {
+    std::vector<double> c(nodes), own;
+    const double* C = cos_matrix(nodes, own);
+    int j = 0;
+    for (; j + 4 <= nodes; j += 4) {
+        const double *r0 = C + (size_t)j * nodes, *r1 = r0 + nodes, *r2 = r1 + nodes, *r3 = r2 + nodes;
+        double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+        for (int k = 0; k < nodes; k++) {
+            s0 += v[k] * r0[k];
+            s1 += v[k] * r1[k];
+            s2 += v[k] * r2[k];
+            s3 += v[k] * r3[k];
+        }
+        c[j] = s0 * 2.0 / nodes;
+        c[j + 1] = s1 * 2.0 / nodes;
+        c[j + 2] = s2 * 2.0 / nodes;
+        c[j + 3] = s3 * 2.0 / nodes;
+    }
+    for (; j < nodes; j++) {
+        const double* r = C + (size_t)j * nodes;
         double s = 0;
-        for (int k = 0; k < nodes; k++) s += v[k] * ct[(j * (2 * k + 1)) % (4 * nodes)];
+        for (int k = 0; k < nodes; k++) s += v[k] * r[k];
         c[j] = s * 2.0 / nodes;
     }
     c[0] *= 0.5;
@@ -227,19 +276,24 @@ int cheb_terms(const std::vector<double>& c, double rel_tol)
 std::vector<double> cheb_to_monomial(const std::vector<double>& c)
 {
     const int n = (int)c.size();
-    // T_{j+1} = 2 t T_j - T_{j-1}
-    std::vector<double> a(n, 0.0), T0(n, 0.0), T1(n, 0.0);
+    // T_{j+1} = 2 t T_j - T_{j-1}, the monomial coefficients of T_{j-1}, T_j and
+    // T_{j+1} rotating through three rows
+    std::vector<double> a(n, 0.0), rows(3 * (size_t)n, 0.0);
+    double* T0 = rows.data();
+    double* T1 = T0 + n;
+    double* Tn = T1 + n;
     T0[0] = 1;
     if (n > 1) T1[1] = 1;
     for (int j = 0; j < n; j++) {
-        const std::vector<double>& Tj = (j == 0) ? T0 : T1;
+        const double* Tj = (j == 0) ? T0 : T1;
         for (int q = 0; q < n; q++) a[q] += c[j] * Tj[q];
         if (j >= 1) {
-            std::vector<double> Tn(n, 0.0);
-            for (int q = 0; q + 1 < n; q++) Tn[q + 1] += 2 * T1[q];
-            for (int q = 0; q < n; q++) Tn[q] -= T0[q];
+            Tn[0] = -T0[0];
+            for (int q = 1; q < n; q++) Tn[q] = 2 * T1[q - 1] - T0[q];
+            double* t = T0;
             T0 = T1;
             T1 = Tn;
+            Tn = t;
         }
     }
     return a;
