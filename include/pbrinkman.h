@@ -38,7 +38,8 @@ extern "C" {
 #define PB_FLAGS_DEFAULT (PB_REAL_SPACE | PB_KSPACE)
 
 /* memory location of user buffers */
-#define PB_HOST 0        /* host memory; the call returns when U is written */
+#define PB_HOST 0        /* host memory; the call returns when U is written (a non-finite
+                            input is found on the device: PB_ERR_INVALID, U unspecified) */
 #define PB_DEVICE 1      /* device memory; ordered on the given stream */
 #define PB_HOST_PINNED 2 /* page-locked host memory; ordered on the given stream, no wait */
 

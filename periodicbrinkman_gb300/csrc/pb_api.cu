@@ -1256,7 +1256,11 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
         return fail(PB_ERR_INVALID, "bad memory location");
     cudaStream_t us = (cudaStream_t)stream_v;
     cudaStream_t s = P->stream;
-    if (where == PB_HOST || where == PB_HOST_PINNED) {
+    // Non-finite inputs: the asynchronous host path scans them here, before
+    // anything is queued; the synchronous host path reads the flags the
+    // binning and preparation kernels set (they map such values to finite
+    // ones), after the execution, and then fails with U unspecified.
+    if (where == PB_HOST_PINNED) {
         for (size_t i = 0; i < 3 * (size_t)P->act_src; i++)
             if (!std::isfinite(x[i]) || !std::isfinite(f[i])) return fail(PB_ERR_INVALID, "non-finite input");
         if (!P->all_same)
@@ -1277,10 +1281,14 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
         cudaMemcpyKind kout = where == PB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
         PB_CK(cudaMemcpyAsync(U, P->U, sizeof(double) * 3 * P->act_tgt, kout, s));
     }
+    if (where == PB_HOST) PB_CK(cudaMemcpyAsync(P->h_bad, P->d_bad, sizeof(int) * P->count, cudaMemcpyDeviceToHost, s));
     P->exec_count++;
     PB_CK(cudaEventRecord(P->ev_out, s));
     PB_CK(cudaStreamWaitEvent(us, P->ev_out, 0));
     if (where == PB_HOST || P->timing) PB_CK(cudaStreamSynchronize(s));
+    if (where == PB_HOST)
+        for (int q = 0; q < P->count; q++)
+            if (P->h_bad[q]) return fail(PB_ERR_INVALID, "non-finite input (instance %d)", q);
     if (P->timing) {
         float ms;
         for (int k = 0; k < 6; k++) {

@@ -193,3 +193,26 @@ def test_empty_and_invalid():
         pb.solve(bad, f, 1.0, 10.0, 0.01)
     u = pb.solve(cuda(np.zeros((0, 3))), cuda(np.zeros((0, 3))), 1.0, 10.0, 0.01, y=cuda(x)).cpu().numpy()
     assert u.shape == (10, 3) and np.all(u == 0)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_host_non_finite_inputs_found_on_device(prec):
+    """Host-memory executions find non-finite positions, forces and targets
+    through the device flags; the plan stays usable and matches a clean run."""
+    from periodicbrinkman_gb300 import _lib
+
+    x, f, y = _case(300, 1.0, 19, m=120)
+    p = make_params(300, 1.0, 10.0, 0.01, n_tgt=120, tol=1e-6, precision=prec)
+    with Plan(p) as plan:
+        ref = plan.execute(x, f, y=y)
+        for arr, idx, val in ((x, (5, 0), np.nan), (f, (7, 2), np.inf), (y, (3, 1), -np.inf)):
+            bad = arr.copy()
+            bad[idx] = val
+            args = dict(x=x, f=f, y=y)
+            args["x" if arr is x else "f" if arr is f else "y"] = bad
+            with pytest.raises(pb.PbError) as ei:
+                plan.execute(args["x"], args["f"], y=args["y"])
+            assert ei.value.code == _lib.PB_ERR_INVALID
+        again = plan.execute(x, f, y=y)
+    # atomics make the summation order vary between runs: equal to rounding
+    assert np.abs(again - ref).max() <= 1e-6 * np.abs(ref).max()
