@@ -155,6 +155,12 @@ int pb_plan_create(const pb_solve_params* p, int count, pb_plan* out);
 /* Packed inputs: instances back to back in the order of creation. */
 int pb_plan_execute(pb_plan plan, const double* x, const double* f, const double* y, double* U, int where,
                     void* stream);
+/* The same plan applied to new forces at the positions (and targets) of its
+ * last successful pb_plan_execute: a matrix-free mobility product for
+ * iterative solves.  Only f (3 x n_src) is read; the cell lists and work
+ * items are reused, so the sorting stage is skipped.  PB_ERR_INVALID if no
+ * execution with positions has succeeded since creation or the last bind. */
+int pb_plan_execute_forces(pb_plan plan, const double* f, double* U, int where, void* stream);
 int pb_plan_instance_info(pb_plan plan, int i, pb_instance_info* info);
 /* A capacity plan (serving slot) with no instances bound yet. */
 int pb_plan_create_slot(const pb_slot_config* cfg, pb_plan* out);

@@ -157,6 +157,7 @@ def lib():
     L.pb_solve.argtypes = [C.POINTER(SolveParams), vp, vp, vp, vp, C.c_int, vp]
     L.pb_plan_create.argtypes = [C.POINTER(SolveParams), C.c_int, C.POINTER(vp)]
     L.pb_plan_execute.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp]
+    L.pb_plan_execute_forces.argtypes = [vp, vp, vp, C.c_int, vp]
     L.pb_plan_instance_info.argtypes = [vp, C.c_int, C.POINTER(InstanceInfo)]
     L.pb_resolve.argtypes = [C.POINTER(SolveParams), C.POINTER(InstanceInfo)]
     L.pb_plan_device_bytes.restype = C.c_longlong

@@ -111,6 +111,23 @@ class Plan:
         check(lib().pb_plan_execute(self._h, _ptr(x), _ptr(f), _ptr(y), _ptr(U), where, s))
         return U
 
+    def execute_forces(self, f, U=None, stream=None):
+        """New forces at the positions of the last `execute` (a matrix-free
+        mobility product: the cell lists and work items are reused)."""
+        if U is None:
+            if _is_torch(f):
+                import torch
+
+                U = torch.empty((self.n_tgt, 3), dtype=torch.float64, device=f.device)
+            else:
+                U = np.empty((self.n_tgt, 3))
+        where = _where([f, U])
+        s = None
+        if stream is not None:
+            s = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        check(lib().pb_plan_execute_forces(self._h, _ptr(f), _ptr(U), where, s))
+        return U
+
     def info(self, i: int = 0) -> dict:
         inf = InstanceInfo()
         check(lib().pb_plan_instance_info(self._h, i, C.byref(inf)))

@@ -344,7 +344,10 @@ struct pb_plan_s {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t gexec_f = nullptr;  // forces-only executions (positions of the last full one)
     int exec_count = 0;
+    int fexec_count = 0;
+    bool have_positions = false;  // a full execution since the last bind sorted the current positions
     int graph_kernels = 0;  // kernel nodes in the captured graph
     bool timing = false;
     cudaEvent_t tev[7] = {};
@@ -671,6 +674,7 @@ void plan_free(pb_plan_s* P)
 {
     if (!P) return;
     if (P->gexec) cudaGraphExecDestroy(P->gexec);
+    if (P->gexec_f) cudaGraphExecDestroy(P->gexec_f);
     if (P->arena) cudaFree(P->arena);
     if (P->staging) cudaFreeHost(P->staging);
     if (P->h_bad) cudaFreeHost(P->h_bad);
@@ -737,21 +741,25 @@ void record(pb_plan_s* P, int k, cudaStream_t s)
     if (P->timing) cudaEventRecord(P->tev[k], s);
 }
 
-// The device work of one execution (inputs already in P->x/f/y).
-void run_compute(pb_plan_s* P, cudaStream_t s)
+// The device work of one execution (inputs already in P->x/f/y).  With
+// `forces_only` the cell lists, target records and work items of the last
+// full execution are kept: only the source records are rebuilt (same
+// positions, new forces).
+void run_compute(pb_plan_s* P, cudaStream_t s, bool forces_only)
 {
     const bool mixed = P->prec == PB_PREC_MIXED;
     record(P, 0, s);
     cudaMemsetAsync(P->d_bad, 0, sizeof(int) * P->count, s);
-    bin_and_sort(P, P->x, P->n_src, P->d_src_off, P->cell_of_s, P->cnt_s, P->start_s, P->fill_s, P->perm_tmp_s,
-                 P->perm_s, s);
+    if (!forces_only)
+        bin_and_sort(P, P->x, P->n_src, P->d_src_off, P->cell_of_s, P->cnt_s, P->start_s, P->fill_s, P->perm_tmp_s,
+                     P->perm_s, s);
     if (mixed)
         launch_prepare_mixed(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count, (float4*)P->spos_a,
                              (float4*)P->spos_b, (float4*)P->sfrc, P->d_bad, s);
     else
         launch_prepare_fp64(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count, (Dbl4*)P->spos_a,
                             (Dbl4*)P->sfrc, P->d_bad, s);
-    if (!P->all_same) {
+    if (!P->all_same && !forces_only) {
         launch_pack_targets(P->x, P->y, P->n_tgt, P->d_tgt_off, P->d_src_off, P->d_y_off, P->count, P->ypack, s);
         bin_and_sort(P, P->ypack, P->n_tgt, P->d_tgt_off, P->cell_of_t, P->cnt_t, P->start_t, P->fill_t,
                      P->perm_tmp_t, P->perm_t, s);
@@ -762,8 +770,9 @@ void run_compute(pb_plan_s* P, cudaStream_t s)
             launch_prepare_fp64(P->ypack, nullptr, P->perm_t, P->n_tgt, P->d_tgt_off, P->d_inst, P->count,
                                 (Dbl4*)P->tpos_a, nullptr, P->d_bad, s);
     }
-    launch_build_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items, P->item_cap,
-                       P->counter + 1, P->nsm, s);
+    if (!forces_only)
+        launch_build_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items, P->item_cap,
+                           P->counter + 1, P->nsm, s);
     record(P, 1, s);
     if (P->any_real) {
         const int* nitems = P->counter + 1;
@@ -989,6 +998,7 @@ int bind_impl(pb_plan P, const pb_solve_params* p, const PbTables* tabs, int cou
     std::memcpy(st + oo + 2 * ob, P->cell_off.data(), ob);
     std::memcpy(st + oo + 3 * ob, P->y_off.data(), ob);
     P->upload_pending = true;
+    P->have_positions = false;
     P->bound = count;
     P->act_src = (int)ns;
     P->act_tgt = (int)nt;
@@ -1004,7 +1014,7 @@ namespace pb {
 
 // Uploads a pending binding and runs the device work: eagerly on the first
 // execution (and when timing), as a captured CUDA graph afterwards.
-int upload_and_compute(pb_plan P, cudaStream_t s)
+int upload_and_compute(pb_plan P, cudaStream_t s, bool forces_only)
 {
     if (P->upload_pending) {
         char* st = P->staging;
@@ -1020,28 +1030,33 @@ int upload_and_compute(pb_plan P, cudaStream_t s)
         P->upload_pending = false;
     }
     if (P->n_tgt <= 0 || P->act_tgt <= 0) return PB_OK;
-    if (P->timing || P->exec_count < 1) {
-        run_compute(P, s);
+    cudaGraphExec_t& gx = forces_only ? P->gexec_f : P->gexec;
+    const int runs = forces_only ? P->fexec_count : P->exec_count;
+    if (P->timing || runs < 1) {
+        run_compute(P, s, forces_only);
     } else {
-        if (!P->gexec) {
+        if (!gx) {
             cudaGraph_t g;
             PB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            run_compute(P, s);
+            run_compute(P, s, forces_only);
             PB_CK(cudaStreamEndCapture(s, &g));
-            size_t nn = 0;
-            cudaGraphGetNodes(g, nullptr, &nn);
-            std::vector<cudaGraphNode_t> nodes(nn);
-            cudaGraphGetNodes(g, nodes.data(), &nn);
-            P->graph_kernels = 0;
-            for (auto nd : nodes) {
-                cudaGraphNodeType ty;
-                if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) P->graph_kernels++;
+            if (!forces_only) {
+                size_t nn = 0;
+                cudaGraphGetNodes(g, nullptr, &nn);
+                std::vector<cudaGraphNode_t> nodes(nn);
+                cudaGraphGetNodes(g, nodes.data(), &nn);
+                P->graph_kernels = 0;
+                for (auto nd : nodes) {
+                    cudaGraphNodeType ty;
+                    if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+                        P->graph_kernels++;
+                }
             }
-            cudaError_t e = cudaGraphInstantiate(&P->gexec, g, 0);
+            cudaError_t e = cudaGraphInstantiate(&gx, g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return fail(PB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
         }
-        PB_CK(cudaGraphLaunch(P->gexec, s));
+        PB_CK(cudaGraphLaunch(gx, s));
     }
     PB_CK(cudaGetLastError());
     return PB_OK;
@@ -1065,7 +1080,7 @@ int plan_execute_parts(pb_plan P, const double* const* xs, const double* const* 
             PB_CK(cudaMemcpyAsync(P->y + 3 * (size_t)P->y_off[q], ys[q], sizeof(double) * 3 * R.n_tgt,
                                   cudaMemcpyHostToDevice, s));
     }
-    int rc = upload_and_compute(P, s);
+    int rc = upload_and_compute(P, s, false);
     if (rc) return rc;
     for (int q = 0; q < P->bound; q++) {
         const Resolved& R = P->res[q];
@@ -1246,11 +1261,16 @@ int pb_plan_stage_ms(pb_plan plan, double* ms6)
     return PB_OK;
 }
 
-int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y, double* U, int where,
-                    void* stream_v)
+// One execution of a plan; with `forces_only` the positions (and targets) of
+// the last full execution are reused and only `f` is read.
+static int execute_impl(pb_plan P, const double* x, const double* f, const double* y, double* U, int where, void* stream_v,
+                 bool forces_only)
 {
     if (!P) return fail(PB_ERR_INVALID, "null plan");
-    if ((P->act_src > 0 && (!x || !f)) || (P->act_tgt > 0 && !U) || (!P->all_same && P->act_y > 0 && !y))
+    if (forces_only && !P->have_positions)
+        return fail(PB_ERR_INVALID, "no sorted positions: execute the plan with positions first");
+    if ((P->act_src > 0 && ((!forces_only && !x) || !f)) || (P->act_tgt > 0 && !U) ||
+        (!forces_only && !P->all_same && P->act_y > 0 && !y))
         return fail(PB_ERR_INVALID, "null buffer");
     if (where != PB_HOST && where != PB_DEVICE && where != PB_HOST_PINNED)
         return fail(PB_ERR_INVALID, "bad memory location");
@@ -1262,8 +1282,9 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
     // ones), after the execution, and then fails with U unspecified.
     if (where == PB_HOST_PINNED) {
         for (size_t i = 0; i < 3 * (size_t)P->act_src; i++)
-            if (!std::isfinite(x[i]) || !std::isfinite(f[i])) return fail(PB_ERR_INVALID, "non-finite input");
-        if (!P->all_same)
+            if ((!forces_only && !std::isfinite(x[i])) || !std::isfinite(f[i]))
+                return fail(PB_ERR_INVALID, "non-finite input");
+        if (!forces_only && !P->all_same)
             for (size_t i = 0; i < 3 * (size_t)P->act_y; i++)
                 if (!std::isfinite(y[i])) return fail(PB_ERR_INVALID, "non-finite target");
     }
@@ -1271,24 +1292,31 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
     PB_CK(cudaStreamWaitEvent(s, P->ev_in, 0));
     cudaMemcpyKind kin = where == PB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (P->act_src > 0) {
-        PB_CK(cudaMemcpyAsync(P->x, x, sizeof(double) * 3 * P->act_src, kin, s));
+        if (!forces_only) PB_CK(cudaMemcpyAsync(P->x, x, sizeof(double) * 3 * P->act_src, kin, s));
         PB_CK(cudaMemcpyAsync(P->f, f, sizeof(double) * 3 * P->act_src, kin, s));
     }
-    if (!P->all_same && P->act_y > 0) PB_CK(cudaMemcpyAsync(P->y, y, sizeof(double) * 3 * P->act_y, kin, s));
-    int rc = upload_and_compute(P, s);
+    if (!forces_only && !P->all_same && P->act_y > 0)
+        PB_CK(cudaMemcpyAsync(P->y, y, sizeof(double) * 3 * P->act_y, kin, s));
+    // a failed full execution leaves no positions to reuse
+    if (!forces_only) P->have_positions = false;
+    int rc = upload_and_compute(P, s, forces_only);
     if (rc) return rc;
     if (P->n_tgt > 0 && P->act_tgt > 0) {
         cudaMemcpyKind kout = where == PB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
         PB_CK(cudaMemcpyAsync(U, P->U, sizeof(double) * 3 * P->act_tgt, kout, s));
     }
     if (where == PB_HOST) PB_CK(cudaMemcpyAsync(P->h_bad, P->d_bad, sizeof(int) * P->count, cudaMemcpyDeviceToHost, s));
-    P->exec_count++;
+    if (forces_only)
+        P->fexec_count++;
+    else
+        P->exec_count++;
     PB_CK(cudaEventRecord(P->ev_out, s));
     PB_CK(cudaStreamWaitEvent(us, P->ev_out, 0));
     if (where == PB_HOST || P->timing) PB_CK(cudaStreamSynchronize(s));
     if (where == PB_HOST)
         for (int q = 0; q < P->count; q++)
             if (P->h_bad[q]) return fail(PB_ERR_INVALID, "non-finite input (instance %d)", q);
+    if (!forces_only) P->have_positions = true;
     if (P->timing) {
         float ms;
         for (int k = 0; k < 6; k++) {
@@ -1297,6 +1325,17 @@ int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y
         }
     }
     return PB_OK;
+}
+
+int pb_plan_execute(pb_plan P, const double* x, const double* f, const double* y, double* U, int where,
+                    void* stream_v)
+{
+    return execute_impl(P, x, f, y, U, where, stream_v, false);
+}
+
+int pb_plan_execute_forces(pb_plan P, const double* f, double* U, int where, void* stream_v)
+{
+    return execute_impl(P, nullptr, f, nullptr, U, where, stream_v, true);
 }
 
 int pb_solve(const pb_solve_params* p, const double* x, const double* f, const double* y, double* U, int where,
