@@ -56,7 +56,9 @@ BATCH = dict(name="batch_512_instances_N_logU100-2e4_L_U0.5-2_alpha_logU1-50_eps
              nmin=100, nmax=20000, seed=4000)
 METRIC = "Brinkman solves/s + p50/p99 latency at <=1e-6 rel err, served vs plain FP64"
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_real_mixed launch of the N = 1e5 solve
-REAL_DRAM_BYTES = 8.06e6
+REAL_DRAM_BYTES = 7.57e6
+# the same for the k-space kernels of that solve (spread 77.7 MB, five FFT passes 136.4 MB, gather 36.8 MB)
+KSPACE_DRAM_BYTES = 250.9e6
 
 
 def peaks():
@@ -403,6 +405,16 @@ def roofline_single(torch, local, steps_warm=3):
         ach = by / (stages[i] * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": ach / pk["hbm_gbs"],
                 "traffic": None, "kernel": dom, "note": f"peak of {src}"}
+    # the k-space path (spread + FFT/Green + gather) against HBM: algorithmic
+    # bytes 4 B x 3 x M^3 x 6 + 36 B n + 24 B n per solve
+    by = 4.0 * 3 * M3 * 6 + 36.0 * n + 24.0 * n
+    tk = float(stages[2] + stages[3] + stages[4]) * 1e-3
+    ach = by / tk / 1e9
+    roof_k = {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": ach / pk["hbm_gbs"],
+              "traffic": KSPACE_DRAM_BYTES, "kernel": "k_spread_f4g + FFT passes + k_gather_f4g",
+              "note": f"peak of {src}; the grid stays in L2, so the path is bound by L2 reductions (spread) and the "
+                      "L1 data pipe (gather), not by HBM (profiles/k_spread_gather_f4_single_solve_N1e5.md)"}
+    roof["kspace"] = roof_k
     plan.close()
     return roof, dict(zip(names, stages.tolist())), info
 
