@@ -50,6 +50,9 @@ SERVE = dict(name="serve_stream_20000req_2000per_s_N1e3-2e5_targets_N/2_alpha1-5
              nreq=20000, rate=2000.0, nmin=1000, nmax=200000, seed=5000, budget=150 << 30)
 SINGLE = dict(name="single_solve_N1e5_uniform_alpha20_eps0.005_grid128_P12_tol1e-6_mixed", n=100_000, L=1.0,
               alpha=20.0, eps=0.005, M=128, P=12, tol=1e-6, seed=2000)
+# the N = 1e5 solve at tol 1e-9: the FP64 path with the autotuned grid and support
+SINGLE_FP64 = dict(name="single_solve_N1e5_uniform_alpha20_eps0.005_tol1e-9_fp64", n=100_000, L=1.0, alpha=20.0,
+                   eps=0.005, M=0, P=0, tol=1e-9, seed=2000, precision="fp64")
 CLUSTERED = dict(name="clustered_N1e6_200clusters_sigma0.02_L2_alpha5_eps0.002_grid256_tol1e-6_mixed", n=1_000_000,
                  L=2.0, alpha=5.0, eps=0.002, M=256, P=0, tol=1e-6, ncl=200, sigma=0.02, seed=3000)
 BATCH = dict(name="batch_512_instances_N_logU100-2e4_L_U0.5-2_alpha_logU1-50_eps0.01L_tol1e-6_mixed", count=512,
@@ -423,7 +426,8 @@ def run_single(args, torch, local, w=SINGLE, inputs=single_inputs, nerr=96):
     from periodicbrinkman_gb300.api import Plan, make_params
 
     x, f = inputs(w)
-    p = make_params(w["n"], w["L"], w["alpha"], w["eps"], tol=w["tol"], M=w["M"], P=w["P"], precision="mixed")
+    p = make_params(w["n"], w["L"], w["alpha"], w["eps"], tol=w["tol"], M=w["M"], P=w["P"],
+                    precision=w.get("precision", "mixed"))
     plan = Plan(p)
     info = plan.info(0)
     xd, fd = torch.from_numpy(x).cuda(), torch.from_numpy(f).cuda()
@@ -542,9 +546,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="serve", choices=["serve", "single", "clustered", "batch"],
-                    help="serve: the serving stream (default); single: the N = 1e5 solve; clustered: the N = 1e6 "
-                         "solve of 200 Gaussian clusters (L = 2, grid 256^3); batch: 512 instances in one plan")
+    ap.add_argument("--workload", default="serve", choices=["serve", "single", "single_fp64", "clustered", "batch"],
+                    help="serve: the serving stream (default); single: the N = 1e5 solve; single_fp64: the same "
+                         "at tol 1e-9 on the FP64 path; clustered: the N = 1e6 solve of 200 Gaussian clusters "
+                         "(L = 2, grid 256^3); batch: 512 instances in one plan")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", nargs="?", const="single", choices=["single", "slot", "serve"],
                     help="for ncu: run the single-solve plan twice (eager, then capture+replay), (slot) one "
@@ -602,15 +607,16 @@ def main():
                 "err_sample": "8 targets of 6 instances vs the FP64 oracle", "clocks": r["clocks"]}
         print(json.dumps(line))
         return
-    if args.workload == "clustered":
-        w = CLUSTERED
-        r = run_single(args, torch, local, w, clustered_inputs, nerr=16)
+    if args.workload in ("clustered", "single_fp64"):
+        w = CLUSTERED if args.workload == "clustered" else SINGLE_FP64
+        r = run_single(args, torch, local, w, clustered_inputs if args.workload == "clustered" else single_inputs,
+                       nerr=16)
         if rank != 0:
             return
         info = r["info"]
         line = {"metric": METRIC, "value": r["value"] * world, "unit": "solves/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["t_dev"] / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if w.get("precision") == "fp64" else "f32+f64",
                 "data": "synthetic (seeded numpy)",
                 "config": {"workload": w["name"], "grid": info["M"], "P": info["P"], "d": info["d"],
                            "rc": info["rc"], "pairs_est_uniform": info["pairs_est"],

@@ -88,6 +88,44 @@ __device__ __forceinline__ void diffH_d(double r, double a, double d, double c_d
          pre / r2 * ((3 + 3 * ar + a2r2) * em + (3 - 3 * ar + a2r2) * ep);
 }
 
+// diffH_d with the per-(alpha, delta) constants hoisted and one division per
+// call (1/r) instead of eight: the FP64 pipe of a GB300 runs at a small
+// fraction of its FP32 rate and a division is a sequence of FP64 FMAs.  The
+// same closed forms (the reference's diffH), rounded differently.
+struct DiffHConsts {
+    double a, a2, d2, inv_d, inv_d2, c_d, g, inv8pia2, ad2;
+};
+
+__device__ __forceinline__ DiffHConsts diffh_consts(double a, double d, double c_d)
+{
+    const double kSqrtPi = 1.77245385090551602729816748334114518;
+    DiffHConsts k;
+    k.a = a;
+    k.a2 = a * a;
+    k.d2 = d * d;
+    k.inv_d = 1.0 / d;
+    k.inv_d2 = k.inv_d * k.inv_d;
+    k.c_d = c_d;
+    k.g = 1.0 / (2 * a * a * d * d * d * kPiD * kSqrtPi);
+    k.inv8pia2 = 1.0 / (8 * kPiD * a * a);
+    k.ad2 = a * d / 2;
+    return k;
+}
+
+__device__ __forceinline__ void diffH_fast_d(double r, double ir, const DiffHConsts& k, double& H1, double& H2)
+{
+    const double r2 = r * r, ir2 = ir * ir, z = r * k.inv_d;
+    const double ex = exp(-r2 * k.inv_d2) * k.c_d;
+    const double ec = erfc(z);
+    const double em = experf_d(-k.ad2, z), ep = experf_d(k.ad2, z);
+    const double pre = k.inv8pia2 * ir2 * ir;
+    const double ar = k.a * r, a2r2 = k.a2 * r2;
+    const double gx = k.g * ir2 * ex;
+    H1 = -2 * pre * ec - (k.d2 + 2 * r2) * gx + pre * ((1 + ar + a2r2) * em + (1 - ar + a2r2) * ep);
+    H2 = 6 * pre * ir2 * ec + (3 * k.d2 + 2 * r2) * gx * ir2 -
+         pre * ir2 * ((3 + 3 * ar + a2r2) * em + (3 - 3 * ar + a2r2) * ep);
+}
+
 // FP64 small-r series of R_eps - R_d in r^2.
 __device__ __forceinline__ void series_H(const PbTables& T, double r2, double& H1, double& H2)
 {

@@ -781,6 +781,8 @@ __global__ void __launch_bounds__(kRealWarps * 32)
         const PbTables& T = tab[it.x];
         const double a = I.alpha, dd = I.d, ee = I.eps;
         const double cd = -expm1(-a * a * dd * dd / 4), ce = -expm1(-a * a * ee * ee / 4);
+        const DiffHConsts kd = diffh_consts(a, dd, cd);
+        const DiffHConsts ke = diffh_consts(a, ee > 0 ? ee : dd, ce);  // used only when eps > 0
         const double rc2 = I.rc * I.rc;
         const double rs2 = (double)T.rs2;
         ItemFrame F;
@@ -848,11 +850,11 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                         H2 = 0;
                                     }
                                 } else {
-                                    double r = sqrt(r2);
-                                    diffH_d(r, a, dd, cd, H1, H2);
+                                    const double r = sqrt(r2), ir = 1.0 / r;
+                                    diffH_fast_d(r, ir, kd, H1, H2);
                                     if (T.blob && r2 < rs2) {
                                         double e1, e2;
-                                        diffH_d(r, a, ee, ce, e1, e2);
+                                        diffH_fast_d(r, ir, ke, e1, e2);
                                         H1 -= e1;
                                         H2 -= e2;
                                     }
