@@ -208,7 +208,7 @@ namespace {
 
 // The matrix C[j][k] = cos(pi j (2k + 1) / (2 nodes)) of the Chebyshev
 // transform, as cos(pi q / (2 nodes)) at q = j (2k + 1) mod 4 nodes; built once
-// per node count for the two counts the fits use, else per call.
+// per node count for the three counts the fits use, else per call.
 const double* cos_matrix(int nodes, std::vector<double>& own)
 {
     static std::once_flag once;
@@ -220,12 +220,15 @@ const double* cos_matrix(int nodes, std::vector<double>& own)
         for (int j = 0; j < n; j++)
             for (int k = 0; k < n; k++) m[(size_t)j * n + k] = ct[(j * (2 * k + 1)) % (4 * n)];
     };
+    static std::vector<double> m96;
     std::call_once(once, [&] {
         fill(m40, 40);
         fill(m64, 64);
+        fill(m96, 96);
     });
     if (nodes == 40) return m40.data();
     if (nodes == 64) return m64.data();
+    if (nodes == 96) return m96.data();
     fill(own, nodes);
     return own.data();
 }
@@ -370,6 +373,19 @@ int build_tables(double a, double d, double eps, double rc, double poly_tol, PbT
         return (int)q1.size();
     };
     t->nn = cheb(Td, r_near, r_mid, t->cn1, t->cn2, &t->tn_scale, &t->tn_off);
+    {
+        // the far piece again, in FP64 for the FP64 path's pairs beyond r_mid
+        std::vector<double> q1, q2;
+        fit_chebyshev_pair(Td, r_far, rc, 96, 1e-14, kMaxCheb64, q1, q2);
+        t->nf = (int)q1.size();
+        for (int k = 0; k < t->nf; k++) {
+            t->cf1[k] = q1[k];
+            t->cf2[k] = q2[k];
+        }
+        t->tf_scale = 2.0 / (rc - r_far);
+        t->tf_off = -(rc + r_far) / (rc - r_far);
+        t->rf2 = r_mid * r_mid;
+    }
     t->rc2 = (float)(rc * rc);
     t->rm2 = (float)(r_mid * r_mid);
     if (eps > 0) {

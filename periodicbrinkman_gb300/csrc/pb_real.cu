@@ -769,8 +769,10 @@ __global__ void __launch_bounds__(kRealWarps * 32)
 {
     __shared__ Dbl4 sh_p[kRealWarps][32];
     __shared__ Dbl4 sh_f[kRealWarps][32];
+    __shared__ double2 sh_cf[kRealWarps][kMaxCheb64];  // far-piece (T1, T2) coefficients of the current instance
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = min(*nitems_ptr, item_cap);
+    int cur_q = -1;
     while (true) {
         int item = 0;
         if (lane == 0) item = atomicAdd(counter, 1);
@@ -785,6 +787,14 @@ __global__ void __launch_bounds__(kRealWarps * 32)
         const DiffHConsts ke = diffh_consts(a, ee > 0 ? ee : dd, ce);  // used only when eps > 0
         const double rc2 = I.rc * I.rc;
         const double rs2 = (double)T.rs2;
+        const double rf2 = T.rf2, tfs = T.tf_scale, tfo = T.tf_off;
+        const int nf = T.nf;
+        if (it.x != cur_q) {
+            cur_q = it.x;
+            __syncwarp();
+            for (int k = lane; k < kMaxCheb64; k += 32) sh_cf[w][k] = make_double2(T.cf1[k], T.cf2[k]);
+            __syncwarp();
+        }
         ItemFrame F;
         item_frame(I, it, F);
         const bool active = lane < F.count;
@@ -849,6 +859,22 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                         H1 = T.self1;
                                         H2 = 0;
                                     }
+                                } else if (r2 >= rf2) {
+                                    // far: the FP64 Chebyshev series of T1 = r H1, T2 = r^3 H2
+                                    const double r = sqrt(r2), ir = 1.0 / r;
+                                    const double t = fma(r, tfs, tfo), t2 = 2.0 * t;
+                                    double b1x = 0.0, b1y = 0.0, b2x = 0.0, b2y = 0.0;
+                                    for (int k = nf - 1; k >= 1; k--) {
+                                        const double2 c = sh_cf[w][k];
+                                        const double b0x = fma(t2, b1x, c.x - b2x), b0y = fma(t2, b1y, c.y - b2y);
+                                        b2x = b1x;
+                                        b1x = b0x;
+                                        b2y = b1y;
+                                        b1y = b0y;
+                                    }
+                                    const double2 c0 = sh_cf[w][0];
+                                    H1 = fma(t, b1x, c0.x - b2x) * ir;
+                                    H2 = fma(t, b1y, c0.y - b2y) * (ir * ir * ir);
                                 } else {
                                     const double r = sqrt(r2), ir = 1.0 / r;
                                     diffH_fast_d(r, ir, kd, H1, H2);

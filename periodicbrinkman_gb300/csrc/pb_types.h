@@ -25,6 +25,7 @@ __host__ __device__
 constexpr int kMaxPoly = 28;    // max terms of the far polynomial (held in registers)
 constexpr int kMaxCheb = 40;    // max terms of the near and blob Chebyshev series (shared memory)
 constexpr int kNumSeries = 16;  // terms of the FP64 small-r series
+constexpr int kMaxCheb64 = 48;  // max terms of the FP64 far Chebyshev series (FP64 path)
 
 // Per-instance real-space kernel tables (built in FP64 on the host).  The pair
 // kernel H = (R_eps - R_d) inside the blob region, S - R_d outside it, is
@@ -48,6 +49,12 @@ struct PbTables {
     double ser1[kNumSeries], ser2[kNumSeries];
     double self1;   // H1 at r = 0
     double rtiny2;  // r_tiny^2
+    // FP64 path: the far piece (T1, T2 of S - R_d for r in [r_mid, rc]) as an
+    // FP64 Chebyshev series in t = r*tf_scale + tf_off (Clenshaw), fitted to
+    // 1e-14 of its largest coefficient; pairs below r_mid use the closed forms
+    double cf1[kMaxCheb64], cf2[kMaxCheb64];
+    double tf_scale, tf_off, rf2;  // argument map; r_mid^2
+    int nf;
 };
 
 // Per-instance descriptor, resident on the device for multi-instance kernels.
