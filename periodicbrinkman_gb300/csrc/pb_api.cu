@@ -536,7 +536,7 @@ int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved&
                   int cell_off, int max_terms)
 {
     set_inst_fields(P->hinst[q], p, R, src_off, tgt_off, cell_off);
-    int trc = build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, &P->htab[q], max_terms);
+    int trc = build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, &P->htab[q], max_terms, p.precision == PB_PREC_FP64);
     if (trc) return fail(PB_ERR_INVALID, "table construction failed");
     return PB_OK;
 }
@@ -1128,7 +1128,7 @@ int prepare_instance(const pb_solve_params& p, int npoly_cap, PbTables* tab, pb_
     Resolved R;
     int rc = resolve(p, R);
     if (rc) return rc;
-    if (build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, tab, npoly_cap))
+    if (build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, tab, npoly_cap, p.precision == PB_PREC_FP64))
         return fail(PB_ERR_INVALID, "table construction failed");
     fill_info(R, tab->nd, info);
     return PB_OK;

@@ -332,7 +332,8 @@ void fit_chebyshev_pair(const std::function<void(double, double*, double*)>& f, 
     c2.resize(n);
 }
 
-int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t, int max_terms)
+int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t, int max_terms,
+                 bool fp64_far)
 {
     if (max_terms <= 0 || max_terms > kMaxPoly) max_terms = kMaxPoly;
     if (!(a > 0) || !(d > 0) || !(rc > 0) || eps < 0) return -1;
@@ -373,7 +374,7 @@ int build_tables(double a, double d, double eps, double rc, double poly_tol, PbT
         return (int)q1.size();
     };
     t->nn = cheb(Td, r_near, r_mid, t->cn1, t->cn2, &t->tn_scale, &t->tn_off);
-    {
+    if (fp64_far) {
         // the far piece again, in FP64 for the FP64 path's pairs beyond r_mid
         std::vector<double> q1, q2;
         fit_chebyshev_pair(Td, r_far, rc, 96, 1e-14, kMaxCheb64, q1, q2);
@@ -385,6 +386,8 @@ int build_tables(double a, double d, double eps, double rc, double poly_tol, PbT
         t->tf_scale = 2.0 / (rc - r_far);
         t->tf_off = -(rc + r_far) / (rc - r_far);
         t->rf2 = r_mid * r_mid;
+    } else {
+        t->rf2 = HUGE_VAL;  // no FP64 far series: every pair takes the closed forms
     }
     t->rc2 = (float)(rc * rc);
     t->rm2 = (float)(r_mid * r_mid);

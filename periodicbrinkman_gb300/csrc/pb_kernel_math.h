@@ -51,7 +51,9 @@ void fit_chebyshev_pair(const std::function<void(double, double*, double*)>& f, 
 
 // Fill the per-instance real-space tables.  poly_tol: relative truncation of
 // the Chebyshev series (1e-9 keeps ~20 terms); max_terms caps the screened
-// polynomial (<= 0: kMaxPoly).  Returns 0 or an error code.
-int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t, int max_terms = 0);
+// polynomial (<= 0: kMaxPoly); fp64_far: also fit the FP64 far series of
+// the FP64 path (nf = 0 otherwise).  Returns 0 or an error code.
+int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t, int max_terms = 0,
+                 bool fp64_far = true);
 
 }  // namespace pb

@@ -859,7 +859,7 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                         H1 = T.self1;
                                         H2 = 0;
                                     }
-                                } else if (r2 >= rf2) {
+                                } else if (nf > 0 && r2 >= rf2) {
                                     // far: the FP64 Chebyshev series of T1 = r H1, T2 = r^3 H2
                                     const double r = sqrt(r2), ir = 1.0 / r;
                                     const double t = fma(r, tfs, tfo), t2 = 2.0 * t;
