@@ -169,32 +169,26 @@ __global__ void __launch_bounds__(kSpreadWarps * 32)
     const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
     const size_t comp = (size_t)I.M[0] * I.M[1] * I.M[2], M12 = (size_t)I.M[1] * I.M[2];
     const T* g0 = grid + I.grid_off;
-    T s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0;
+    // plain FP64 sums (x rows by FMA, then weighted by the row's y-z weight):
+    // a few hundred same-sign-weighted terms per lane lose ~1e-14, and GB300's
+    // FP64 pipe is the limit here (compensated sums per point cost 4x the work)
+    T s0 = 0, s1 = 0, s2 = 0;
     for (int id = lane; id < P2 * R; id += 32) {
         const int xs = id / P2, yz = id - xs * P2, py = yz / Pz, pz = yz - py * Pz;
         const T wyz = wgt[w][1][py] * wgt[w][2][pz];
         const size_t oyz = (size_t)gidx[w][1][py] * I.M[2] + gidx[w][2][pz];
+        T r0 = 0, r1 = 0, r2 = 0;
         for (int px = xs; px < Px; px += R) {
-            const T wv = wgt[w][0][px] * wyz;
+            const T wx = wgt[w][0][px];
             const size_t o = (size_t)gidx[w][0][px] * M12 + oyz;
-            T v0 = wv * __ldg(g0 + o), v1 = wv * __ldg(g0 + comp + o), v2 = wv * __ldg(g0 + 2 * comp + o);
-            // Kahan: running value s - c
-            T y = v0 - c0, t = s0 + y;
-            c0 = (t - s0) - y;
-            s0 = t;
-            y = v1 - c1;
-            t = s1 + y;
-            c1 = (t - s1) - y;
-            s1 = t;
-            y = v2 - c2;
-            t = s2 + y;
-            c2 = (t - s2) - y;
-            s2 = t;
+            r0 = fma(wx, __ldg(g0 + o), r0);
+            r1 = fma(wx, __ldg(g0 + comp + o), r1);
+            r2 = fma(wx, __ldg(g0 + 2 * comp + o), r2);
         }
+        s0 = fma(wyz, r0, s0);
+        s1 = fma(wyz, r1, s1);
+        s2 = fma(wyz, r2, s2);
     }
-    s0 -= c0;
-    s1 -= c1;
-    s2 -= c2;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         s0 += __shfl_xor_sync(kFull, s0, o);
