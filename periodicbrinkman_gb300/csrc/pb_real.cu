@@ -23,8 +23,11 @@
 // accumulator.  The self pair of targets that are the sources is skipped here
 // and added in FP64 by the combine kernel (R_eps(0) - R_d(0)) f_i.
 //
-// FP64 (k_real_fp64): the reference's closed forms (cuda/periodicBrinkman.h:85-176)
-// in double precision, FP64 series below r_tiny.
+// FP64 (k_real_fp64): beyond r_mid an FP64 Chebyshev series of the screened
+// kernel (fitted on the host to the reference's closed forms), below it the
+// closed forms themselves (cuda/periodicBrinkman.h:85-176) in double precision,
+// FP64 series below r_tiny.  The in-cutoff pairs of each chunk are compacted
+// and evaluated 32 at a time, so the FP64 pipe sees full warps.
 #include "pb_device.cuh"
 #include "pb_kernels.h"
 
@@ -770,6 +773,10 @@ __global__ void __launch_bounds__(kRealWarps * 32)
     __shared__ Dbl4 sh_p[kRealWarps][32];
     __shared__ Dbl4 sh_f[kRealWarps][32];
     __shared__ double2 sh_cf[kRealWarps][kMaxCheb64];  // far-piece (T1, T2) coefficients of the current instance
+    __shared__ Dbl4 sh_t[kRealWarps][32];               // the item's targets
+    __shared__ unsigned short sh_q[kRealWarps][1024];   // in-cutoff pairs of a chunk, target-major (t << 5 | j)
+    __shared__ double sh_v[kRealWarps][3][32];          // one batch's pair contributions
+    __shared__ int sh_tq[kRealWarps][32];               // and their targets
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = min(*nitems_ptr, item_cap);
     int cur_q = -1;
@@ -802,6 +809,8 @@ __global__ void __launch_bounds__(kRealWarps * 32)
         const int self_src = I.same ? tidx - I.tgt_off + I.src_off : -1;
         Dbl4 tp = tpos[tidx];
         if (!active) tp.x = tp.y = tp.z = 3.0e300;  // inactive lanes pair with nothing
+        __syncwarp();
+        sh_t[w][lane] = tp;
         double v0 = 0, v1 = 0, v2 = 0;
         const int ny1 = 2 * I.S[1] + 1, ncol = (2 * I.S[0] + 1) * ny1;
         const int csplit = max(1, I.csplit);
@@ -844,13 +853,30 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                             if (self_src >= base && self_src < base + ncand && zero_shift)
                                 mask &= ~(1u << (self_src - base));
                         }
-                        while (__any_sync(kFull, mask)) {
-                            if (mask) {
-                                int jj = __ffs(mask) - 1;
-                                mask &= mask - 1;
-                                Dbl4 p = sh_p[w][jj], f = sh_f[w][jj];
-                                double dx = tp.x - p.x, dy = tp.y - p.y, dz = tp.z - p.z;
-                                double r2 = dx * dx + dy * dy + dz * dz;
+                        // compact the in-cutoff pairs target-major, then evaluate them 32 at a
+                        // time with every lane busy (the FP64 pipe issues a warp instruction
+                        // whatever the number of active lanes); lane t sums target t's entries
+                        const int cnt = __popc(mask);
+                        const int qoff = warp_excl_scan(cnt, lane);
+                        const int total = __shfl_sync(kFull, qoff + cnt, 31);
+                        for (int k = qoff; mask; k++) {
+                            const int jj = __ffs(mask) - 1;
+                            mask &= mask - 1;
+                            sh_q[w][k] = (unsigned short)((lane << 5) | jj);
+                        }
+                        __syncwarp();
+                        for (int qb = 0; qb < total; qb += 32) {
+                            const int qi = qb + lane;
+                            double c0 = 0.0, c1 = 0.0, c2 = 0.0;
+                            int tq = -1;
+                            if (qi < total) {
+                                const int ent = sh_q[w][qi];
+                                tq = ent >> 5;
+                                const int jj = ent & 31;
+                                const Dbl4 tt = sh_t[w][tq];
+                                const Dbl4 p = sh_p[w][jj], f = sh_f[w][jj];
+                                const double dx = tt.x - p.x, dy = tt.y - p.y, dz = tt.z - p.z;
+                                const double r2 = dx * dx + dy * dy + dz * dz;
                                 double H1, H2;
                                 if (r2 < T.rtiny2 || r2 == 0.0) {
                                     if (T.blob) {
@@ -872,9 +898,9 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                         b2y = b1y;
                                         b1y = b0y;
                                     }
-                                    const double2 c0 = sh_cf[w][0];
-                                    H1 = fma(t, b1x, c0.x - b2x) * ir;
-                                    H2 = fma(t, b1y, c0.y - b2y) * (ir * ir * ir);
+                                    const double2 cc = sh_cf[w][0];
+                                    H1 = fma(t, b1x, cc.x - b2x) * ir;
+                                    H2 = fma(t, b1y, cc.y - b2y) * (ir * ir * ir);
                                 } else {
                                     const double r = sqrt(r2), ir = 1.0 / r;
                                     diffH_fast_d(r, ir, kd, H1, H2);
@@ -885,11 +911,24 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                         H2 -= e2;
                                     }
                                 }
-                                double fd = f.x * dx + f.y * dy + f.z * dz;
-                                v0 += H1 * f.x + H2 * fd * dx;
-                                v1 += H1 * f.y + H2 * fd * dy;
-                                v2 += H1 * f.z + H2 * fd * dz;
+                                const double fd = f.x * dx + f.y * dy + f.z * dz;
+                                c0 = H1 * f.x + H2 * fd * dx;
+                                c1 = H1 * f.y + H2 * fd * dy;
+                                c2 = H1 * f.z + H2 * fd * dz;
                             }
+                            sh_v[w][0][lane] = c0;
+                            sh_v[w][1][lane] = c1;
+                            sh_v[w][2][lane] = c2;
+                            sh_tq[w][lane] = tq;
+                            __syncwarp();
+                            const int nb = min(32, total - qb);
+                            for (int i = 0; i < nb; i++)
+                                if (sh_tq[w][i] == lane) {
+                                    v0 += sh_v[w][0][i];
+                                    v1 += sh_v[w][1][i];
+                                    v2 += sh_v[w][2][i];
+                                }
+                            __syncwarp();
                         }
                         __syncwarp();
                     }
