@@ -887,7 +887,7 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                     }
                                 } else if (nf > 0 && r2 >= rf2) {
                                     // far: the FP64 Chebyshev series of T1 = r H1, T2 = r^3 H2
-                                    const double r = sqrt(r2), ir = 1.0 / r;
+                                    const double ir = rsqrt(r2), r = r2 * ir;
                                     const double t = fma(r, tfs, tfo), t2 = 2.0 * t;
                                     double b1x = 0.0, b1y = 0.0, b2x = 0.0, b2y = 0.0;
                                     for (int k = nf - 1; k >= 1; k--) {
