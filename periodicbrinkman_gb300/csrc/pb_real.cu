@@ -775,8 +775,7 @@ __global__ void __launch_bounds__(kRealWarps * 32)
     __shared__ double2 sh_cf[kRealWarps][kMaxCheb64];  // far-piece (T1, T2) coefficients of the current instance
     __shared__ Dbl4 sh_t[kRealWarps][32];               // the item's targets
     __shared__ unsigned short sh_q[kRealWarps][1024];   // in-cutoff pairs of a chunk, target-major (t << 5 | j)
-    __shared__ double sh_v[kRealWarps][3][32];          // one batch's pair contributions
-    __shared__ int sh_tq[kRealWarps][32];               // and their targets
+    __shared__ double sh_v[kRealWarps][3][32];          // one batch's sums per target
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = min(*nitems_ptr, item_cap);
     int cur_q = -1;
@@ -855,7 +854,7 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                         }
                         // compact the in-cutoff pairs target-major, then evaluate them 32 at a
                         // time with every lane busy (the FP64 pipe issues a warp instruction
-                        // whatever the number of active lanes); lane t sums target t's entries
+                        // whatever the number of active lanes)
                         const int cnt = __popc(mask);
                         const int qoff = warp_excl_scan(cnt, lane);
                         const int total = __shfl_sync(kFull, qoff + cnt, 31);
@@ -916,18 +915,33 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                 c1 = H1 * f.y + H2 * fd * dy;
                                 c2 = H1 * f.z + H2 * fd * dz;
                             }
-                            sh_v[w][0][lane] = c0;
-                            sh_v[w][1][lane] = c1;
-                            sh_v[w][2][lane] = c2;
-                            sh_tq[w][lane] = tq;
-                            __syncwarp();
-                            const int nb = min(32, total - qb);
-                            for (int i = 0; i < nb; i++)
-                                if (sh_tq[w][i] == lane) {
-                                    v0 += sh_v[w][0][i];
-                                    v1 += sh_v[w][1][i];
-                                    v2 += sh_v[w][2][i];
+                            // the batch is target-major: sum each target's contiguous run by a
+                            // segmented scan, then its last lane hands the sum to the target's lane
+#pragma unroll
+                            for (int o = 1; o < 32; o <<= 1) {
+                                const double u0 = __shfl_up_sync(kFull, c0, o), u1 = __shfl_up_sync(kFull, c1, o),
+                                             u2 = __shfl_up_sync(kFull, c2, o);
+                                const int tu = __shfl_up_sync(kFull, tq, o);
+                                if (lane >= o && tu == tq) {
+                                    c0 += u0;
+                                    c1 += u1;
+                                    c2 += u2;
                                 }
+                            }
+                            const int tn = __shfl_down_sync(kFull, tq, 1);
+                            const bool last = tq >= 0 && (lane == 31 || tn != tq);
+                            if (last) {
+                                sh_v[w][0][tq] = c0;
+                                sh_v[w][1][tq] = c1;
+                                sh_v[w][2][tq] = c2;
+                            }
+                            const unsigned tmask = __reduce_or_sync(kFull, last ? 1u << tq : 0u);
+                            __syncwarp();
+                            if ((tmask >> lane) & 1u) {
+                                v0 += sh_v[w][0][lane];
+                                v1 += sh_v[w][1][lane];
+                                v2 += sh_v[w][2][lane];
+                            }
                             __syncwarp();
                         }
                         __syncwarp();
