@@ -239,6 +239,10 @@ const char* pb_version(void);
  * (FP32 Horner), for testing the tables without a GPU. */
 int pb_debug_pair_kernel(double alpha, double d, double eps, double rc, int n, const double* r, double* H1,
                          double* H2);
+/* The same for the FP64 path: its FP64 Chebyshev far series beyond r_mid,
+ * the closed forms below it, evaluated on the host as the GPU does. */
+int pb_debug_pair_kernel64(double alpha, double d, double eps, double rc, int n, const double* r, double* H1,
+                           double* H2);
 /* Number of CUDA devices visible (0 without a GPU). */
 int pb_device_count(void);
 

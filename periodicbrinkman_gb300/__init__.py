@@ -31,7 +31,8 @@ from ._lib import (  # noqa: F401
     lib,
     lib_path,
 )
-from .api import Plan, Server, fftBrinkman, pair_kernel_tables, periodicBrinkman, solve, shell_counts  # noqa: F401
+from .api import (Plan, Server, fftBrinkman, pair_kernel_tables, pair_kernel_tables64, periodicBrinkman,  # noqa: F401
+                  shell_counts, solve)
 
 __all__ = [
     "PbError",
@@ -43,6 +44,7 @@ __all__ = [
     "solve",
     "shell_counts",
     "pair_kernel_tables",
+    "pair_kernel_tables64",
     "device_count",
     "lib",
     "lib_path",

@@ -169,6 +169,7 @@ def lib():
     L.pb_plan_stage_ms.argtypes = [vp, dp]
     L.pb_plan_destroy.argtypes = [vp]
     L.pb_debug_pair_kernel.argtypes = [C.c_double] * 4 + [C.c_int, dp, dp, dp]
+    L.pb_debug_pair_kernel64.argtypes = [C.c_double] * 4 + [C.c_int, dp, dp, dp]
     L.pb_plan_create_slot.argtypes = [C.POINTER(SlotConfig), C.POINTER(vp)]
     L.pb_slot_estimate_bytes.restype = C.c_longlong
     L.pb_slot_estimate_bytes.argtypes = [C.POINTER(SlotConfig)]

@@ -367,6 +367,17 @@ def shell_counts(L, M: int, N: int):
     return Mx, Nx
 
 
+def pair_kernel_tables64(alpha: float, d: float, eps: float, rc: float, r) -> tuple[np.ndarray, np.ndarray]:
+    """H1(r), H2(r) of the FP64 path (FP64 far series beyond r_mid, closed forms
+    below), evaluated on the host as the GPU does."""
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    h1 = np.zeros_like(r)
+    h2 = np.zeros_like(r)
+    check(lib().pb_debug_pair_kernel64(alpha, d, eps, rc, r.size, r.ctypes.data_as(_dp), h1.ctypes.data_as(_dp),
+                                       h2.ctypes.data_as(_dp)))
+    return h1, h2
+
+
 def pair_kernel_tables(alpha: float, d: float, eps: float, rc: float, r) -> tuple[np.ndarray, np.ndarray]:
     """H1(r), H2(r) of the FP32 polynomial tables, evaluated on the host as the
     GPU does (for testing the tables without a GPU)."""

@@ -1433,6 +1433,55 @@ int pb_fft_brinkman(double* U, const double* y, int m_tgt, const double* f, cons
     return pb_solve(&p, xn, f, y, U, PB_HOST, nullptr);
 }
 
+int pb_debug_pair_kernel64(double alpha, double d, double eps, double rc, int n, const double* r, double* H1,
+                           double* H2)
+{
+    PbTables T;
+    if (build_tables(alpha, d, eps, rc, 1e-9, &T, 0, true)) return fail(PB_ERR_INVALID, "bad kernel parameters");
+    for (int i = 0; i < n; i++) {
+        const double ri = r[i], r2 = ri * ri;
+        if (r2 < T.rtiny2 || r2 == 0.0) {  // the FP64 small-r series (eps > 0) or the r -> 0 limit
+            double s1 = 0, s2 = 0;
+            if (T.blob) {
+                s1 = T.ser1[kNumSeries - 1];
+                s2 = T.ser2[kNumSeries - 1];
+                for (int m = kNumSeries - 2; m >= 0; m--) {
+                    s1 = std::fma(s1, r2, T.ser1[m]);
+                    s2 = std::fma(s2, r2, T.ser2[m]);
+                }
+            } else {
+                s1 = T.self1;
+            }
+            H1[i] = s1;
+            H2[i] = s2;
+        } else if (T.nf > 0 && r2 >= T.rf2) {  // the FP64 far series, by the GPU's Clenshaw recurrence
+            const double t = std::fma(ri, T.tf_scale, T.tf_off), t2 = 2.0 * t;
+            double b1x = 0, b1y = 0, b2x = 0, b2y = 0;
+            for (int k = T.nf - 1; k >= 1; k--) {
+                const double b0x = std::fma(t2, b1x, T.cf1[k] - b2x), b0y = std::fma(t2, b1y, T.cf2[k] - b2y);
+                b2x = b1x;
+                b1x = b0x;
+                b2y = b1y;
+                b1y = b0y;
+            }
+            H1[i] = std::fma(t, b1x, T.cf1[0] - b2x) / ri;
+            H2[i] = std::fma(t, b1y, T.cf2[0] - b2y) / (r2 * ri);
+        } else {  // the closed forms, as the GPU's FP64 kernel evaluates them there
+            double h1 = 0, h2 = 0;
+            diffH_closed(ri, alpha, d, &h1, &h2);
+            if (T.blob && r2 < (double)T.rs2) {
+                double e1, e2;
+                diffH_closed(ri, alpha, eps, &e1, &e2);
+                h1 -= e1;
+                h2 -= e2;
+            }
+            H1[i] = h1;
+            H2[i] = h2;
+        }
+    }
+    return PB_OK;
+}
+
 int pb_debug_pair_kernel(double alpha, double d, double eps, double rc, int n, const double* r, double* H1,
                          double* H2)
 {

@@ -71,6 +71,24 @@ def test_resolved_parameters_are_a_fixed_point(n, L, a, e, M):
     assert r2 == r
 
 
+def test_fp64_kernel_tables_match_oracle():
+    # the FP64 path's pair kernel (FP64 far series beyond r_mid, closed forms
+    # below) vs the oracle's accurate kernel, relative to the largest |H| term
+    for a, d, e, rc in [(20, 0.015, 0.005, 0.0707), (10, 0.125, 0.01, 0.6), (3, 0.05, 0.0, 0.25), (45, 0.02, 0.002, 0.1)]:
+        r = np.linspace(0, rc, 1201)[1:-1]
+        h1, h2 = pb.pair_kernel_tables64(a, d, e, rc, r)
+        ex = np.array([oracle.pair_H(rr, a, d, e) for rr in r])
+        t1, t2 = np.abs(ex[:, 0]), np.abs(ex[:, 1]) * r * r
+        err = (np.abs(h1 - ex[:, 0]) + np.abs(h2 - ex[:, 1]) * r * r) / max(t1.max(), t2.max())
+        far = r >= 0.25 * rc
+        assert err[far].max() < 1e-11, (a, d, e, err[far].max())
+        # closer in: the closed forms of the reference, which cancel as r -> 0
+        # when eps = 0 (S - R_d, both singular); with eps > 0 the FP64 series
+        # takes over below 0.8 eps
+        near = r >= (0.05 * d if e == 0 else 0.0)
+        assert err[near].max() < 1e-9, (a, d, e, err[near].max())
+
+
 def test_kernel_tables_match_oracle():
     # FP32 polynomial tables evaluated as on the GPU vs the FP64 oracle kernel
     for a, d, e, rc in [(10, 0.125, 0.01, 0.35), (20, 0.02, 0.005, 0.08), (1, 0.05, 0.005, 0.2), (3, 0.1, 0.0, 0.4)]:
