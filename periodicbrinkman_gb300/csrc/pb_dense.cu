@@ -6,14 +6,17 @@
 // in FP64 with the reference's per-axis shell counts.  One warp per (i, j)
 // pair; lanes stride over images and wave vectors, the nine tensor sums are
 // reduced with warp shuffles.  The phase e^{i k.x} is built from per-axis
-// tables e^{i l theta_a} held in shared memory.
+// tables e^{i l theta_a} held in shared memory; the pair-independent factor
+// of each wave vector (its Gaussian, the Brinkman denominator and 1/tau) is
+// computed once per block into a shared tile that all the block's pairs read.
 #include "pb_device.cuh"
 #include "pb_kernels.h"
 
 namespace pb {
 
-constexpr int kDenseWarps = 4;
+constexpr int kDenseWarps = 8;
 constexpr int kDenseMaxN = 256;  // max Fourier shells per axis
+constexpr int kDenseKT = 1024;   // wave vectors per shared tile
 
 struct DenseArgs {
     double a, d, e, c_d, c_e, tau_inv;
@@ -28,9 +31,13 @@ __global__ void __launch_bounds__(kDenseWarps * 32)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int tab_len = (2 * A.Nx[0] + 1) + (2 * A.Nx[1] + 1) + (2 * A.Nx[2] + 1);
-    double2* tab = (double2*)smem_raw + (size_t)w * tab_len;
+    double* kg = (double*)smem_raw;                      // [kDenseKT] factor of each wave vector of the tile
+    int* kl = (int*)(kg + kDenseKT);                     // [kDenseKT] its shell indices, 10 bits each
+    double2* tab = (double2*)(kl + kDenseKT) + (size_t)w * tab_len;
     long long pair = (long long)blockIdx.x * kDenseWarps + w;
-    if (pair >= (long long)A.m * A.n) return;
+    // warps past the last pair still take part in the block's k tiles
+    const bool live = pair < (long long)A.m * A.n;
+    if (!live) pair = 0;
     const int i = (int)(pair % A.m), j = (int)(pair / A.m);
     double xh0[3];
     for (int q = 0; q < 3; q++) xh0[q] = dx[3 * (size_t)i + q] - dx0[3 * (size_t)j + q];
@@ -39,7 +46,7 @@ __global__ void __launch_bounds__(kDenseWarps * 32)
     // real-space images (cuda/periodicBrinkman.h:265-282)
     const int n0 = 2 * A.Mx[0] + 1, n1 = 2 * A.Mx[1] + 1, n2 = 2 * A.Mx[2] + 1;
     const int nimg = (A.Mx[0] >= 0) ? n0 * n1 * n2 : 0;
-    for (int t = lane; t < nimg; t += 32) {
+    for (int t = lane; t < (live ? nimg : 0); t += 32) {
         int l1 = t % n0 - A.Mx[0];
         int l2 = (t / n0) % n1 - A.Mx[1];
         int l3 = t / (n0 * n1) - A.Mx[2];
@@ -101,30 +108,43 @@ __global__ void __launch_bounds__(kDenseWarps * 32)
         const double a1 = -expm1(-x / 4), a0 = x + 6 * a1;
         const long long m0 = 2 * N0 + 1, m1 = 2 * N1 + 1, m2 = 2 * N2 + 1;
         const long long nk = m0 * m1 * m2;
-        for (long long t = lane; t < nk; t += 32) {
-            int l1 = (int)(t % m0) - N0;
-            int l2 = (int)((t / m0) % m1) - N1;
-            int l3 = (int)(t / (m0 * m1)) - N2;
-            if (l1 == 0 && l2 == 0 && l3 == 0) continue;
-            double k0 = 2 * kPiD * l1 / A.L[0], k1 = 2 * kPiD * l2 / A.L[1], k2 = 2 * kPiD * l3 / A.L[2];
-            double kn = k0 * k0 + k1 * k1 + k2 * k2;
-            double wv = A.d * A.d * kn;
-            double2 e0 = t0[l1 + N0], e1 = t1[l2 + N1], e2 = t2[l3 + N2];
-            double pr = e0.x * e1.x - e0.y * e1.y, pi = e0.x * e1.y + e0.y * e1.x;
-            double cosv = pr * e2.x - pi * e2.y;
-            double bhat = 1 / x * (a1 * (wv - 6) + a0) * exp(-wv / 4) * cosv / (kn * (kn + A.a * A.a)) * A.tau_inv;
-            s[0] += (k1 * k1 + k2 * k2) * bhat;
-            s[1] += (k0 * k0 + k2 * k2) * bhat;
-            s[2] += (k0 * k0 + k1 * k1) * bhat;
-            s[3] -= k0 * k1 * bhat;
-            s[4] -= k0 * k2 * bhat;
-            s[5] -= k1 * k2 * bhat;
+        const double w0 = 2 * kPiD / A.L[0], w1 = 2 * kPiD / A.L[1], w2 = 2 * kPiD / A.L[2];
+        for (long long kb = 0; kb < nk; kb += kDenseKT) {
+            const int cnt = (int)min((long long)kDenseKT, nk - kb);
+            __syncthreads();  // the previous tile is consumed
+            for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+                const long long t = kb + q;
+                const int l1 = (int)(t % m0) - N0, l2 = (int)((t / m0) % m1) - N1, l3 = (int)(t / (m0 * m1)) - N2;
+                const double k0 = w0 * l1, k1 = w1 * l2, k2 = w2 * l3;
+                const double kn = k0 * k0 + k1 * k1 + k2 * k2;
+                const double wv = A.d * A.d * kn;
+                kg[q] = (l1 == 0 && l2 == 0 && l3 == 0)
+                            ? 0.0
+                            : (a1 * (wv - 6) + a0) * exp(-wv / 4) / (x * kn * (kn + A.a * A.a)) * A.tau_inv;
+                kl[q] = (l1 + N0) | ((l2 + N1) << 10) | ((l3 + N2) << 20);
+            }
+            __syncthreads();
+            if (!live) continue;
+            for (int q = lane; q < cnt; q += 32) {
+                const int pk = kl[q];
+                const int i1 = pk & 1023, i2 = (pk >> 10) & 1023, i3 = pk >> 20;
+                const double k0 = w0 * (i1 - N0), k1 = w1 * (i2 - N1), k2 = w2 * (i3 - N2);
+                const double2 e0 = t0[i1], e1 = t1[i2], e2 = t2[i3];
+                const double pr = e0.x * e1.x - e0.y * e1.y, pi = e0.x * e1.y + e0.y * e1.x;
+                const double bhat = kg[q] * (pr * e2.x - pi * e2.y);
+                s[0] += (k1 * k1 + k2 * k2) * bhat;
+                s[1] += (k0 * k0 + k2 * k2) * bhat;
+                s[2] += (k0 * k0 + k1 * k1) * bhat;
+                s[3] -= k0 * k1 * bhat;
+                s[4] -= k0 * k2 * bhat;
+                s[5] -= k1 * k2 * bhat;
+            }
         }
     }
 #pragma unroll
     for (int q = 0; q < 6; q++)
         for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_xor_sync(kFull, s[q], o);
-    if (lane == 0) {
+    if (lane == 0 && live) {
         const size_t ld = 3 * (size_t)A.m;
         double blk[3][3] = {{s[0], s[3], s[4]}, {s[3], s[1], s[5]}, {s[4], s[5], s[2]}};
         for (int c = 0; c < 3; c++)
@@ -153,7 +173,7 @@ int launch_dense_matrix(double* dA, const double* dx, int m, const double* dx0, 
     A.m = m;
     A.n = n;
     int tab_len = (2 * A.Nx[0] + 1) + (2 * A.Nx[1] + 1) + (2 * A.Nx[2] + 1);
-    size_t smem = (size_t)kDenseWarps * tab_len * sizeof(double2);
+    size_t smem = (size_t)kDenseKT * (sizeof(double) + sizeof(int)) + (size_t)kDenseWarps * tab_len * sizeof(double2);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     long long pairs = (long long)m * n;
     unsigned blocks = (unsigned)((pairs + kDenseWarps - 1) / kDenseWarps);
