@@ -16,7 +16,7 @@ namespace pb {
 
 constexpr int kDenseWarps = 8;
 constexpr int kDenseMaxN = 256;  // max Fourier shells per axis
-constexpr int kDenseKT = 1024;   // wave vectors per shared tile
+constexpr int kDenseKT = 512;    // wave vectors per shared tile
 
 struct DenseArgs {
     double a, d, e, c_d, c_e, tau_inv;
@@ -31,8 +31,10 @@ __global__ void __launch_bounds__(kDenseWarps * 32)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int tab_len = (2 * A.Nx[0] + 1) + (2 * A.Nx[1] + 1) + (2 * A.Nx[2] + 1);
-    double* kg = (double*)smem_raw;                      // [kDenseKT] factor of each wave vector of the tile
-    int* kl = (int*)(kg + kDenseKT);                     // [kDenseKT] its shell indices, 10 bits each
+    // per wave vector of the tile: its factor times the six entries of
+    // k^2 I - k k^T (xx, yy, zz, xy, xz, yz), and its shell indices (10 bits each)
+    double2* kg = (double2*)smem_raw;                    // [3][kDenseKT]
+    int* kl = (int*)(kg + 3 * kDenseKT);                 // [kDenseKT]
     double2* tab = (double2*)(kl + kDenseKT) + (size_t)w * tab_len;
     long long pair = (long long)blockIdx.x * kDenseWarps + w;
     // warps past the last pair still take part in the block's k tiles
@@ -118,9 +120,12 @@ __global__ void __launch_bounds__(kDenseWarps * 32)
                 const double k0 = w0 * l1, k1 = w1 * l2, k2 = w2 * l3;
                 const double kn = k0 * k0 + k1 * k1 + k2 * k2;
                 const double wv = A.d * A.d * kn;
-                kg[q] = (l1 == 0 && l2 == 0 && l3 == 0)
-                            ? 0.0
-                            : (a1 * (wv - 6) + a0) * exp(-wv / 4) / (x * kn * (kn + A.a * A.a)) * A.tau_inv;
+                const double g = (l1 == 0 && l2 == 0 && l3 == 0)
+                                     ? 0.0
+                                     : (a1 * (wv - 6) + a0) * exp(-wv / 4) / (x * kn * (kn + A.a * A.a)) * A.tau_inv;
+                kg[q] = make_double2((k1 * k1 + k2 * k2) * g, (k0 * k0 + k2 * k2) * g);
+                kg[kDenseKT + q] = make_double2((k0 * k0 + k1 * k1) * g, -k0 * k1 * g);
+                kg[2 * kDenseKT + q] = make_double2(-k0 * k2 * g, -k1 * k2 * g);
                 kl[q] = (l1 + N0) | ((l2 + N1) << 10) | ((l3 + N2) << 20);
             }
             __syncthreads();
@@ -128,16 +133,16 @@ __global__ void __launch_bounds__(kDenseWarps * 32)
             for (int q = lane; q < cnt; q += 32) {
                 const int pk = kl[q];
                 const int i1 = pk & 1023, i2 = (pk >> 10) & 1023, i3 = pk >> 20;
-                const double k0 = w0 * (i1 - N0), k1 = w1 * (i2 - N1), k2 = w2 * (i3 - N2);
                 const double2 e0 = t0[i1], e1 = t1[i2], e2 = t2[i3];
                 const double pr = e0.x * e1.x - e0.y * e1.y, pi = e0.x * e1.y + e0.y * e1.x;
-                const double bhat = kg[q] * (pr * e2.x - pi * e2.y);
-                s[0] += (k1 * k1 + k2 * k2) * bhat;
-                s[1] += (k0 * k0 + k2 * k2) * bhat;
-                s[2] += (k0 * k0 + k1 * k1) * bhat;
-                s[3] -= k0 * k1 * bhat;
-                s[4] -= k0 * k2 * bhat;
-                s[5] -= k1 * k2 * bhat;
+                const double cv = pr * e2.x - pi * e2.y;  // cos(k . x)
+                const double2 g01 = kg[q], g23 = kg[kDenseKT + q], g45 = kg[2 * kDenseKT + q];
+                s[0] = fma(g01.x, cv, s[0]);
+                s[1] = fma(g01.y, cv, s[1]);
+                s[2] = fma(g23.x, cv, s[2]);
+                s[3] = fma(g23.y, cv, s[3]);
+                s[4] = fma(g45.x, cv, s[4]);
+                s[5] = fma(g45.y, cv, s[5]);
             }
         }
     }
@@ -173,7 +178,7 @@ int launch_dense_matrix(double* dA, const double* dx, int m, const double* dx0, 
     A.m = m;
     A.n = n;
     int tab_len = (2 * A.Nx[0] + 1) + (2 * A.Nx[1] + 1) + (2 * A.Nx[2] + 1);
-    size_t smem = (size_t)kDenseKT * (sizeof(double) + sizeof(int)) + (size_t)kDenseWarps * tab_len * sizeof(double2);
+    size_t smem = (size_t)kDenseKT * (3 * sizeof(double2) + sizeof(int)) + (size_t)kDenseWarps * tab_len * sizeof(double2);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     long long pairs = (long long)m * n;
     unsigned blocks = (unsigned)((pairs + kDenseWarps - 1) / kDenseWarps);
