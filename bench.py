@@ -64,6 +64,18 @@ REAL_DRAM_BYTES = 7.57e6
 KSPACE_DRAM_BYTES = 250.9e6
 
 
+def max_over_ranks(v, dist, device="cuda"):
+    """The largest value of v over all ranks (v itself without a process group):
+    whole-job times are the slowest rank's."""
+    if dist is None:
+        return float(v)
+    import torch
+
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
 def peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
@@ -227,11 +239,7 @@ def run_serve(args, w, rank, world, dist, torch):
     st1 = srv.stats()
     launches = st1["kernels"] - k_before
     sched_busy = st1["scheduler_busy_s"] - st0["scheduler_busy_s"]
-    t_tot = float(np.sum(step_s))
-    if dist:
-        tt = torch.tensor([t_tot], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_tot = float(tt[0])
+    t_tot = max_over_ranks(float(np.sum(step_s)), dist)
     value = world * args.steps * step_req / t_tot
     stats = srv.stats()
     # open-loop latency under the stream's Poisson arrivals (first 6000 requests, 3 s)
@@ -593,6 +601,8 @@ def main():
     if args.workload == "batch":
         w = BATCH
         r = run_batch(args, torch, local)
+        r["t_dev"] = max_over_ranks(r["t_dev"], dist)
+        r["value"] = w["count"] * args.steps / r["t_dev"]
         if rank != 0:
             return
         line = {"metric": METRIC, "value": r["value"] * world, "unit": "solves/s", "n_gpus": world,
@@ -611,6 +621,8 @@ def main():
         w = CLUSTERED if args.workload == "clustered" else SINGLE_FP64
         r = run_single(args, torch, local, w, clustered_inputs if args.workload == "clustered" else single_inputs,
                        nerr=16)
+        r["t_dev"] = max_over_ranks(r["t_dev"], dist)
+        r["value"] = args.steps / r["t_dev"]
         if rank != 0:
             return
         info = r["info"]
@@ -631,6 +643,8 @@ def main():
     roof, stages, info = roofline_single(torch, local)
     if args.workload == "single":
         r = run_single(args, torch, local)
+        r["t_dev"] = max_over_ranks(r["t_dev"], dist)
+        r["value"] = args.steps / r["t_dev"]
         if rank != 0:
             return
         w = SINGLE
