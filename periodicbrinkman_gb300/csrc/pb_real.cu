@@ -774,6 +774,7 @@ __global__ void __launch_bounds__(kRealWarps * 32)
     __shared__ Dbl4 sh_f[kRealWarps][32];
     __shared__ double2 sh_cf[kRealWarps][kMaxCheb64];  // far-piece (T1, T2) coefficients of the current instance
     __shared__ Dbl4 sh_t[kRealWarps][32];               // the item's targets
+    __shared__ float4 sh_pf[kRealWarps][32];            // staged sources rounded to FP32 (classification)
     __shared__ unsigned short sh_q[kRealWarps][1024];   // in-cutoff pairs of a chunk, target-major (t << 5 | j)
     __shared__ double sh_v[kRealWarps][3][32];          // one batch's sums per target
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -810,6 +811,14 @@ __global__ void __launch_bounds__(kRealWarps * 32)
         if (!active) tp.x = tp.y = tp.z = 3.0e300;  // inactive lanes pair with nothing
         __syncwarp();
         sh_t[w][lane] = tp;
+        // candidates are classified in FP32 against a cutoff widened by the
+        // rounding of the shifted positions (|value| <= 3 L: at most 2^-24 x 3L
+        // per coordinate, under 16 x 2^-24 L over a displacement vector) and of
+        // the FP32 arithmetic; pairs the FP64 distance puts beyond rc add nothing
+        const float tpx = (float)tp.x, tpy = (float)tp.y, tpz = (float)tp.z;
+        const double lmax = fmax(I.L[0], fmax(I.L[1], I.L[2]));
+        const double rcw = I.rc + 16.0 * lmax * 5.9604644775390625e-8;
+        const float rcf2 = (float)(rcw * rcw * (1.0 + 1e-6));
         double v0 = 0, v1 = 0, v2 = 0;
         const int ny1 = 2 * I.S[1] + 1, ncol = (2 * I.S[0] + 1) * ny1;
         const int csplit = max(1, I.csplit);
@@ -837,6 +846,7 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                         if (j < e) {
                             Dbl4 p = spos[j];
                             sh_p[w][lane] = make_dbl4(p.x + sh0, p.y + sh1, p.z + sh2, 0.0);
+                            sh_pf[w][lane] = make_float4((float)(p.x + sh0), (float)(p.y + sh1), (float)(p.z + sh2), 0.f);
                             sh_f[w][lane] = sfrc[j];
                         }
                         __syncwarp();
@@ -844,10 +854,10 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                         unsigned mask = 0;
                         if (active) {
                             for (int jj = 0; jj < ncand; jj++) {
-                                Dbl4 p = sh_p[w][jj];
-                                double dx = tp.x - p.x, dy = tp.y - p.y, dz = tp.z - p.z;
-                                double r2 = dx * dx + dy * dy + dz * dz;
-                                mask |= (r2 < rc2 ? 1u : 0u) << jj;
+                                const float4 p = sh_pf[w][jj];
+                                const float dx = tpx - p.x, dy = tpy - p.y, dz = tpz - p.z;
+                                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                                mask |= (r2 < rcf2 ? 1u : 0u) << jj;
                             }
                             if (self_src >= base && self_src < base + ncand && zero_shift)
                                 mask &= ~(1u << (self_src - base));
@@ -876,8 +886,10 @@ __global__ void __launch_bounds__(kRealWarps * 32)
                                 const Dbl4 p = sh_p[w][jj], f = sh_f[w][jj];
                                 const double dx = tt.x - p.x, dy = tt.y - p.y, dz = tt.z - p.z;
                                 const double r2 = dx * dx + dy * dy + dz * dz;
-                                double H1, H2;
-                                if (r2 < T.rtiny2 || r2 == 0.0) {
+                                double H1 = 0.0, H2 = 0.0;
+                                if (r2 >= rc2) {
+                                    // beyond the cutoff in FP64 (kept by the widened FP32 test)
+                                } else if (r2 < T.rtiny2 || r2 == 0.0) {
                                     if (T.blob) {
                                         series_H(T, r2, H1, H2);
                                     } else {
