@@ -58,10 +58,13 @@ CLUSTERED = dict(name="clustered_N1e6_200clusters_sigma0.02_L2_alpha5_eps0.002_g
 BATCH = dict(name="batch_512_instances_N_logU100-2e4_L_U0.5-2_alpha_logU1-50_eps0.01L_tol1e-6_mixed", count=512,
              nmin=100, nmax=20000, seed=4000)
 METRIC = "Brinkman solves/s + p50/p99 latency at <=1e-6 rel err, served vs plain FP64"
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_real_mixed launch of the N = 1e5 solve
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the N = 1e5 solve's
+# kernels, taken from a separate ncu capture of the same code (not measured by this run); reported
+# with that label as `traffic`
 REAL_DRAM_BYTES = 7.57e6
-# the same for the k-space kernels of that solve (spread 77.7 MB, five FFT passes 136.4 MB, gather 36.8 MB)
+# the k-space kernels of that solve (spread 77.7 MB, five FFT passes 136.4 MB, gather 36.8 MB)
 KSPACE_DRAM_BYTES = 250.9e6
+TRAFFIC_SOURCE = "ncu dram read+write bytes per launch from a separate capture of this workload, not this run"
 
 
 def max_over_ranks(v, dist, device="cuda"):
@@ -179,6 +182,52 @@ def serve_server(w):
                   grids=(16, 32, 64, 128, 256), max_src=w["nmax"], max_tgt=w["nmax"] // 2 + 1)
 
 
+def grid_class(w, n, alpha, eps, tol, grids=(16, 32, 64, 128, 256)):
+    """The provisioned grid a request of the stream is served on (autotuner, host only)."""
+    from periodicbrinkman_gb300.api import make_params, resolve
+
+    M = max(resolve(make_params(n, 1.0, alpha, eps, n_tgt=n // 2, tol=tol, precision="mixed"))["M"])
+    return next((g for g in grids if g >= M), grids[-1])
+
+
+def serve_accuracy(w, pool, N, alpha, eps, tol, per_class=3, ntgt=64, scan=4000):
+    """Max and RMS relative error of served requests against the FP64 oracle:
+    `per_class` requests of every grid class of the stream (the first ones of
+    the stream in that class), `ntgt` seeded targets each (all targets when
+    fewer), per class and per tolerance."""
+    import oracle
+
+    srv = serve_server(dict(w, budget=24 << 30))
+    rng = np.random.default_rng(9)
+    picked = {}
+    for k in range(min(scan, len(N))):
+        g = grid_class(w, int(N[k]), float(alpha[k]), float(eps[k]), float(tol[k]))
+        if len(picked.setdefault(g, [])) < per_class:
+            picked[g].append(k)
+    by_grid, by_tol = {}, {}
+    for g, ks in sorted(picked.items()):
+        for k in ks:
+            x, f, y = pool.get(k, int(N[k]))
+            t = srv.submit(x, f, 1.0, float(alpha[k]), float(eps[k]), y=y, tol=float(tol[k]))
+            U, _ = srv.result(t, timeout=600)
+            sel = np.sort(rng.choice(y.shape[0], min(ntgt, y.shape[0]), replace=False))
+            ref = oracle.ewald_velocity(y[sel], x, f, 1.0, float(alpha[k]), float(eps[k]))
+            mx, rms = oracle.rel_errors(U[sel], ref)
+            for key, dct in ((str(g), by_grid), (f"tol{tol[k]:g}", by_tol)):
+                e = dct.setdefault(key, {"max": 0.0, "rms": 0.0, "requests": 0, "N": []})
+                e["max"] = max(e["max"], mx)
+                e["rms"] = max(e["rms"], rms)
+                e["requests"] += 1
+                e["N"].append(int(N[k]))
+    srv.close()
+    out = dict(by_tol)
+    out["by_grid"] = by_grid
+    out["sample"] = (f"{per_class} requests per grid class (first of the stream in the class), {ntgt} seeded "
+                     f"targets each, vs the FP64 oracle; max = max_i |u_i - u*_i| / max_i |u*_i|, rms = "
+                     f"||u - u*|| / ||u*|| (worst request)")
+    return out
+
+
 def run_serve(args, w, rank, world, dist, torch):
     import periodicbrinkman_gb300 as pb
 
@@ -186,11 +235,9 @@ def run_serve(args, w, rank, world, dist, torch):
     pool = InputPool(w["nmax"], pinned=True)
     step_req = 500
     srv = serve_server(w)
-    # page-locked velocity buffers: one arena slice per request of a step / of the latency run
-    nlat = min(6000, w["nreq"])
+    # page-locked velocity buffers: one arena slice per request of a step
     per_step = max(int(np.sum(N[i:i + step_req] // 2)) for i in range(0, w["nreq"], step_req))
     out_step = host_array((per_step + 1, 3), True)
-    out_lat = host_array((int(np.sum(N[:nlat] // 2)) + 1, 3), True)
 
     def submit(k, arena, off):
         x, f, y = pool.get(k, int(N[k]))
@@ -242,55 +289,82 @@ def run_serve(args, w, rank, world, dist, torch):
     t_tot = max_over_ranks(float(np.sum(step_s)), dist)
     value = world * args.steps * step_req / t_tot
     stats = srv.stats()
-    # open-loop latency under the stream's Poisson arrivals (first 6000 requests, 3 s)
-    lat = np.zeros(nlat)
-    t_start = time.perf_counter()
-    tickets, off = [], 0
-    for k in range(nlat):
-        dt = arrive[k] - (time.perf_counter() - t_start)
-        if dt > 0:
-            time.sleep(dt)
-        t, off = submit(k, out_lat, off)
-        tickets.append(t)
-    for k, t in enumerate(tickets):
-        _, lat[k] = srv.result(t, timeout=600)
+    lat, lat_wall = serve_latency(srv, w, pool, arrive, N, alpha, eps, tol)
+    peak_bytes = srv.stats()["device_bytes"]
     srv.close()
     if rank != 0:
         return None
-    # accuracy of sampled requests against the FP64 oracle (subsampled targets)
-    err = {}
+    # accuracy of requests of every grid class against the FP64 oracle (subsampled targets)
     try:
-        import oracle
-
-        srv2 = serve_server(dict(w, budget=8 << 30))
-        rng = np.random.default_rng(9)
-        for tl in (1e-6, 1e-4):
-            ks = [k for k in range(200) if tol[k] == tl and N[k] <= 20000][:3]
-            worst = 0.0
-            for k in ks:
-                x, f, y = pool.get(k, int(N[k]))
-                t = srv2.submit(x, f, 1.0, float(alpha[k]), float(eps[k]), y=y, tol=tl)
-                U, _ = srv2.result(t)
-                sel = rng.choice(y.shape[0], min(48, y.shape[0]), replace=False)
-                ref = oracle.ewald_velocity(y[sel], x, f, 1.0, float(alpha[k]), float(eps[k]))
-                worst = max(worst, oracle.rel_errors(U[sel], ref)[0])
-            err[f"tol{tl:g}"] = worst
-        srv2.close()
+        err = serve_accuracy(w, pool, N, alpha, eps, tol)
     except Exception as exc:  # pragma: no cover
-        err["error"] = str(exc)
-    # plain FP64 per-solve path on a sample of the stream
-    sample = np.random.default_rng(4).choice(nreq, 24, replace=False)
+        err = {"error": str(exc)}
+    # plain FP64 per-solve path on 200 requests of the stream
+    nplain = 200
+    sample = np.random.default_rng(4).choice(nreq, nplain + 2, replace=False)
     for k in sample[:2]:  # warm-up
         x, f, y = pool.get(int(k), int(N[k]))
         pb.solve(x, f, 1.0, float(alpha[k]), float(eps[k]), y=y, tol=float(tol[k]), precision="fp64")
     t0 = time.perf_counter()
-    for k in sample:
+    for k in sample[2:]:
         x, f, y = pool.get(int(k), int(N[k]))
         pb.solve(x, f, 1.0, float(alpha[k]), float(eps[k]), y=y, tol=float(tol[k]), precision="fp64")
-    plain = len(sample) / (time.perf_counter() - t0)
-    return dict(value=value, step_s=step_s, sub_s=sub_s, sched_busy=sched_busy, steps=args.steps, step_req=step_req, stats=stats,
-                p50=float(np.percentile(lat, 50)), p99=float(np.percentile(lat, 99)), lat_n=nlat, err=err,
-                plain=plain, h2d=h2d, d2h=d2h, clocks=clk.summary(), launches=launches)
+    plain = nplain / (time.perf_counter() - t0)
+    return dict(value=value, step_s=step_s, sub_s=sub_s, sched_busy=sched_busy, steps=args.steps, step_req=step_req,
+                stats=stats, p50=float(np.percentile(lat, 50)), p99=float(np.percentile(lat, 99)), lat_n=len(lat),
+                lat_wall=lat_wall, err=err, plain=plain, plain_n=nplain, h2d=h2d, d2h=d2h, clocks=clk.summary(),
+                launches=launches, peak_bytes=peak_bytes)
+
+
+def serve_latency(srv, w, pool, arrive, N, alpha, eps, tol, ring_bytes=384 << 20):
+    """Open-loop latency over the whole stream: every request submitted at its
+    Poisson arrival time (a 10 s stream at 2,000/s), latency = submission ->
+    velocities in host memory, as the server measures it.  Velocities land in
+    slices of a page-locked ring; a slice is reused only after the request
+    that held it has been collected."""
+    from collections import deque
+
+    ring = host_array((ring_bytes // 24, 3), True)
+    cap = ring.shape[0]
+    live = deque()  # (ticket, start, end) in submission order
+    lat = []
+    head = 0
+    t_start = time.perf_counter()
+
+    def collect(block):
+        while live:
+            t, _, _ = live[0]
+            st, status, l = srv.poll(t)
+            if st != 2 and not block:
+                return
+            _, l = srv.result(t, timeout=600)
+            lat.append(l)
+            live.popleft()
+            if not block:
+                continue
+            return
+
+    for k in range(len(N)):
+        m = int(N[k]) // 2
+        if head + m > cap:
+            head = 0
+        # the slice [head, head + m) must be free: collect older requests that overlap it
+        while live and any(s < head + m and head < e for _, s, e in live):
+            collect(True)
+        dt = arrive[k] - (time.perf_counter() - t_start)
+        while dt > 2e-4:
+            collect(False)
+            dt = arrive[k] - (time.perf_counter() - t_start)
+            if dt > 2e-4:
+                time.sleep(min(dt - 1e-4, 1e-3))
+        x, f, y = pool.get(k, int(N[k]))
+        t = srv.submit(x, f, 1.0, float(alpha[k]), float(eps[k]), y=y, tol=float(tol[k]), out=ring[head:head + m])
+        live.append((t, head, head + m))
+        head += m
+        collect(False)
+    while live:
+        collect(True)
+    return np.asarray(lat), time.perf_counter() - t_start
 
 
 # ---------------------------------------------------------------- single solve
@@ -357,13 +431,14 @@ def run_batch(args, torch, local):
 
         Un = Uh.numpy()
         offs = np.cumsum([0] + [i[0] for i in inst])
-        worst = 0.0
-        for q in np.random.default_rng(6).choice(len(inst), 6, replace=False):
+        worst, worst_rms = 0.0, 0.0
+        for q in np.random.default_rng(6).choice(len(inst), 12, replace=False):
             n, L, a, e, x, f = inst[q]
             sel = np.arange(min(n, 8))
             ref = oracle.ewald_velocity(x[sel], x, f, L, a, e)
-            worst = max(worst, oracle.rel_errors(Un[offs[q]:offs[q + 1]][sel], ref)[0])
-        err = worst
+            mx, rms = oracle.rel_errors(Un[offs[q]:offs[q + 1]][sel], ref)
+            worst, worst_rms = max(worst, mx), max(worst_rms, rms)
+        err = {"max": worst, "rms": worst_rms}
     except Exception:
         pass
     nk = plan.kernel_count
@@ -406,10 +481,9 @@ def roofline_single(torch, local, steps_warm=3):
         fp32_peak = nsm * 128 * 2 * (pk.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
         roof = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
                 "traffic": REAL_DRAM_BYTES, "kernel": "k_real_mixed",
+                "traffic_source": TRAFFIC_SOURCE,
                 "note": "FP32 SIMT pair kernel (no tensor-core work in this path); 64 flop per pair inside rc; "
-                        "peak = SMs x 128 lanes x 2 flop x max SM clock (nominal: no measured FP32 peak exists); "
-                        "traffic = ncu dram read+write bytes of one launch of this workload "
-                        "(profiles/k_real_mixed_single_solve_N1e5.md)"}
+                        "peak = SMs x 128 lanes x 2 flop x max SM clock (nominal: no measured FP32 peak exists)"}
     else:
         by = 4.0 * 3 * M3 * 6 + 36.0 * n + 24.0 * n
         i = names.index(dom)
@@ -422,9 +496,10 @@ def roofline_single(torch, local, steps_warm=3):
     tk = float(stages[2] + stages[3] + stages[4]) * 1e-3
     ach = by / tk / 1e9
     roof_k = {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": ach / pk["hbm_gbs"],
-              "traffic": KSPACE_DRAM_BYTES, "kernel": "k_spread_f4g + FFT passes + k_gather_f4g",
+              "traffic": KSPACE_DRAM_BYTES, "traffic_source": TRAFFIC_SOURCE,
+              "kernel": "k_spread_f4g + FFT passes + k_gather_f4g",
               "note": f"peak of {src}; the grid stays in L2, so the path is bound by L2 reductions (spread) and the "
-                      "L1 data pipe (gather), not by HBM (profiles/k_spread_gather_f4_single_solve_N1e5.md)"}
+                      "L1 data pipe (gather), not by HBM"}
     roof["kspace"] = roof_k
     plan.close()
     return roof, dict(zip(names, stages.tolist())), info
@@ -503,6 +578,23 @@ def cpu_sample_serve(w, nsample=3, ntgt=16):
     return len(ks) / tot, [int(N[k]) for k in ks]
 
 
+def cpu_whole_small(w, count=3):
+    """The FP64 oracle on the smallest requests of the stream, timed whole
+    (all sources, all N/2 targets): solves/s and the requests' N."""
+    import oracle
+
+    arrive, N, alpha, eps, tol = gen_stream(w)
+    ks = np.argsort(N, kind="stable")[:count]
+    pool = InputPool(int(N[ks].max()) + 2, sets=1)
+    t = 0.0
+    for k in ks:
+        x, f, y = pool.get(0, int(N[k]))
+        t0 = time.perf_counter()
+        oracle.ewald_velocity(y, x, f, 1.0, float(alpha[k]), float(eps[k]))
+        t += time.perf_counter() - t0
+    return count / t, [int(N[k]) for k in ks]
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -519,7 +611,8 @@ def run_reference(args):
                 secs.append(1.0 / v)
         v = len(secs) / float(np.sum(secs))  # requests per second over the sampled requests
         sample = (f"FP64 direct-Ewald oracle restating the reference's sums ({th} threads): per step one request of "
-                  f"the stream, all sources, 8 of its N/2 targets, extrapolated to all targets")
+                  f"the stream, all sources and 8 of its N/2 targets timed, the time EXTRAPOLATED linearly to all "
+                  f"N/2 targets (not a whole solve: a whole large request takes hours on the host)")
         cfg = {"workload": w["name"]}
     else:
         w = SINGLE
@@ -615,7 +708,7 @@ def main():
                 "e2e": {"value": r["e2e"] * world, "unit": "solves/s", "h2d_bytes_per_step": 2 * 3 * r["nsrc"] * 8,
                         "d2h_bytes_per_step": 3 * r["nsrc"] * 8},
                 "gpu_launches": r["nk"] * args.steps, "max_rel_err": r["err"],
-                "err_sample": "8 targets of 6 instances vs the FP64 oracle", "clocks": r["clocks"]}
+                "err_sample": "8 targets of 12 instances vs the FP64 oracle (max, rms)", "clocks": r["clocks"]}
         print(json.dumps(line))
         return
     if args.workload in ("clustered", "single_fp64"):
@@ -638,7 +731,8 @@ def main():
                 "e2e": {"value": r["e2e"] * world, "unit": "solves/s", "h2d_bytes_per_step": 2 * 3 * w["n"] * 8,
                         "d2h_bytes_per_step": 3 * w["n"] * 8},
                 "gpu_launches": r["nk"] * args.steps, "stage_ms": r["stages"],
-                "max_rel_err": r["err"][0] if r["err"] else None, "err_sample": "16 targets vs the FP64 oracle",
+                "max_rel_err": {"max": r["err"][0], "rms": r["err"][1]} if r["err"] else None,
+                "err_sample": "16 targets vs the FP64 oracle",
                 "clocks": r["clocks"]}
         print(json.dumps(line))
         return
@@ -662,7 +756,8 @@ def main():
                 "e2e": {"value": r["e2e"] * world, "unit": "solves/s", "h2d_bytes_per_step": 2 * 3 * w["n"] * 8,
                         "d2h_bytes_per_step": 3 * w["n"] * 8},
                 "gpu_launches": r["nk"] * args.steps, "roofline": roof, "stage_ms": stages,
-                "max_rel_err": r["err"][0] if r["err"] else None, "clocks": r["clocks"], "cpu_baseline": cb}
+                "max_rel_err": {"max": r["err"][0], "rms": r["err"][1]} if r["err"] else None,
+                "err_sample": "96 targets vs the FP64 oracle", "clocks": r["clocks"], "cpu_baseline": cb}
         print(json.dumps(line))
         return
     w = SERVE
@@ -675,9 +770,12 @@ def main():
             import oracle
 
             v, ns = cpu_sample_serve(w)
+            vs, nsm = cpu_whole_small(w)
             cb = {"value": v, "unit": "solves/s", "cores": oracle.num_threads(), "kind": "port",
-                  "sample": f"FP64 oracle (C/OpenMP), 3 requests of the stream (N={ns}), all sources, 16 of N/2 "
-                            f"targets each, extrapolated to all targets"}
+                  "sample": f"FP64 oracle (C/OpenMP), 3 random requests of the stream (N={ns}), all sources and 16 "
+                            f"of N/2 targets timed, EXTRAPOLATED linearly to all targets",
+                  "timed_whole": {"value": vs, "unit": "solves/s", "N": nsm,
+                                  "sample": "the 3 smallest requests of the stream, every target, timed whole"}}
         except Exception as exc:  # pragma: no cover
             cb = {"value": None, "error": str(exc)}
     st = r["stats"]
@@ -687,14 +785,15 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded numpy)",
         "config": {"workload": w["name"], "requests_per_step": r["step_req"], "budget_bytes": w["budget"],
                    "server": {"slots": st["slots"], "device_bytes": st["device_bytes"],
-                              "mean_batch": st["mean_batch"]},
+                              "device_bytes_after_stream": r["peak_bytes"], "mean_batch": st["mean_batch"]},
                    "l2": "inputs of a step (hundreds of MB) exceed L2", "parallelism": f"replicas x{world}",
                    "timing": "host wall time between device-wide synchronizes (multi-stream server)",
                    "submit_s_per_step": float(np.mean(r["sub_s"])),
                    "scheduler_busy_s_per_step": r["sched_busy"] / max(1, r["steps"])},
-        "latency_s": {"p50": r["p50"], "p99": r["p99"], "requests": r["lat_n"], "arrival": "Poisson 2000/s"},
+        "latency_s": {"p50": r["p50"], "p99": r["p99"], "requests": r["lat_n"], "arrival": "Poisson 2000/s",
+                      "stream_wall_s": r["lat_wall"]},
         "plain_fp64": {"value": r["plain"], "unit": "solves/s", "path": "pb_solve FP64, one solve per call",
-                       "served_over_plain": r["value"] / r["plain"]},
+                       "requests": r["plain_n"], "served_over_plain": r["value"] / r["plain"]},
         "e2e": {"value": r["value"], "unit": "solves/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
         "gpu_launches": r["launches"],

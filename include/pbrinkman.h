@@ -132,7 +132,10 @@ int pb_fft_brinkman(double* U, const double* y, int m_tgt, const double* f, cons
  * intermediates live in one fixed array of 21.2 MB (20.2 MiB) compiled into the
  * library, which every GPU that loads the library holds until the process
  * exits.  Limits: M[a] <= 64, n <= 65536, m_tgt <= 65536; larger sizes return
- * PB_ERR_UNSUPPORTED.  The first call on a device looks up the array's
+ * PB_ERR_UNSUPPORTED.  Nothing is autotuned: M[a] and P[0] must be given
+ * (> 0, else PB_ERR_INVALID).  The descriptor and twiddles travel as a
+ * kernel launch parameter, so no host memory is read after the call
+ * returns.  The first call on a device looks up the array's
  * device address for that device (make it before any stream capture).  All
  * calls share the array, so calls that overlap on the GPU race: serialise
  * them on one stream. */
@@ -184,6 +187,15 @@ long long pb_plan_estimate_bytes(const pb_solve_params* p, int count);
  * enabled with pb_plan_set_timing: [0] sort, [1] real space, [2] spread,
  * [3] FFT + Green, [4] gather, [5] combine. */
 int pb_plan_set_timing(pb_plan plan, int enable);
+/* Waits for the plan's last execution and returns its device-side status:
+ * PB_ERR_INVALID if an input was not finite (those inputs were computed as
+ * 0), PB_ERR_UNSUPPORTED if a capacity was exceeded (results incomplete),
+ * else PB_OK.  Executions with PB_HOST buffers check this themselves. */
+int pb_plan_status(pb_plan plan);
+/* Testing aid: lowers the plan's real-space work-item capacity to `cap`
+ * (at most what the plan allocated), so that the overflow check can be
+ * exercised; drops the captured graphs. */
+int pb_plan_set_item_capacity(pb_plan plan, int cap);
 int pb_plan_stage_ms(pb_plan plan, double* ms6);
 int pb_plan_destroy(pb_plan plan);
 
@@ -243,6 +255,17 @@ int pb_debug_pair_kernel(double alpha, double d, double eps, double rc, int n, c
  * the closed forms below it, evaluated on the host as the GPU does. */
 int pb_debug_pair_kernel64(double alpha, double d, double eps, double rc, int n, const double* r, double* H1,
                            double* H2);
+/* The k-space grid operator alone, for checking the hand-written FFT passes
+ * against a library FFT: forward 3D real FFT of the three components of a
+ * DEVICE grid, the Green-tensor multiply with Gaussian deconvolution (the
+ * instance's kfac (1 + (1 - e^{-alpha^2 d^2/4}) k^2/alpha^2)
+ * e^{-k^2 (d^2/4 - eta/2)} / (k^2 (k^2 + alpha^2)) (k^2 I - k k^T); Nyquist
+ * planes and k = 0 zeroed) and the unnormalised inverse FFT, in place.  The
+ * grid M and the splitting of `p` are resolved as a solve resolves them (M
+ * must be given).  Layout: PB_PREC_MIXED, M^3 float4 (x, y, z, unused);
+ * PB_PREC_FP64, four planes of M^3 doubles (x, y, z, unused).  Allocates a
+ * temporary spectrum and synchronises `stream`. */
+int pb_debug_fft_green(const pb_solve_params* p, void* grid, void* stream);
 /* Number of CUDA devices visible (0 without a GPU). */
 int pb_device_count(void);
 

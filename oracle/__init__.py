@@ -51,6 +51,64 @@ def build_ref() -> bool:
     return os.path.exists(_REF_PATH)
 
 
+_REF_LAUNCH_SRC = os.path.join(_HERE, "ref_launch.cpp")
+_REF_LAUNCH_LIB = os.path.join(_BUILD, "libpbref_launch.so")
+_REF_IMAGES = [os.path.join(_HERE, "_ref", "ref_kernels." + k) for k in ("cubin", "ptx")]
+_ref_gpu = None
+
+
+def ref_gpu_available() -> str | None:
+    """None when the reference's compiled kernel image is present here, else why not."""
+    if not any(os.path.exists(p) for p in _REF_IMAGES):
+        return ("the reference's kernel image oracle/_ref/ref_kernels.{cubin,ptx} was not built (it needs the "
+                "reference's sources, which stay out of this repository)")
+    return None
+
+
+def ref_gpu():
+    """The launcher of the reference's own CUDA kernels (ref_launch.cpp), built
+    here with g++ against the CUDA driver API, with the kernel image loaded
+    into the current CUDA context.  TEST INFRASTRUCTURE: the checker of the
+    dense drop-in and a timed baseline, never the product path."""
+    global _ref_gpu
+    if _ref_gpu is not None:
+        return _ref_gpu
+    why = ref_gpu_available()
+    if why:
+        raise RuntimeError(why)
+    if not os.path.exists(_REF_LAUNCH_LIB) or os.path.getmtime(_REF_LAUNCH_LIB) < os.path.getmtime(_REF_LAUNCH_SRC):
+        os.makedirs(_BUILD, exist_ok=True)
+        tmp = _REF_LAUNCH_LIB + f".tmp{os.getpid()}"
+        cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+        subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-I", os.path.join(cuda, "include"), "-o", tmp,
+                        _REF_LAUNCH_SRC, "-L", os.path.join(cuda, "lib64", "stubs"), "-lcuda"], check=True)
+        os.replace(tmp, _REF_LAUNCH_LIB)
+    L = C.CDLL(_REF_LAUNCH_LIB)
+    L.refk_error.restype = C.c_char_p
+    L.refk_load.argtypes = [C.c_char_p]
+    L.refk_periodic_brinkman.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double,
+                                         C.c_double, C.c_double, C.c_int, C.c_int, _dp, C.c_int]
+    errs = []
+    for img in _REF_IMAGES:
+        if os.path.exists(img):
+            if L.refk_load(img.encode()) == 0:
+                _ref_gpu = L
+                return L
+            errs.append(f"{os.path.basename(img)}: {L.refk_error().decode()}")
+    raise RuntimeError("reference kernel image not loaded: " + "; ".join(errs))
+
+
+def ref_gpu_periodic_brinkman(dA_ptr, dx_ptr, m, dx0_ptr, n, a, d, e, M, N, L, max_block=256):
+    """The reference's periodicBrinkman() on its own compiled kernels: dA
+    (device, 3m x 3n column-major) += A.  Device pointers; waits."""
+    Lv = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), (3,)))
+    lib_ = ref_gpu()
+    rc = lib_.refk_periodic_brinkman(dA_ptr, dx_ptr, int(m), dx0_ptr, int(n), float(a), float(d), float(e), int(M),
+                                     int(N), _p(Lv), int(max_block))
+    if rc != 0:
+        raise RuntimeError("reference kernels: " + lib_.refk_error().decode())
+
+
 def lib():
     global _lib
     if _lib is None:

@@ -166,10 +166,13 @@ def lib():
     L.pb_plan_estimate_bytes.restype = C.c_longlong
     L.pb_plan_estimate_bytes.argtypes = [C.POINTER(SolveParams), C.c_int]
     L.pb_plan_set_timing.argtypes = [vp, C.c_int]
+    L.pb_plan_status.argtypes = [vp]
+    L.pb_plan_set_item_capacity.argtypes = [vp, C.c_int]
     L.pb_plan_stage_ms.argtypes = [vp, dp]
     L.pb_plan_destroy.argtypes = [vp]
     L.pb_debug_pair_kernel.argtypes = [C.c_double] * 4 + [C.c_int, dp, dp, dp]
     L.pb_debug_pair_kernel64.argtypes = [C.c_double] * 4 + [C.c_int, dp, dp, dp]
+    L.pb_debug_fft_green.argtypes = [C.POINTER(SolveParams), vp, vp]
     L.pb_plan_create_slot.argtypes = [C.POINTER(SlotConfig), C.POINTER(vp)]
     L.pb_slot_estimate_bytes.restype = C.c_longlong
     L.pb_slot_estimate_bytes.argtypes = [C.POINTER(SlotConfig)]

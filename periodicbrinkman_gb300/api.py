@@ -128,6 +128,15 @@ class Plan:
         check(lib().pb_plan_execute_forces(self._h, _ptr(f), _ptr(U), where, s))
         return U
 
+    def status(self) -> None:
+        """Waits for the last execution and raises PbError if the device found a
+        non-finite input or a capacity overflow (pb_plan_status)."""
+        check(lib().pb_plan_status(self._h))
+
+    def set_item_capacity(self, cap: int) -> None:
+        """Testing aid: lower the real-space work-item capacity."""
+        check(lib().pb_plan_set_item_capacity(self._h, int(cap)))
+
     def info(self, i: int = 0) -> dict:
         inf = InstanceInfo()
         check(lib().pb_plan_instance_info(self._h, i, C.byref(inf)))
@@ -311,6 +320,7 @@ def solve(x, f, L, alpha, eps, y=None, **kw):
     p = make_params(n, L, alpha, eps, n_tgt=m, **kw)
     with Plan(p) as plan:
         U = plan.execute(x, f, y)
+        plan.status()
     return U
 
 

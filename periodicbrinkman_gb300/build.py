@@ -75,7 +75,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if os.path.exists(LIB) and all(os.path.getmtime(o) <= os.path.getmtime(LIB) for o in objs):
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lcudart"]
+    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")

@@ -327,8 +327,11 @@ struct pb_plan_s {
     int4* items = nullptr;
     void *spos_a = nullptr, *spos_b = nullptr, *sfrc = nullptr, *tpos_a = nullptr, *tpos_b = nullptr;
     double *u_real = nullptr, *fsum = nullptr;
-    int* d_bad = nullptr;     // per instance: an input was not finite (set by the binning kernels)
-    int* h_bad = nullptr;     // pinned copy, written by plan_execute_parts
+    // per instance: an input was not finite (set by the binning kernels); entry
+    // [count]: capacity bits of the execution (kCapItems: the real-space work
+    // items outgrew the item array, so items were dropped)
+    int* d_bad = nullptr;
+    int* h_bad = nullptr;     // pinned copy, written at the end of every execution
     int item_cap = 0;         // capacity of the real-space work item array
     void *u_k = nullptr, *grid = nullptr, *spec = nullptr;
 
@@ -412,7 +415,7 @@ size_t plan_layout(pb_plan_s* P, bool assign)
     }
     size_t o_ur = L.take<double>(3 * (size_t)nt);
     size_t o_uk = mixed ? L.take<float>(3 * (size_t)nt) : L.take<double>(3 * (size_t)nt);
-    size_t o_fsum = L.take<double>(3 * (size_t)q), o_bad = L.take<int>(q);
+    size_t o_fsum = L.take<double>(3 * (size_t)q), o_bad = L.take<int>(q + 1);
     size_t esz = mixed ? 4 : 8;
     size_t o_grid = L.off;
     L.off += align_up(P->grid_elems * esz + 16);
@@ -702,8 +705,8 @@ int plan_alloc(pb_plan_s* P)
     PB_CK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
     P->staging_bytes = (sizeof(PbInst) + sizeof(PbTables)) * (size_t)P->count + 4 * sizeof(int) * (P->count + 1);
     PB_CK(cudaMallocHost(&P->staging, P->staging_bytes));
-    PB_CK(cudaMallocHost(&P->h_bad, sizeof(int) * P->count));
-    std::memset(P->h_bad, 0, sizeof(int) * P->count);
+    PB_CK(cudaMallocHost(&P->h_bad, sizeof(int) * (P->count + 1)));
+    std::memset(P->h_bad, 0, sizeof(int) * (P->count + 1));
     PB_CK(cudaEventCreateWithFlags(&P->ev_upload, cudaEventDisableTiming));
     PB_CK(cudaEventCreateWithFlags(&P->ev_in, cudaEventDisableTiming));
     PB_CK(cudaEventCreateWithFlags(&P->ev_out, cudaEventDisableTiming));
@@ -748,8 +751,9 @@ void record(pb_plan_s* P, int k, cudaStream_t s)
 void run_compute(pb_plan_s* P, cudaStream_t s, bool forces_only)
 {
     const bool mixed = P->prec == PB_PREC_MIXED;
+    NvtxRange nv_all("pb.compute");
     record(P, 0, s);
-    cudaMemsetAsync(P->d_bad, 0, sizeof(int) * P->count, s);
+    cudaMemsetAsync(P->d_bad, 0, sizeof(int) * (P->count + 1), s);
     if (!forces_only)
         bin_and_sort(P, P->x, P->n_src, P->d_src_off, P->cell_of_s, P->cnt_s, P->start_s, P->fill_s, P->perm_tmp_s,
                      P->perm_s, s);
@@ -772,8 +776,9 @@ void run_compute(pb_plan_s* P, cudaStream_t s, bool forces_only)
     }
     if (!forces_only)
         launch_build_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items, P->item_cap,
-                           P->counter + 1, P->nsm, s);
+                           P->counter + 1, P->d_bad + P->count, P->nsm, s);
     record(P, 1, s);
+    nvtxRangePushA("pb.real_space");
     if (P->any_real) {
         const int* nitems = P->counter + 1;
         if (mixed)
@@ -786,7 +791,9 @@ void run_compute(pb_plan_s* P, cudaStream_t s, bool forces_only)
                              (const Dbl4*)P->sfrc, P->start_s, (const Dbl4*)P->tpos_a, P->n_tgt, P->u_real,
                              P->counter, P->nsm, s);
     }
+    nvtxRangePop();
     record(P, 2, s);
+    nvtxRangePushA("pb.kspace");
     if (P->any_k) {
         launch_zero_grids(P->d_inst, P->count, P->grid, mixed ? 4 : 8, s);
         if (mixed)
@@ -817,6 +824,7 @@ void run_compute(pb_plan_s* P, cudaStream_t s, bool forces_only)
         record(P, 3, s);
         record(P, 4, s);
     }
+    nvtxRangePop();
     record(P, 5, s);
     if (P->any_zero) launch_force_sums(P->d_inst, P->f, P->d_src_off, P->count, P->fsum, s);
     if (mixed)
@@ -1066,6 +1074,7 @@ int plan_execute_parts(pb_plan P, const double* const* xs, const double* const* 
                        double* const* Us, cudaStream_t us)
 {
     if (!P) return fail(PB_ERR_INVALID, "null plan");
+    NvtxRange nv("pb_plan_execute_parts");
     cudaStream_t s = P->stream;
     PB_CK(cudaEventRecord(P->ev_in, us));
     PB_CK(cudaStreamWaitEvent(s, P->ev_in, 0));
@@ -1088,7 +1097,7 @@ int plan_execute_parts(pb_plan P, const double* const* xs, const double* const* 
             PB_CK(cudaMemcpyAsync(Us[q], P->U + 3 * (size_t)P->tgt_off[q], sizeof(double) * 3 * R.n_tgt,
                                   cudaMemcpyDeviceToHost, s));
     }
-    PB_CK(cudaMemcpyAsync(P->h_bad, P->d_bad, sizeof(int) * P->count, cudaMemcpyDeviceToHost, s));
+    PB_CK(cudaMemcpyAsync(P->h_bad, P->d_bad, sizeof(int) * (P->count + 1), cudaMemcpyDeviceToHost, s));
     P->exec_count++;
     PB_CK(cudaEventRecord(P->ev_out, s));
     PB_CK(cudaStreamWaitEvent(us, P->ev_out, 0));
@@ -1140,6 +1149,8 @@ int plan_bind_prepared(pb_plan P, const pb_solve_params* p, const PbTables* tabs
 }
 
 const int* plan_bad_flags(pb_plan P) { return P->h_bad; }
+
+int plan_exec_status(pb_plan P) { return P->h_bad[P->count]; }
 
 int kspace_instance(const pb_solve_params& p, PbInst* inst)
 {
@@ -1261,12 +1272,46 @@ int pb_plan_stage_ms(pb_plan plan, double* ms6)
     return PB_OK;
 }
 
+// Status of the finished last execution from its flags (h_bad).
+static int status_of(pb_plan P)
+{
+    if (P->h_bad[P->count] & kCapItems)
+        return fail(PB_ERR_UNSUPPORTED, "real-space work items exceeded the plan's item capacity (%d)", P->item_cap);
+    for (int q = 0; q < P->count; q++)
+        if (P->h_bad[q]) return fail(PB_ERR_INVALID, "non-finite input (instance %d)", q);
+    return PB_OK;
+}
+
+int pb_plan_status(pb_plan P)
+{
+    if (!P) return fail(PB_ERR_INVALID, "null plan");
+    PB_CK(cudaStreamSynchronize(P->stream));
+    return status_of(P);
+}
+
+int pb_plan_set_item_capacity(pb_plan P, int cap)
+{
+    if (!P || cap < 1) return fail(PB_ERR_INVALID, "bad arguments");
+    const int full = 4 * std::max(P->n_tgt, 1) + 4096;  // as plan_layout sizes the array
+    if (cap > full) return fail(PB_ERR_INVALID, "item capacity above the allocated %d", full);
+    PB_CK(cudaStreamSynchronize(P->stream));
+    P->item_cap = cap;
+    // the captured graphs hold the old capacity in their kernel parameters
+    if (P->gexec) cudaGraphExecDestroy(P->gexec);
+    if (P->gexec_f) cudaGraphExecDestroy(P->gexec_f);
+    P->gexec = P->gexec_f = nullptr;
+    P->exec_count = P->fexec_count = 0;
+    P->have_positions = false;
+    return PB_OK;
+}
+
 // One execution of a plan; with `forces_only` the positions (and targets) of
 // the last full execution are reused and only `f` is read.
 static int execute_impl(pb_plan P, const double* x, const double* f, const double* y, double* U, int where, void* stream_v,
                  bool forces_only)
 {
     if (!P) return fail(PB_ERR_INVALID, "null plan");
+    NvtxRange nv(forces_only ? "pb_plan_execute_forces" : "pb_plan_execute");
     if (forces_only && !P->have_positions)
         return fail(PB_ERR_INVALID, "no sorted positions: execute the plan with positions first");
     if ((P->act_src > 0 && ((!forces_only && !x) || !f)) || (P->act_tgt > 0 && !U) ||
@@ -1305,7 +1350,7 @@ static int execute_impl(pb_plan P, const double* x, const double* f, const doubl
         cudaMemcpyKind kout = where == PB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
         PB_CK(cudaMemcpyAsync(U, P->U, sizeof(double) * 3 * P->act_tgt, kout, s));
     }
-    if (where == PB_HOST) PB_CK(cudaMemcpyAsync(P->h_bad, P->d_bad, sizeof(int) * P->count, cudaMemcpyDeviceToHost, s));
+    PB_CK(cudaMemcpyAsync(P->h_bad, P->d_bad, sizeof(int) * (P->count + 1), cudaMemcpyDeviceToHost, s));
     if (forces_only)
         P->fexec_count++;
     else
@@ -1313,9 +1358,10 @@ static int execute_impl(pb_plan P, const double* x, const double* f, const doubl
     PB_CK(cudaEventRecord(P->ev_out, s));
     PB_CK(cudaStreamWaitEvent(us, P->ev_out, 0));
     if (where == PB_HOST || P->timing) PB_CK(cudaStreamSynchronize(s));
-    if (where == PB_HOST)
-        for (int q = 0; q < P->count; q++)
-            if (P->h_bad[q]) return fail(PB_ERR_INVALID, "non-finite input (instance %d)", q);
+    if (where == PB_HOST) {
+        int rc = status_of(P);
+        if (rc) return rc;
+    }
     if (!forces_only) P->have_positions = true;
     if (P->timing) {
         float ms;
@@ -1341,6 +1387,7 @@ int pb_plan_execute_forces(pb_plan P, const double* f, double* U, int where, voi
 int pb_solve(const pb_solve_params* p, const double* x, const double* f, const double* y, double* U, int where,
              void* stream)
 {
+    NvtxRange nv("pb_solve");
     pb_plan P = nullptr;
     int rc = pb_plan_create(p, 1, &P);
     if (rc) return rc;
@@ -1365,6 +1412,7 @@ int pb_periodic_brinkman_ex(double* dA, const double* dx, int m, const double* d
     if (!std::isfinite(a) || !(a > 0) || !std::isfinite(d) || !(d > 0) || !std::isfinite(e) || e < 0)
         return fail(PB_ERR_INVALID, "need alpha > 0, d > 0, e >= 0");
     if (pb_device_count() <= 0) return fail(PB_ERR_CUDA, "no CUDA device");
+    NvtxRange nv("pb_periodic_brinkman");
     int rc = launch_dense_matrix(dA, dx, m, dx0, n, a, d, e, Mx, Nx, L, tau_scaled, (cudaStream_t)stream);
     if (rc) return fail(PB_ERR_UNSUPPORTED, "more than 256 Fourier shells per axis");
     PB_CK(cudaGetLastError());
@@ -1479,6 +1527,51 @@ int pb_debug_pair_kernel64(double alpha, double d, double eps, double rc, int n,
             H2[i] = h2;
         }
     }
+    return PB_OK;
+}
+
+int pb_debug_fft_green(const pb_solve_params* p, void* grid, void* stream)
+{
+    if (!p || !grid) return fail(PB_ERR_INVALID, "bad arguments");
+    for (int a = 0; a < 3; a++)
+        if (p->M[a] <= 0) return fail(PB_ERR_INVALID, "the grid M must be given");
+    Resolved R;
+    int rc = resolve(*p, R);
+    if (rc) return rc;
+    if (pb_device_count() <= 0) return fail(PB_ERR_CUDA, "no CUDA device");
+    PbInst I;
+    std::memset(&I, 0, sizeof(I));
+    set_inst_fields(I, *p, R, 0, 0, 0);
+    I.n_src = I.n_tgt = 1;  // a live instance for the passes
+    const bool fp64 = p->precision == PB_PREC_FP64;
+    const size_t esz = fp64 ? 8 : 4, spec = 3 * (size_t)R.M[0] * R.M[1] * (R.M[2] / 2 + 1) * 2 * esz;
+    const size_t twb = twiddle_bytes(R.M, fp64);
+    std::vector<char> tw(twb);
+    fill_twiddles(R.M, fp64, tw.data());
+    const size_t o_inst = 0, o_b = align_up(sizeof(PbInst)), o_tw = o_b + 256, o_spec = o_tw + align_up(twb);
+    char* arena = nullptr;
+    cudaError_t e = cudaMalloc(&arena, o_spec + spec);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(PB_ERR_NOMEM, "device allocation failed");
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int zero = 0;
+    e = cudaMemcpy(arena + o_inst, &I, sizeof(I), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(arena + o_b, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(arena + o_tw, tw.data(), twb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        if (fp64)
+            launch_kspace_fft<double>((const PbInst*)(arena + o_inst), (const int*)(arena + o_b), 1, 0, R.M,
+                                      (double*)grid, arena + o_spec, arena + o_tw, s);
+        else
+            launch_kspace_fft<float>((const PbInst*)(arena + o_inst), (const int*)(arena + o_b), 1, 0, R.M,
+                                     (float*)grid, arena + o_spec, arena + o_tw, s);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(arena);
+    if (e != cudaSuccess) return fail(PB_ERR_CUDA, "%s", cudaGetErrorString(e));
     return PB_OK;
 }
 

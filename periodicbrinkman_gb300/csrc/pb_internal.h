@@ -2,11 +2,21 @@
 // include/pbrinkman.h).
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "pb_types.h"
 #include "pbrinkman.h"
 
 namespace pb {
+
+// An NVTX range over a scope of host code (API calls, server steps, the
+// launch of each stage): visible in Nsight Systems timelines, free otherwise.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Sets the calling thread's pb_last_error() message; returns `code`.
 int api_error(int code, const char* msg);
@@ -29,5 +39,7 @@ int plan_execute_parts(pb_plan P, const double* const* xs, const double* const* 
 // After an execution by plan_execute_parts has completed: flags[q] != 0 when
 // instance q had a non-finite input (those inputs were computed as 0).
 const int* plan_bad_flags(pb_plan P);
+// After such an execution: its capacity status bits (kCapItems, ...).
+int plan_exec_status(pb_plan P);
 
 }  // namespace pb

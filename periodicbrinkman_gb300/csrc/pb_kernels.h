@@ -38,9 +38,11 @@ void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, 
 // times csplit stencil column groups:
 // int4 {inst, first target, local row, count | za << 8 | zb << 16 | group << 24}.
 // Builds the items of all row-start cells (cell_offsets[ninst] = actual cells);
-// *nitems = number of items (may exceed cap: the real-space kernels clamp).
+// *nitems = number of items.  Items beyond `cap` are not written: the
+// real-space kernels clamp to cap and *status gets kCapItems, which the host
+// turns into an error.
 void launch_build_items(const int* start, int ncell_cap, const int* cell_offsets, const PbInst* inst, int ninst,
-                        int4* items, int cap, int* nitems, int nsm, cudaStream_t s);
+                        int4* items, int cap, int* nitems, int* status, int nsm, cudaStream_t s);
 
 // ---- real space (pb_real.cu) ----
 // Mixed precision: FP32 polynomial kernel, hi/lo displacements, Kahan sums.

@@ -105,7 +105,10 @@ int grid_index(pb_server_s* S, int g)
 
 void finish_slot(pb_server_s* S, Slot& sl, int status)
 {
+    pb::NvtxRange nv("pb_server.finish");
     size_t off = 0;
+    // work items beyond the slot's item array: every request of the execution lost pairs
+    if (status == PB_OK && (pb::plan_exec_status(sl.plan) & pb::kCapItems)) status = PB_ERR_UNSUPPORTED;
     const int* bad = status == PB_OK ? pb::plan_bad_flags(sl.plan) : nullptr;
     for (size_t k = 0; k < sl.reqs.size(); k++) {
         Req* r = sl.reqs[k];
@@ -127,6 +130,7 @@ void finish_slot(pb_server_s* S, Slot& sl, int status)
 bool dispatch(pb_server_s* S, Slot& sl, std::deque<Req*>& q)
 {
     if (q.empty()) return false;
+    pb::NvtxRange nv("pb_server.dispatch");
     const pb_slot_config& c = sl.cfg;
     // batching window: a short queue waits (up to linger_us after its oldest
     // request arrived) for more requests to share the slot execution
@@ -349,6 +353,7 @@ int pb_server_submit(pb_server S, const pb_solve_params* p, const double* x, con
     *ticket = 0;
     if (p->precision != S->cfg.precision) return PB_ERR_INVALID;
     if (p->n_src <= 0 || (p->n_tgt > 0 && !y) || !x || !f || !U) return PB_ERR_INVALID;
+    pb::NvtxRange nv("pb_server_submit");
     // autotune and build the real-space tables here, in the caller's thread, so
     // the scheduler only binds.  The instance runs on its slot's grid: when the
     // autotuned grid is not a provisioned one, resolve again for the slot's grid.

@@ -312,7 +312,7 @@ constexpr int kItemWarps = 8;
 __global__ void __launch_bounds__(kItemWarps * 32)
     k_build_items(const int* __restrict__ start, const int* __restrict__ cell_offsets,
                   const PbInst* __restrict__ inst, int ninst, int4* __restrict__ items, int cap,
-                  int* __restrict__ nitems)
+                  int* __restrict__ nitems, int* __restrict__ status)
 {
     __shared__ int st[kItemWarps][129];  // nc[2] <= 128
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -344,6 +344,7 @@ __global__ void __launch_bounds__(kItemWarps * 32)
                 walk_row<false>(st[w], 0, nz, rq, rl / nz, G, nullptr, 0, 0, n);
                 if (n > 0) {
                     const int k0 = atomicAdd(nitems, n);
+                    if (k0 + n > cap) atomicOr(status, kCapItems);  // items dropped: reported, not silent
                     walk_row<true>(st[w], 0, nz, rq, rl / nz, G, items, k0, cap, n);
                 }
             }
@@ -352,13 +353,14 @@ __global__ void __launch_bounds__(kItemWarps * 32)
 }
 
 void launch_build_items(const int* start, int ncell_cap, const int* cell_offsets, const PbInst* inst, int ninst,
-                        int4* items, int cap, int* nitems, int nsm, cudaStream_t s)
+                        int4* items, int cap, int* nitems, int* status, int nsm, cudaStream_t s)
 {
     cudaMemsetAsync(nitems, 0, sizeof(int), s);
     if (ncell_cap <= 0) return;
     long long blocks = ((long long)ncell_cap + 32 * kItemWarps - 1) / (32 * kItemWarps);
     if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
-    k_build_items<<<(int)blocks, kItemWarps * 32, 0, s>>>(start, cell_offsets, inst, ninst, items, cap, nitems);
+    k_build_items<<<(int)blocks, kItemWarps * 32, 0, s>>>(start, cell_offsets, inst, ninst, items, cap, nitems,
+                                                          status);
 }
 
 }  // namespace pb

@@ -10,6 +10,12 @@
 // the process exits.  Every call shares it and it keeps the last call's
 // contents, so the grid is cleared at the start of each call, and calls that
 // overlap on the GPU (other streams, other host threads) race.
+//
+// The instance descriptor and the FFT twiddles are built on the host and
+// handed to a one-block set-up kernel as its (by-value) launch parameter,
+// which writes them into the array: no host-to-device copy from pageable
+// memory, which the driver could stage through its own buffer and order
+// against the whole device.
 #include <cstring>
 #include <mutex>
 
@@ -48,6 +54,15 @@ constexpr size_t kOffSpec = kOffGrid + al256(4 * kGridMax * sizeof(double));  //
 constexpr size_t kScratchBytes =
     kOffSpec + al256(3 * (size_t)kStaticMaxGrid * kStaticMaxGrid * (kStaticMaxGrid / 2 + 1) * sizeof(double2));
 
+// Launch parameter of the set-up kernel: the header and the twiddle table
+// (4.6 KB, within the 32 KB a kernel parameter list may hold on this GPU).
+struct StaticSetup {
+    StaticHeader h;
+    alignas(16) unsigned char tw[kTwMax];
+};
+static_assert(sizeof(StaticHeader) % 4 == 0 && kTwMax % 4 == 0, "word copies");
+static_assert(sizeof(StaticSetup) < 30000, "kernel parameter size");
+
 }  // namespace
 
 // The scratch array.  In host code this name is only a stand-in for the
@@ -81,6 +96,16 @@ int static_scratch(char** out)
     return PB_OK;
 }
 
+// Writes the header and `twn` bytes of twiddles from the launch parameter
+// into the scratch array (one block).
+__global__ void k_static_setup(const StaticSetup su, unsigned* __restrict__ hdr, unsigned* __restrict__ tw, int twn)
+{
+    const unsigned* hs = reinterpret_cast<const unsigned*>(&su.h);
+    const unsigned* ts = reinterpret_cast<const unsigned*>(su.tw);
+    for (int i = threadIdx.x; i < (int)(sizeof(StaticHeader) / 4); i += blockDim.x) hdr[i] = hs[i];
+    for (int i = threadIdx.x; i < twn / 4; i += blockDim.x) tw[i] = ts[i];
+}
+
 // Positions wrapped into the box as FP64 records of instance 0, forces beside.
 __global__ void k_static_records(const double* __restrict__ pos, const double* __restrict__ frc, int n, double L0,
                                  double L1, double L2, Dbl4* __restrict__ pos_out, Dbl4* __restrict__ frc_out)
@@ -100,14 +125,19 @@ extern "C" int pb_fft_brinkman_static(double* U, const double* y, int m_tgt, con
 {
     if (!L || !M || !P || msd <= 0 || n < 0 || m_tgt < 0) return api_error(PB_ERR_INVALID, "bad arguments");
     if (m_tgt == 0) return PB_OK;
-    if (!U || !y || (n > 0 && (!f || !xn))) return api_error(PB_ERR_INVALID, "null buffer");
+    if (!U || !y || (n > 0 && (!f || !xn))) return api_error(PB_ERR_INVALID, "bad arguments: null buffer");
     if (n > kStaticMaxPoints || m_tgt > kStaticMaxPoints)
         return api_error(PB_ERR_UNSUPPORTED,
                          "pb_fft_brinkman_static: more than 65536 sources or targets exceeds its static scratch");
+    // the grid is the caller's (no autotuning here: an autotuned grid could
+    // outgrow the array) and the support must be given
+    for (int a = 0; a < 3; a++)
+        if (M[a] <= 0) return api_error(PB_ERR_INVALID, "pb_fft_brinkman_static: M[a] must be given (> 0)");
     for (int a = 0; a < 3; a++)
         if (M[a] > kStaticMaxGrid)
             return api_error(PB_ERR_UNSUPPORTED,
                              "pb_fft_brinkman_static: grid above 64 points per axis exceeds its static scratch");
+    if (P[0] <= 0) return api_error(PB_ERR_INVALID, "pb_fft_brinkman_static: support P[0] must be > 0");
     // the parameter mapping of pb_fft_brinkman (k space only, FP64)
     pb_solve_params p;
     std::memset(&p, 0, sizeof(p));
@@ -126,16 +156,22 @@ extern "C" int pb_fft_brinkman_static(double* U, const double* y, int m_tgt, con
     p.rc = d;
     p.precision = PB_PREC_FP64;
     p.flags = PB_KSPACE;
-    StaticHeader h;
-    std::memset(&h, 0, sizeof(h));
+    StaticSetup su;
+    std::memset(&su, 0, sizeof(su));
+    StaticHeader& h = su.h;
     int rc = kspace_instance(p, &h.inst);
     if (rc) return rc;
+    // every kernel below indexes the grid the descriptor holds: it must be the
+    // caller's, within the array, with the support inside it
+    for (int a = 0; a < 3; a++)
+        if (h.inst.M[a] != M[a] || h.inst.M[a] > kStaticMaxGrid || h.inst.Pa[a] <= 0 || h.inst.Pa[a] > h.inst.M[a])
+            return api_error(PB_ERR_UNSUPPORTED, "pb_fft_brinkman_static: grid or support outside its static scratch");
     h.src_off[1] = n;
     h.tgt_off[1] = m_tgt;
-    const int Mi[3] = {M[0], M[1], M[2]};
-    alignas(16) unsigned char tw[kTwMax];
-    if (twiddle_bytes(Mi, true) > kTwMax) return api_error(PB_ERR_UNSUPPORTED, "twiddle table exceeds its slot");
-    fill_twiddles(Mi, true, tw);
+    const int Mi[3] = {h.inst.M[0], h.inst.M[1], h.inst.M[2]};
+    const size_t twn = twiddle_bytes(Mi, true);
+    if (twn > kTwMax || twn % 4) return api_error(PB_ERR_UNSUPPORTED, "twiddle table exceeds its slot");
+    fill_twiddles(Mi, true, su.tw);
     char* base = nullptr;
     rc = static_scratch(&base);
     if (rc) return rc;
@@ -146,10 +182,9 @@ extern "C" int pb_fft_brinkman_static(double* U, const double* y, int m_tgt, con
     Dbl4* tpos = (Dbl4*)(base + kOffTpos);
     double* grid = (double*)(base + kOffGrid);
     double2* spec = (double2*)(base + kOffSpec);
-    cudaError_t ce = cudaMemcpyAsync(dh, &h, sizeof(h), cudaMemcpyHostToDevice, s);
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(base + kOffTw, tw, twiddle_bytes(Mi, true), cudaMemcpyHostToDevice, s);
-    if (ce == cudaSuccess)
-        ce = cudaMemsetAsync(grid, 0, 4 * (size_t)Mi[0] * Mi[1] * Mi[2] * sizeof(double), s);
+    k_static_setup<<<1, 256, 0, s>>>(su, (unsigned*)dh, (unsigned*)(base + kOffTw), (int)twn);
+    cudaError_t ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(grid, 0, 4 * (size_t)Mi[0] * Mi[1] * Mi[2] * sizeof(double), s);
     if (ce != cudaSuccess) return api_error(PB_ERR_CUDA, cudaGetErrorString(ce));
     if (n > 0)
         k_static_records<<<(n + 255) / 256, 256, 0, s>>>(xn, f, n, L[0], L[1], L[2], spos, sfrc);

@@ -26,6 +26,7 @@ constexpr int kMaxPoly = 28;    // max terms of the far polynomial (held in regi
 constexpr int kMaxCheb = 40;    // max terms of the near and blob Chebyshev series (shared memory)
 constexpr int kNumSeries = 16;  // terms of the FP64 small-r series
 constexpr int kMaxCheb64 = 48;  // max terms of the FP64 far Chebyshev series (FP64 path)
+constexpr int kCapItems = 1;    // execution status bit: real-space work items beyond the item array
 
 // Per-instance real-space kernel tables (built in FP64 on the host).  The pair
 // kernel H = (R_eps - R_d) inside the blob region, S - R_d outside it, is

@@ -1,0 +1,134 @@
+"""GPU parity at the sizes of the benchmark configurations, against the FP64
+oracle on subsampled targets (max and RMS relative error, the convention of
+oracle.rel_errors):
+
+* the N = 1e5 uniform solve (alpha 20, eps 0.005, L 1) in mixed precision on
+  its 128^3 grid with support 12 at tol 1e-6, and on the FP64 path at tol 1e-9;
+* the N = 1e6 solve of 200 Gaussian clusters (sigma 0.02, L 2, alpha 5,
+  eps 0.002, grid 256^3) at tol 1e-6;
+* the 512-instance batch (N log-uniform in [100, 2e4], L in [0.5, 2], alpha
+  log-uniform in [1, 50], eps 0.01 L) as one plan at tol 1e-6;
+* the serving stream's large requests (N in [5e4, 2e5], targets N/2) on 128^3
+  and 256^3 slots, mixed with small ones: each the same alone and in the mix.
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import periodicbrinkman_gb300 as pb  # noqa: E402
+from periodicbrinkman_gb300.api import Plan, Server, make_params, resolve  # noqa: E402
+
+
+def cuda(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device():
+    assert torch.cuda.is_available()
+
+
+def _uniform(n, L, seed):
+    rng = np.random.default_rng(seed)
+    return rng.random((n, 3)) * L, rng.standard_normal((n, 3)), rng
+
+
+@pytest.mark.parametrize("prec,tol,M,P,bound", [("mixed", 1e-6, 128, 12, 1e-6), ("fp64", 1e-9, 0, 0, 1e-9)])
+def test_single_N1e5(prec, tol, M, P, bound):
+    n, L, alpha, eps = 100_000, 1.0, 20.0, 0.005
+    x, f, rng = _uniform(n, L, 2000)
+    u = pb.solve(cuda(x), cuda(f), L, alpha, eps, tol=tol, M=M, P=P, precision=prec).cpu().numpy()
+    assert np.isfinite(u).all()
+    idx = np.sort(rng.choice(n, 64, replace=False))
+    mx, rms = oracle.rel_errors(u[idx], oracle.ewald_velocity(x[idx], x, f, L, alpha, eps))
+    assert mx < bound and rms < bound, (mx, rms)
+
+
+def test_clustered_N1e6():
+    n, L, alpha, eps, ncl, sigma = 1_000_000, 2.0, 5.0, 0.002, 200, 0.02
+    rng = np.random.default_rng(3000)
+    centres = rng.random((ncl, 3)) * L
+    x = (centres[rng.integers(0, ncl, n)] + sigma * rng.standard_normal((n, 3))) % L
+    f = rng.standard_normal((n, 3))
+    u = pb.solve(cuda(x), cuda(f), L, alpha, eps, tol=1e-6, M=256, precision="mixed").cpu().numpy()
+    assert np.isfinite(u).all()
+    idx = np.sort(rng.choice(n, 16, replace=False))
+    mx, rms = oracle.rel_errors(u[idx], oracle.ewald_velocity(x[idx], x, f, L, alpha, eps))
+    assert mx < 1e-6 and rms < 1e-6, (mx, rms)
+
+
+def test_batch_512_instances():
+    rng = np.random.default_rng(4000)
+    inst = []
+    for _ in range(512):
+        n = int(np.exp(rng.uniform(np.log(100), np.log(20000))))
+        L = float(rng.uniform(0.5, 2.0))
+        a = float(np.exp(rng.uniform(0.0, np.log(50.0))))
+        inst.append((n, L, a, 0.01 * L, rng.random((n, 3)) * L, rng.standard_normal((n, 3))))
+    params = [make_params(n, L, a, e, tol=1e-6, precision="mixed") for n, L, a, e, _, _ in inst]
+    with Plan(params) as plan:
+        X = cuda(np.concatenate([i[4] for i in inst]))
+        F = cuda(np.concatenate([i[5] for i in inst]))
+        plan.execute(X, F)  # eager, then captured and replayed
+        U = plan.execute(X, F).cpu().numpy()
+        plan.status()
+    offs = np.cumsum([0] + [i[0] for i in inst])
+    worst = (0.0, 0.0)
+    for q in np.random.default_rng(6).choice(512, 12, replace=False):
+        n, L, a, e, x, f = inst[q]
+        sel = np.arange(min(n, 8))
+        mx, rms = oracle.rel_errors(U[offs[q]:offs[q + 1]][sel], oracle.ewald_velocity(x[sel], x, f, L, a, e))
+        worst = (max(worst[0], mx), max(worst[1], rms))
+    assert worst[0] < 1e-6 and worst[1] < 1e-6, worst
+
+
+def _grid_class(n, a, e, tol, grids=(16, 32, 64, 128, 256)):
+    M = max(resolve(make_params(n, 1.0, a, e, n_tgt=n // 2, tol=tol, precision="mixed"))["M"])
+    return next(g for g in grids if g >= M)
+
+
+def test_server_large_requests_alone_and_in_the_mix():
+    """Requests of the stream's size range on the 128^3 and 256^3 slots,
+    submitted together with small ones: every result matches the oracle on
+    64 targets and equals the same instance solved alone on its slot's grid."""
+    rng = np.random.default_rng(55)
+    reqs = []
+    want = {128: 3, 256: 2}
+    tries = 0
+    while any(v > 0 for v in want.values()) and tries < 4000:
+        tries += 1
+        n = int(np.exp(rng.uniform(np.log(5e4), np.log(2e5))))
+        a = float(np.exp(rng.uniform(0, np.log(50))))
+        e = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e-2))))
+        g = _grid_class(n, a, e, 1e-6)
+        if want.get(g, 0) > 0:
+            want[g] -= 1
+            reqs.append((n, a, e, 1e-6, g))
+    assert not any(v > 0 for v in want.values()), want
+    for _ in range(4):  # small requests share the batches of the small grids
+        n = int(rng.integers(1000, 4000))
+        a = float(np.exp(rng.uniform(0, np.log(50))))
+        e = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e-2))))
+        reqs.append((n, a, e, 1e-6, _grid_class(n, a, e, 1e-6)))
+    data = []
+    for n, a, e, tol, g in reqs:
+        x, f, _ = _uniform(n, 1.0, int(rng.integers(1 << 30)))
+        y = rng.random((n // 2, 3))
+        data.append((x, f, y))
+    with Server(precision="mixed", budget_bytes=40 << 30, max_batch=4, slots_per_grid=1,
+                grids=(16, 32, 64, 128, 256), max_src=200_000, max_tgt=100_001, linger_us=20000) as srv:
+        tickets = [srv.submit(x, f, 1.0, a, e, y=y, tol=tol) for (x, f, y), (n, a, e, tol, g) in zip(data, reqs)]
+        outs = [srv.result(t, timeout=600)[0] for t in tickets]
+        st = srv.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    for k, ((x, f, y), (n, a, e, tol, g), U) in enumerate(zip(data, reqs, outs)):
+        assert np.isfinite(U).all(), k
+        alone = pb.solve(cuda(x), cuda(f), 1.0, a, e, y=cuda(y), tol=tol, M=g).cpu().numpy()
+        assert np.abs(U - alone).max() <= 1e-6 * np.abs(alone).max(), (k, n, g)
+        sel = np.sort(rng.choice(y.shape[0], 64, replace=False))
+        mx, rms = oracle.rel_errors(U[sel], oracle.ewald_velocity(y[sel], x, f, 1.0, a, e))
+        assert mx < 1e-6 and rms < 1e-6, (k, n, g, mx, rms)

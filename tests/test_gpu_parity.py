@@ -216,3 +216,29 @@ def test_host_non_finite_inputs_found_on_device(prec):
         again = plan.execute(x, f, y=y)
     # atomics make the summation order vary between runs: equal to rounding
     assert np.abs(again - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_item_capacity_overflow_is_an_error(prec):
+    """Real-space work items beyond the plan's item array are reported (an
+    error, not silently dropped pairs), on host and device buffers; at full
+    capacity the same plan runs clean again."""
+    from periodicbrinkman_gb300 import _lib
+
+    x, f, _ = _case(4000, 1.0, 23)
+    p = make_params(4000, 1.0, 10.0, 0.01, tol=1e-6, precision=prec)
+    with Plan(p) as plan:
+        ref = plan.execute(x, f)
+        full = 4 * 4000 + 4096
+        plan.set_item_capacity(8)
+        with pytest.raises(pb.PbError) as ei:
+            plan.execute(x, f)
+        assert ei.value.code == _lib.PB_ERR_UNSUPPORTED and "item capacity" in str(ei.value)
+        plan.execute(cuda(x), cuda(f))
+        with pytest.raises(pb.PbError) as ei:
+            plan.status()
+        assert ei.value.code == _lib.PB_ERR_UNSUPPORTED
+        plan.set_item_capacity(full)
+        again = plan.execute(x, f)
+        plan.status()
+    assert np.abs(again - ref).max() <= 1e-6 * np.abs(ref).max()

@@ -48,7 +48,16 @@ def _static_call(y, f, x, L, M, P, msd, e, d, alpha, stream):
     return Ud.cpu().numpy()
 
 
+# Against the FP64 oracle's direct k-space sum, max relative error: the
+# spectral sum carries the Gaussian window's truncation exp(-(P/2 - 1)^2 / s)
+# and aliasing, s = eta / h^2 = P^2 / (2 msd^2): 1e-7 for the reference's
+# parameters (P 16, msd 7), 3.7e-6 truncation for P 12, msd 6.
+ORACLE_TOL = {41: 1e-7, 42: 2e-5}
+
+
 def test_static_entry_matches_fft_brinkman_on_two_calls():
+    import oracle
+
     assert torch.cuda.is_available()
     stream = torch.cuda.Stream()
     cases = [
@@ -62,6 +71,11 @@ def test_static_entry_matches_fft_brinkman_on_two_calls():
         got = _static_call(y, f, x, L, M, P, msd, e, d, a, stream)
         assert np.isfinite(got).all()
         assert np.abs(got - ref).max() <= TOL * np.abs(ref).max(), (seed, np.abs(got - ref).max())
+        # and against the FP64 oracle's k-space sum on a subset of the targets
+        sel = np.arange(0, m, max(1, m // 40))
+        uo = oracle.ewald_velocity(y[sel], x, f, np.asarray(L), a, e, d=d, real=False)
+        mx, _ = oracle.rel_errors(got[sel], uo)
+        assert mx < ORACLE_TOL[seed], (seed, mx)
 
 
 def test_static_entry_rejects_sizes_beyond_its_scratch():
@@ -70,3 +84,8 @@ def test_static_entry_rejects_sizes_beyond_its_scratch():
         _static_call(y, f, x, [1.0, 1.0, 1.0], [128, 128, 128], [16, 16, 16], 7, 0.01, 0.125, 10.0,
                      torch.cuda.Stream())
     assert ei.value.code == _lib.PB_ERR_UNSUPPORTED and "static scratch" in str(ei.value)
+    # no autotuned grid: an unset grid or support is refused before anything runs
+    for M, P in (([0, 0, 0], [16, 16, 16]), ([64, 0, 64], [16, 16, 16]), ([64, 64, 64], [0, 0, 0])):
+        with pytest.raises(_lib.PbError) as ei:
+            _static_call(y, f, x, [1.0, 1.0, 1.0], M, P, 7, 0.01, 0.125, 10.0, torch.cuda.Stream())
+        assert ei.value.code == _lib.PB_ERR_INVALID
