@@ -143,6 +143,23 @@ int pb_fft_brinkman_static(double* U, const double* y, int m_tgt, const double* 
                            const double* L, const int* M, const int* P, int msd, double e, double d, double alpha,
                            void* stream);
 
+/* Free-space (non-periodic) Brinkmanlet, the GPU counterpart of the
+ * reference's Brinkmanlet() (cuda/periodicBrinkman.h:119-141): the
+ * regularized R_eps of regH (53-78) for eps > 0, the singular S of singH
+ * (31-46) for eps = 0.  Velocities U (3 x m) at targets y (3 x m) of forces
+ * f (3 x n) at x (3 x n), overwritten; a direct FP64 sum (O(m n)).  where =
+ * PB_HOST (copies in and out, synchronous) or PB_DEVICE (queued on stream).
+ * With eps = 0 a coincident pair (r <= 1e-12) has no finite velocity and is
+ * skipped. */
+int pb_brinkmanlet(double* U, const double* y, int m, const double* x, const double* f, int n, double alpha,
+                   double eps, int where, void* stream);
+/* The dense form: dA (DEVICE, 3m x 3n column-major, the layout of
+ * pb_periodic_brinkman) += the Brinkmanlet tensor of every (target, source)
+ * pair, queued on stream.  A coincident singular pair gets singH's sentinel
+ * 1.79e308 on its diagonal, as the reference's Brinkmanlet does. */
+int pb_brinkmanlet_matrix(double* dA, const double* dx, int m, const double* dx0, int n, double alpha, double eps,
+                          void* stream);
+
 /* ---- evaluator ----------------------------------------------------------- */
 
 /* One-shot solve.  x, f: 3 x n_src; y: 3 x n_tgt (NULL when n_tgt == 0);
@@ -181,6 +198,29 @@ long long pb_plan_device_bytes(pb_plan plan);
 /* CUDA kernels one execution launches (kernel nodes of the captured graph;
  * 0 before the graph exists, i.e. before the second pb_plan_execute). */
 int pb_plan_kernel_count(pb_plan plan);
+/* One row of pb_tune_report. */
+typedef struct pb_tune_row {
+    int status;              /* PB_OK, or the error this candidate met (then max_err = rms_err = -1) */
+    double d, rc;            /* splitting blob width and real-space cutoff it resolved to */
+    int M[3], P;             /* grid and Gaussian support it resolved to */
+    long long pairs_est;     /* estimated real-space pairs inside rc */
+    double max_err, rms_err; /* against the reference solution: max_i |u_i - u*_i| / max_i |u*_i|, ||u - u*|| / ||u*|| */
+    double ms;               /* device time of one execution (CUDA events, median of three replays) */
+} pb_tune_row;
+
+/* Error-versus-parameter report and splitting-independence study, the
+ * concept of the reference's optimalNumShells (cuda/periodicBrinkman.h:
+ * 836-1015, commented out there) and of its driver's d study
+ * (cuda/periodicBrinkman.cu:139-203): the instance p with x, f (and y when
+ * p->n_tgt > 0; where = PB_HOST or PB_DEVICE) is solved once per candidate
+ * splitting width d_values[k] (0 = the autotuner's choice; p's other tuning
+ * fields kept, 0 = autotuned for that d), and each result is compared with
+ * a reference solution of the same instance: the FP64 path at tolerance
+ * ref_tol (0 = 1e-12) with every tuning field autotuned.  The Ewald total
+ * does not depend on d, so a row whose error exceeds p->tol marks a
+ * parameter choice that misses the tolerance.  Allocates; synchronous. */
+int pb_tune_report(const pb_solve_params* p, const double* x, const double* f, const double* y, int where,
+                   const double* d_values, int nd, double ref_tol, pb_tune_row* rows);
 /* Bytes a plan for these parameters would hold (for admission control). */
 long long pb_plan_estimate_bytes(const pb_solve_params* p, int count);
 /* Per-stage device time of the last pb_plan_execute (ms), if timing was
@@ -242,6 +282,25 @@ int pb_server_release(pb_server s, long long ticket);
 int pb_server_drain(pb_server s, double timeout_s);
 int pb_server_stats(pb_server s, pb_server_counters* out);
 int pb_server_destroy(pb_server s);
+
+/* ---- parameter files --------------------------------------------------- */
+
+/* Mirrors readData's array twin (cuda/periodicBrinkman.h:524-554): reads the
+ * text file's lines, splits each at any character of `delimiters` (NULL =
+ * ": "), and where the first token equals names[k] stores the second token,
+ * converted as atof does, in values[k]; other lines are ignored and values
+ * of names absent from the file are left as they are.  PB_ERR_INVALID if the
+ * file cannot be opened (the reference returns 1) or a line has a name but
+ * no value. */
+int pb_read_params(const char* file_name, const char* delimiters, const char* const* names, double* values,
+                   int numel);
+/* Mirrors readData's map form (cuda/periodicBrinkman.cu:44-70): every name
+ * of the file with its value (a later line overrides an earlier one), in
+ * order of first appearance.  Writes up to max_keys names (NUL-terminated,
+ * at most 63 characters) and values; returns the number of distinct names
+ * (which may exceed max_keys: call again with more room) or an error. */
+int pb_read_param_file(const char* file_name, const char* delimiters, char (*keys)[64], double* values,
+                       int max_keys);
 
 /* ---- misc ----------------------------------------------------------------- */
 const char* pb_last_error(void);

@@ -132,6 +132,8 @@ def lib():
         L.pbo_get_eps_switch.restype = C.c_double
         L.pbo_phihat.restype = C.c_double
         L.pbo_phihat.argtypes = [C.c_double] * 3
+        L.pbo_brinkmanlet.argtypes = [_dp, _dp, C.c_double, C.c_double]
+        L.pbo_brinkmanlet_velocity.argtypes = [_dp, _dp, C.c_int, _dp, _dp, C.c_int, C.c_double, C.c_double]
         L.pbo_num_threads.restype = C.c_int
         L.pbo_set_num_threads.argtypes = [C.c_int]
     return _lib
@@ -260,6 +262,24 @@ def ewald_velocity(y, x, f, L, alpha, eps, d=None, rc=0.0, kc=0.0, real=True, ks
                                      float(d), float(rc), float(kc), flags)
     if rcode != 0:
         raise ValueError("oracle: bad input")
+    return U
+
+
+def brinkmanlet(xh, alpha, d):
+    """The reference's Brinkmanlet tensor (3x3) at displacement xh (faithful closed forms)."""
+    A = np.zeros(9)
+    xv = _c64(xh).reshape(3)
+    lib().pbo_brinkmanlet(_p(A), _p(xv), float(alpha), float(d))
+    return A.reshape(3, 3).T  # column-major storage -> (row, col)
+
+
+def brinkmanlet_velocity(y, x, f, alpha, eps):
+    """Free-space (non-periodic) velocities at y of forces f at x, accurate FP64 kernel."""
+    y = _c64(y).reshape(-1, 3)
+    x = _c64(x).reshape(-1, 3)
+    f = _c64(f).reshape(-1, 3)
+    U = np.zeros_like(y)
+    lib().pbo_brinkmanlet_velocity(_p(U), _p(y), y.shape[0], _p(x), _p(f), x.shape[0], float(alpha), float(eps))
     return U
 
 

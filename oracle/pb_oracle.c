@@ -742,3 +742,65 @@ int pbo_ewald_velocity(double *U, const double *y, int m, const double *x, const
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Free-space Brinkmanlet (no periodicity)                             */
+/* ------------------------------------------------------------------ */
+
+/* The reference's Brinkmanlet(A, xh, a, d) (cuda/periodicBrinkman.h:119-141):
+ * A = H1 I + H2 xh xh^T with regH (d > 0) or singH (d = 0), the faithful
+ * closed forms with the switch radius; A is 3x3 column-major. */
+void pbo_brinkmanlet(double *A, const double *xh, double a, double d)
+{
+    double H1, H2, r2 = xh[0] * xh[0] + xh[1] * xh[1] + xh[2] * xh[2];
+    if (d > 0)
+        pbo_regH(r2, a, d, &H1, &H2);
+    else
+        pbo_singH(r2, a, &H1, &H2);
+    for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) A[3 * j + i] = xh[i] * xh[j] * H2 + (i == j ? H1 : 0.0);
+}
+
+/* Accurate free-space kernel: R_e (e > 0) from its Fourier integral where
+ * r < 0.2 e or alpha r < 0.2 (the closed forms cancel there), else the
+ * closed forms of regH; S (e = 0) without the small-alpha r cancellation. */
+static void free_pairH(double r, double a, double e, double *H1, double *H2)
+{
+    if (e > 0) {
+        if (r < 0.2 * e || (a * r < 0.2 && r < 9 * e)) {
+            pbo_reg_quad(r, a, e, e, 0, H1, H2);
+            return;
+        }
+        double sw = g_eps_switch;
+        g_eps_switch = -1.0;
+        pbo_regH(r * r, a, e, H1, H2);
+        g_eps_switch = sw;
+        return;
+    }
+    stable_S(r, a, H1, H2);
+}
+
+/* Free-space velocities u_i = sum_j (H1 I + H2 x x^T) f_j, x = y_i - x_j,
+ * with the accurate kernel; for e = 0, coincident pairs (r <= 1e-12) are
+ * skipped (no finite velocity).  OpenMP over targets. */
+void pbo_brinkmanlet_velocity(double *U, const double *y, int m, const double *x, const double *f, int n,
+                              double a, double e)
+{
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i = 0; i < m; i++) {
+        double u0 = 0, u1 = 0, u2 = 0;
+        for (int j = 0; j < n; j++) {
+            double dx = y[3 * i] - x[3 * j], dy = y[3 * i + 1] - x[3 * j + 1], dz = y[3 * i + 2] - x[3 * j + 2];
+            double r = sqrt(dx * dx + dy * dy + dz * dz), H1, H2;
+            if (e == 0 && r <= 1e-12) continue;
+            free_pairH(r, a, e, &H1, &H2);
+            double g = H2 * (f[3 * j] * dx + f[3 * j + 1] * dy + f[3 * j + 2] * dz);
+            u0 += H1 * f[3 * j] + g * dx;
+            u1 += H1 * f[3 * j + 1] + g * dy;
+            u2 += H1 * f[3 * j + 2] + g * dz;
+        }
+        U[3 * i] = u0;
+        U[3 * i + 1] = u1;
+        U[3 * i + 2] = u2;
+    }
+}

@@ -9,8 +9,10 @@
  * normalisation pi^{3/2} = PI*SPI of the Gaussian blob), the switch radius
  * `eps`, dot() on 3-vectors, host and device column-major matrices
  * (MatrixOnHost / MatrixOnDevice), chooseSize() and warpReduce().  Only the
- * members the reference calls are provided.  The reference's kernels are
- * compiled but never launched by the fixture generator.
+ * members the reference calls are provided, plus data() (the column-major
+ * storage, for include/pbrinkman.hpp's overloads in tests/cxx/).  The
+ * reference's kernels are compiled into oracle/_ref/ref_kernels.* and
+ * launched by oracle/ref_launch.cpp, never by the fixture generator.
  */
 #ifndef PB_REF_SHIM_MATRIX_H
 #define PB_REF_SHIM_MATRIX_H
@@ -45,6 +47,7 @@ class MatrixOnHost {
     operator const double *() const { return d_.data(); }
     void setElements(double v) { for (auto &x : d_) x = v; }
     double *data() { return d_.data(); }
+    const double *data() const { return d_.data(); }
 
   private:
     int r_, c_;
@@ -56,6 +59,7 @@ struct MatrixOnDevice {
     int r, c;
     __host__ __device__ int rows() const { return r; }
     __host__ __device__ int columns() const { return c; }
+    __host__ __device__ double *data() const { return p; }
     __device__ double &operator()(int i, int j) { return p[(size_t)j * r + i]; }
     __device__ double operator()(int i, int j) const { return p[(size_t)j * r + i]; }
 };
@@ -67,6 +71,7 @@ inline unsigned chooseSize(unsigned n, unsigned maxBit = 16)
     return s;
 }
 
+#ifdef __CUDACC__  /* device code: only in CUDA translation units (a host C++ caller includes this too) */
 __device__ inline void warpReduce(double *U, unsigned tid, unsigned blockSize)
 {
     for (unsigned s = 32; s > 0; s >>= 1) {
@@ -74,4 +79,5 @@ __device__ inline void warpReduce(double *U, unsigned tid, unsigned blockSize)
         __syncwarp();
     }
 }
+#endif
 #endif

@@ -9,6 +9,8 @@ module is the host-side mirror of the reference's entry points:
   arrays, accumulates into dA);
 * ``fftBrinkman(U, y, f, xn, L, M, P, m, C, e, tol, d, alpha=1)`` -- the
   k-space velocities of cuda/fftBrinkman.h:34-287 (host arrays, U overwritten);
+* ``Brinkmanlet(y, x, f, alpha, eps)`` -- free-space velocities of the
+  reference's Brinkmanlet (cuda/periodicBrinkman.h:119-141);
 
 plus the full evaluator (real + k space + self), batched plans and the
 continuous-batching server.  There is no CPU fallback: without the built
@@ -31,10 +33,13 @@ from ._lib import (  # noqa: F401
     lib,
     lib_path,
 )
-from .api import (Plan, Server, fftBrinkman, pair_kernel_tables, pair_kernel_tables64, periodicBrinkman,  # noqa: F401
-                  shell_counts, solve)
+from .api import (Brinkmanlet, Plan, Server, brinkmanlet_matrix, fftBrinkman, pair_kernel_tables,  # noqa: F401
+                  pair_kernel_tables64, periodicBrinkman, read_data, read_data_array, shell_counts, solve,
+                  tune_report)
 
 __all__ = [
+    "Brinkmanlet",
+    "brinkmanlet_matrix",
     "PbError",
     "Plan",
     "Server",
@@ -43,6 +48,9 @@ __all__ = [
     "periodicBrinkman",
     "solve",
     "shell_counts",
+    "tune_report",
+    "read_data",
+    "read_data_array",
     "pair_kernel_tables",
     "pair_kernel_tables64",
     "device_count",

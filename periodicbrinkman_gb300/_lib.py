@@ -87,6 +87,20 @@ class SlotConfig(C.Structure):
     ]
 
 
+class TuneRow(C.Structure):
+    _fields_ = [
+        ("status", C.c_int),
+        ("d", C.c_double),
+        ("rc", C.c_double),
+        ("M", C.c_int * 3),
+        ("P", C.c_int),
+        ("pairs_est", C.c_longlong),
+        ("max_err", C.c_double),
+        ("rms_err", C.c_double),
+        ("ms", C.c_double),
+    ]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [
         ("budget_bytes", C.c_longlong),
@@ -173,6 +187,12 @@ def lib():
     L.pb_debug_pair_kernel.argtypes = [C.c_double] * 4 + [C.c_int, dp, dp, dp]
     L.pb_debug_pair_kernel64.argtypes = [C.c_double] * 4 + [C.c_int, dp, dp, dp]
     L.pb_debug_fft_green.argtypes = [C.POINTER(SolveParams), vp, vp]
+    L.pb_read_params.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), dp, C.c_int]
+    L.pb_read_param_file.argtypes = [C.c_char_p, C.c_char_p, C.c_void_p, dp, C.c_int]
+    L.pb_tune_report.argtypes = [C.POINTER(SolveParams), vp, vp, vp, C.c_int, dp, C.c_int, C.c_double,
+                                 C.POINTER(TuneRow)]
+    L.pb_brinkmanlet.argtypes = [vp, vp, C.c_int, vp, vp, C.c_int, C.c_double, C.c_double, C.c_int, vp]
+    L.pb_brinkmanlet_matrix.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_double, C.c_double, vp]
     L.pb_plan_create_slot.argtypes = [C.POINTER(SlotConfig), C.POINTER(vp)]
     L.pb_slot_estimate_bytes.restype = C.c_longlong
     L.pb_slot_estimate_bytes.argtypes = [C.POINTER(SlotConfig)]

@@ -22,6 +22,7 @@ from ._lib import (
     ServerCounters,
     SlotConfig,
     SolveParams,
+    TuneRow,
     check,
     lib,
 )
@@ -302,6 +303,22 @@ def resolve(params: SolveParams) -> dict:
             "ncell": list(inf.ncell), "npoly": inf.npoly, "pairs_est": int(inf.pairs_est)}
 
 
+def tune_report(x, f, L, alpha, eps, y=None, d_values=(0.0,), ref_tol: float = 0.0, **kw) -> list[dict]:
+    """pb_tune_report: per candidate splitting width (0 = autotuned) the
+    resolved (d, rc, M, P), the max / RMS relative error against the FP64
+    reference solution at ref_tol (0 = 1e-12), and the device time (ms)."""
+    n = int(x.shape[0])
+    m = int(y.shape[0]) if y is not None else 0
+    p = make_params(n, L, alpha, eps, n_tgt=m, **kw)
+    where = _where([x, f, y])
+    dv = np.ascontiguousarray(d_values, dtype=np.float64)
+    rows = (TuneRow * max(len(dv), 1))()
+    check(lib().pb_tune_report(C.byref(p), _ptr(x), _ptr(f), _ptr(y), where, dv.ctypes.data_as(_dp), len(dv),
+                               float(ref_tol), rows))
+    return [{"status": r.status, "d": r.d, "rc": r.rc, "M": list(r.M), "P": r.P, "pairs_est": int(r.pairs_est),
+             "max_err": r.max_err, "rms_err": r.rms_err, "ms": r.ms} for r in rows[:len(dv)]]
+
+
 def estimate_bytes(params: SolveParams | Iterable[SolveParams]) -> int:
     if isinstance(params, SolveParams):
         params = [params]
@@ -356,6 +373,73 @@ def fftBrinkman(U, y, f, xn, L, M, P, m, C_, e, tol, d, alpha=1.0):
                                 Lv.ctypes.data_as(_dp), Mv.ctypes.data_as(_ip), Pv.ctypes.data_as(_ip), int(m), int(C_),
                                 float(e), float(tol), float(d), float(alpha)))
     return U
+
+
+def Brinkmanlet(y, x, f, alpha: float, eps: float = 0.0, U=None, stream=None):
+    """Free-space velocities (m, 3) at y of forces f at x: the reference's
+    Brinkmanlet (cuda/periodicBrinkman.h:119-141), regularized (eps > 0) or
+    singular (eps = 0), summed directly on the GPU in FP64.  Host numpy or
+    device torch buffers (all alike)."""
+    m, n = int(y.shape[0]), int(x.shape[0])
+    if U is None:
+        if _is_torch(y):
+            import torch
+
+            U = torch.empty((m, 3), dtype=torch.float64, device=y.device)
+        else:
+            U = np.empty((m, 3))
+    where = _where([y, x, f, U])
+    s = None
+    if stream is not None:
+        s = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+    check(lib().pb_brinkmanlet(_ptr(U), _ptr(y), m, _ptr(x), _ptr(f), n, float(alpha), float(eps), where, s))
+    return U
+
+
+def brinkmanlet_matrix(dA, dx, dx0, alpha: float, eps: float = 0.0, stream=None):
+    """dA (device, (3m, 3n) column-major) += the free-space Brinkmanlet tensors."""
+    if not (_is_torch(dA) and dA.is_cuda):
+        raise ValueError("brinkmanlet_matrix works on device tensors")
+    m, n = int(dx.shape[0]), int(dx0.shape[0])
+    if tuple(dA.shape) != (3 * m, 3 * n) or not dA.t().is_contiguous():
+        raise ValueError("dA must be (3m, 3n) column-major")
+    s = None
+    if stream is not None:
+        s = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+    check(lib().pb_brinkmanlet_matrix(dA.data_ptr(), _ptr(dx), m, _ptr(dx0), n, float(alpha), float(eps), s))
+    return dA
+
+
+def read_data(file_name: str, params: dict | None = None, delimiters: str = ": ") -> dict:
+    """readData's map form (cuda/periodicBrinkman.cu:44-70): the file's
+    "name<delimiters>value" lines into `params` (created if None; entries of
+    names absent from the file keep their values, e.g. the defaults the
+    reference's driver sets at cuda/periodicBrinkman.cu:78-87)."""
+    params = {} if params is None else params
+    cap = 64
+    while True:
+        keys = (C.c_char * 64 * cap)()
+        vals = np.zeros(cap)
+        n = lib().pb_read_param_file(str(file_name).encode(), delimiters.encode(), keys, vals.ctypes.data_as(_dp),
+                                     cap)
+        if n < 0:
+            check(n)
+        if n <= cap:
+            break
+        cap = n
+    for k in range(n):
+        params[bytes(keys[k]).split(b"\0", 1)[0].decode()] = float(vals[k])
+    return params
+
+
+def read_data_array(file_name: str, names, values=None, delimiters: str = ": "):
+    """readData's array twin (cuda/periodicBrinkman.h:524-554): values[k] for names[k]."""
+    names = list(names)
+    vals = np.zeros(len(names)) if values is None else np.ascontiguousarray(values, dtype=np.float64)
+    arr = (C.c_char_p * max(len(names), 1))(*[s.encode() for s in names])
+    check(lib().pb_read_params(str(file_name).encode(), delimiters.encode(), arr, vals.ctypes.data_as(_dp),
+                               len(names)))
+    return vals
 
 
 def shell_counts(L, M: int, N: int):

@@ -8,8 +8,9 @@ oracle.rel_errors):
   eps 0.002, grid 256^3) at tol 1e-6;
 * the 512-instance batch (N log-uniform in [100, 2e4], L in [0.5, 2], alpha
   log-uniform in [1, 50], eps 0.01 L) as one plan at tol 1e-6;
-* the serving stream's large requests (N in [5e4, 2e5], targets N/2) on 128^3
-  and 256^3 slots, mixed with small ones: each the same alone and in the mix.
+* the serving stream's large requests (N in [5e4, 2e5], targets N/2) on the
+  128^3 slot (where the autotuner puts them) and on the 256^3 slot (grid asked
+  for), mixed with small ones: each the same alone and in the mix.
 """
 import numpy as np
 import pytest
@@ -96,36 +97,34 @@ def test_server_large_requests_alone_and_in_the_mix():
     submitted together with small ones: every result matches the oracle on
     64 targets and equals the same instance solved alone on its slot's grid."""
     rng = np.random.default_rng(55)
-    reqs = []
-    want = {128: 3, 256: 2}
-    tries = 0
-    while any(v > 0 for v in want.values()) and tries < 4000:
-        tries += 1
+    reqs = []  # (N, alpha, eps, tol, slot grid, grid asked for: 0 = autotuned)
+    want = 3
+    while want > 0:  # the autotuner puts the stream's large requests on 128^3
         n = int(np.exp(rng.uniform(np.log(5e4), np.log(2e5))))
         a = float(np.exp(rng.uniform(0, np.log(50))))
         e = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e-2))))
-        g = _grid_class(n, a, e, 1e-6)
-        if want.get(g, 0) > 0:
-            want[g] -= 1
-            reqs.append((n, a, e, 1e-6, g))
-    assert not any(v > 0 for v in want.values()), want
+        if _grid_class(n, a, e, 1e-6) == 128:
+            want -= 1
+            reqs.append((n, a, e, 1e-6, 128, 0))
+    for n, a, e in ((180_000, 30.0, 0.002), (120_000, 8.0, 0.005)):  # the 256^3 slot, asked for explicitly
+        reqs.append((n, a, e, 1e-6, 256, 256))
     for _ in range(4):  # small requests share the batches of the small grids
         n = int(rng.integers(1000, 4000))
         a = float(np.exp(rng.uniform(0, np.log(50))))
         e = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e-2))))
-        reqs.append((n, a, e, 1e-6, _grid_class(n, a, e, 1e-6)))
+        reqs.append((n, a, e, 1e-6, _grid_class(n, a, e, 1e-6), 0))
     data = []
-    for n, a, e, tol, g in reqs:
+    for n, a, e, tol, g, Mq in reqs:
         x, f, _ = _uniform(n, 1.0, int(rng.integers(1 << 30)))
         y = rng.random((n // 2, 3))
         data.append((x, f, y))
     with Server(precision="mixed", budget_bytes=40 << 30, max_batch=4, slots_per_grid=1,
                 grids=(16, 32, 64, 128, 256), max_src=200_000, max_tgt=100_001, linger_us=20000) as srv:
-        tickets = [srv.submit(x, f, 1.0, a, e, y=y, tol=tol) for (x, f, y), (n, a, e, tol, g) in zip(data, reqs)]
+        tickets = [srv.submit(x, f, 1.0, a, e, y=y, tol=tol, M=Mq) for (x, f, y), (n, a, e, tol, g, Mq) in zip(data, reqs)]
         outs = [srv.result(t, timeout=600)[0] for t in tickets]
         st = srv.stats()
     assert st["completed"] == len(reqs) and st["failed"] == 0
-    for k, ((x, f, y), (n, a, e, tol, g), U) in enumerate(zip(data, reqs, outs)):
+    for k, ((x, f, y), (n, a, e, tol, g, Mq), U) in enumerate(zip(data, reqs, outs)):
         assert np.isfinite(U).all(), k
         alone = pb.solve(cuda(x), cuda(f), 1.0, a, e, y=cuda(y), tol=tol, M=g).cpu().numpy()
         assert np.abs(U - alone).max() <= 1e-6 * np.abs(alone).max(), (k, n, g)

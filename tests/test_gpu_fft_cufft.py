@@ -28,7 +28,8 @@ TOL = {"mixed": 5e-6, "fp64": 1e-12}
 def _green_cufft(G, L, M, alpha, d, eta):
     """G: (3, M0, M1, M2) float64 CUDA tensor -> the operator's output, via torch.fft."""
     L = np.asarray(L, dtype=np.float64)
-    kfac = np.prod(L / np.asarray(M)) / (np.prod(M) * (np.pi * eta) ** 1.5)
+    # the normalisations of spreading and gathering, (pi eta)^{-3/2} each, and h^3 / M^3
+    kfac = np.prod(L / np.asarray(M)) / (np.prod(M) * (np.pi * eta) ** 3)
     Gh = torch.fft.rfftn(G, dim=(1, 2, 3), norm="backward")  # unnormalised forward
     dev = G.device
     n0 = torch.fft.fftfreq(M[0], d=1.0 / M[0], dtype=torch.float64, device=dev)
