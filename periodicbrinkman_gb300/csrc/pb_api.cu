@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -739,6 +740,17 @@ void bin_and_sort(pb_plan_s* P, const double* pos, int n, const int* d_off, int*
     launch_sort_cells(perm_tmp, perm, start, P->ncell, P->d_cell_off, P->d_inst, P->count, pos, P->nsm, s);
 }
 
+// PB_SPREAD=atomic selects the point-wise spreading kernel (with a grid
+// clear) in place of the tiled one, for comparing the two.
+bool spread_atomic()
+{
+    static const bool v = [] {
+        const char* e = std::getenv("PB_SPREAD");
+        return e && std::strcmp(e, "atomic") == 0;
+    }();
+    return v;
+}
+
 void record(pb_plan_s* P, int k, cudaStream_t s)
 {
     if (P->timing) cudaEventRecord(P->tev[k], s);
@@ -795,13 +807,19 @@ void run_compute(pb_plan_s* P, cudaStream_t s, bool forces_only)
     record(P, 2, s);
     nvtxRangePushA("pb.kspace");
     if (P->any_k) {
-        launch_zero_grids(P->d_inst, P->count, P->grid, mixed ? 4 : 8, s);
-        if (mixed)
+        if (mixed && !spread_atomic()) {
+            for (auto& B : P->buckets)
+                launch_spread_tiles(P->d_inst, B.d_inst, (int)B.inst.size(), B.M, P->start_s, (const float4*)P->spos_a,
+                                    (const float4*)P->spos_b, (const float4*)P->sfrc, (float*)P->grid, s);
+        } else if (mixed) {
+            launch_zero_grids(P->d_inst, P->count, P->grid, 4, s);
             launch_spread<float>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
                                  (float*)P->grid, s);
-        else
+        } else {
+            launch_zero_grids(P->d_inst, P->count, P->grid, 8, s);
             launch_spread<double>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
                                   (double*)P->grid, s);
+        }
         record(P, 3, s);
         for (auto& B : P->buckets) {
             const PbInst& I0 = P->hinst[B.inst[0]];

@@ -69,6 +69,12 @@ void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int nc
 template <class T>
 void launch_kspace_fft(const PbInst* inst_dev, const int* bucket_inst, int ninst_bucket, long long base_off,
                        const int* M, T* grid, void* spec, const void* twiddles, cudaStream_t s);
+// FP32 grids of one grid-size bucket, tile by tile (pb_spread.cu): `nb`
+// instances bucket_inst[0..nb) of grid M, points from the source cell list
+// (src_start, sorted records); every tile of a live instance is written
+// whole, so the grids need no clearing.
+void launch_spread_tiles(const PbInst* inst, const int* bucket_inst, int nb, const int* M, const int* src_start,
+                         const float4* pos_a, const float4* pos_b, const float4* frc, float* grid, cudaStream_t s);
 // Zeroes the grids (4 M^3 elements of esz bytes) of instances with sources or targets.
 void launch_zero_grids(const PbInst* inst, int ninst, void* grid, int esz, cudaStream_t s);
 size_t twiddle_bytes(const int* M, bool fp64);
