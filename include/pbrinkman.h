@@ -242,35 +242,48 @@ int pb_plan_destroy(pb_plan plan);
 /* ---- continuous-batching server ------------------------------------------- */
 
 typedef struct pb_server_config {
-    long long budget_bytes; /* device memory for resident slots (0: 150 GiB) */
+    long long budget_bytes; /* device memory for all slots, resident and dynamic (0: 150 GiB) */
     int precision;          /* PB_PREC_MIXED or PB_PREC_FP64 */
     int max_batch;          /* instances per slot execution (0: 16) */
-    int slots_per_grid;     /* concurrent slots per grid size (0: 2) */
+    int slots_per_grid;     /* resident slots per grid size, created with the server (0: 2) */
     int n_grids;            /* grid sizes provisioned (0: 8, 16, ..., 256) */
     int grids[8];
-    int max_src;            /* source capacity of a slot = largest request (0: 262144) */
-    int max_tgt;            /* target capacity of a slot (0: max_src) */
+    int max_src;            /* source capacity of a resident slot (0: 262144) */
+    int max_tgt;            /* target capacity of a resident slot (0: max_src) */
     int queue_capacity;     /* pending requests before PB_ERR_BUSY (0: unbounded) */
     int linger_us;          /* an idle slot waits up to this long for a fuller batch (0: dispatch at once) */
+    int max_dynamic_per_grid; /* dynamic slots per grid made from the unused budget (0: slots_per_grid; < 0: none) */
+    int dynamic_idle_ms;    /* an idle dynamic slot is released after this long (0: 1000) */
 } pb_server_config;
 
 typedef struct pb_server_counters {
     long long submitted, completed, failed, rejected, batches;
     double mean_batch;      /* instances per slot execution */
-    long long device_bytes; /* held by the slots */
-    int slots;
+    long long device_bytes; /* held by the slots now */
+    int slots;              /* slots now (resident + dynamic) */
     long long kernels;      /* kernel launches of the slot executions (graph kernel nodes) */
     double scheduler_busy_s; /* time the scheduler thread spent binding, staging and launching */
+    long long peak_device_bytes; /* most device memory the slots held at once */
+    long long slots_created, slots_released; /* dynamic slots made and given back */
+    long long memory_waits; /* times a request waited for device memory to free up */
 } pb_server_counters;
 
 typedef struct pb_server_s* pb_server;
 
-/* Creates the resident slots within the budget and starts the scheduler. */
+/* Creates the resident slots within the budget and starts the scheduler.
+ * Admission is by device-memory budget: a request that no slot of its grid
+ * can hold gets a dynamic slot sized for it, and a grid whose queue backs up
+ * while its slots are busy gets extra dynamic slots, both from the part of
+ * the budget the slots do not hold; when the budget is taken, the request
+ * waits in its queue while idle dynamic slots are released, and is admitted
+ * as memory frees up.  Idle dynamic slots are also released after
+ * dynamic_idle_ms. */
 int pb_server_create(const pb_server_config* cfg, pb_server* out);
 /* Queue one solve (HOST buffers the caller keeps alive until it completes;
  * U receives 3 x n_tgt, or 3 x n_src when n_tgt = 0).  The request is
  * autotuned here and assigned to the smallest provisioned grid that holds
- * its k-space resolution.  PB_ERR_BUDGET: no slot can hold it. */
+ * its k-space resolution.  PB_ERR_BUDGET: even a slot of its own would not
+ * fit the budget (larger than the largest grid, or too many points). */
 int pb_server_submit(pb_server s, const pb_solve_params* p, const double* x, const double* f, const double* y,
                      double* U, long long* ticket);
 /* state: 0 queued, 1 on the GPU, 2 done (then status and latency are set). */

@@ -113,6 +113,8 @@ class ServerConfig(C.Structure):
         ("max_tgt", C.c_int),
         ("queue_capacity", C.c_int),
         ("linger_us", C.c_int),
+        ("max_dynamic_per_grid", C.c_int),
+        ("dynamic_idle_ms", C.c_int),
     ]
 
 
@@ -128,6 +130,10 @@ class ServerCounters(C.Structure):
         ("slots", C.c_int),
         ("kernels", C.c_longlong),
         ("scheduler_busy_s", C.c_double),
+        ("peak_device_bytes", C.c_longlong),
+        ("slots_created", C.c_longlong),
+        ("slots_released", C.c_longlong),
+        ("memory_waits", C.c_longlong),
     ]
 
 

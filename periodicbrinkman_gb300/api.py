@@ -196,6 +196,21 @@ def make_slot(M: int, max_instances: int, max_src: int, max_tgt: int, max_cells:
     return plan
 
 
+def slot_estimate_bytes(M: int, max_instances: int, max_src: int, max_tgt: int, max_cells: int,
+                        precision: str | int = "mixed", npoly: int = 20) -> int:
+    """Device bytes of a capacity plan (pb_slot_estimate_bytes), host only."""
+    c = SlotConfig()
+    for a in range(3):
+        c.M[a] = int(M)
+    c.max_instances, c.max_src, c.max_tgt, c.max_cells = int(max_instances), int(max_src), int(max_tgt), int(max_cells)
+    c.precision = {"mixed": PB_PREC_MIXED, "fp64": PB_PREC_FP64}.get(precision, precision)
+    c.npoly = int(npoly)
+    v = int(lib().pb_slot_estimate_bytes(C.byref(c)))
+    if v < 0:
+        check(v)
+    return v
+
+
 def bind(plan: "Plan", params) -> None:
     """Bind instances to a plan (see pb_plan_bind); sets the packed sizes."""
     params = list(params)
@@ -212,7 +227,8 @@ class Server:
 
     def __init__(self, precision: str | int = "mixed", budget_bytes: int = 150 << 30, max_batch: int = 16,
                  slots_per_grid: int = 2, grids=(8, 16, 32, 64, 128, 256), max_src: int = 1 << 18,
-                 max_tgt: int = 0, queue_capacity: int = 0, linger_us: int = 0):
+                 max_tgt: int = 0, queue_capacity: int = 0, linger_us: int = 0, max_dynamic_per_grid: int = 0,
+                 dynamic_idle_ms: int = 0):
         c = ServerConfig()
         c.budget_bytes = int(budget_bytes)
         c.precision = {"mixed": PB_PREC_MIXED, "fp64": PB_PREC_FP64}.get(precision, precision)
@@ -225,6 +241,8 @@ class Server:
         c.max_tgt = int(max_tgt)
         c.queue_capacity = int(queue_capacity)
         c.linger_us = int(linger_us)
+        c.max_dynamic_per_grid = int(max_dynamic_per_grid)
+        c.dynamic_idle_ms = int(dynamic_idle_ms)
         self.precision = c.precision
         h = C.c_void_p()
         check(lib().pb_server_create(C.byref(c), C.byref(h)))

@@ -2,14 +2,21 @@
 //
 // Requests of different sizes are autotuned on submission, assigned to the
 // smallest provisioned FFT grid that holds their k-space resolution, and
-// queued per grid.  A scheduler thread keeps a fixed set of resident slots
-// (capacity plans with their own stream, buffers, pinned staging and CUDA
-// graph): whenever a slot is idle it binds the next requests of its grid
-// queue that fit its capacity, stages their inputs, and launches the slot's
-// graph; slots run concurrently, so requests arriving while others are on the
-// GPU are admitted as soon as a slot frees up.  Device memory is fixed at
-// creation and bounded by the configured budget (admission by memory
-// budget); a request no slot can hold is rejected at submission.
+// queued per grid.  A scheduler thread keeps a set of slots (capacity plans
+// with their own stream, buffers, pinned staging and CUDA graph): whenever a
+// slot is idle it binds the next requests of its grid queue that fit its
+// capacity, stages their inputs, and launches the slot's graph; slots run
+// concurrently, so requests arriving while others are on the GPU are
+// admitted as soon as a slot frees up.
+//
+// Admission by device-memory budget: the resident slots are created with the
+// server; the part of the budget they leave is given out as dynamic slots,
+// sized for a request that no slot of its grid can hold, or of the resident
+// size when a grid's queue backs up while all its slots are busy.  When the
+// budget is taken the request waits in its queue; idle dynamic slots are
+// released (least recently used first) to make room, and dynamic slots idle
+// for dynamic_idle_ms are released anyway.  Only a request that a slot of
+// its own could not fit within the whole budget is rejected at submission.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -17,6 +24,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -38,6 +46,8 @@ struct Req {
     pb::PbTables tab;  // real-space tables, built at submission
     int grid;
     int n_tgt_eff;
+    long long cells = 0;       // real-space cells of the instance on its slot's grid
+    bool waited = false;       // counted once in memory_waits
     const double *x, *f, *y;
     double* U;
     bool pin_in = false, pin_out = false;  // page-locked client buffers: copied by DMA, no staging
@@ -48,6 +58,9 @@ struct Req {
 
 struct Slot {
     int grid = 0;
+    bool dynamic = false;       // made from the unused budget; released when idle
+    long long bytes = 0;        // device bytes of its plan
+    Clock::time_point last_used;
     pb_plan plan = nullptr;
     pb_slot_config cfg{};
     cudaStream_t stream = nullptr;
@@ -67,9 +80,10 @@ std::string g_srv_err;
 
 struct pb_server_s {
     pb_server_config cfg{};
-    std::vector<Slot> slots;
+    std::vector<std::unique_ptr<Slot>> slots;
     std::vector<int> grids;
-    long long device_bytes = 0;
+    std::atomic<long long> device_bytes{0}, peak_bytes{0}, slots_created{0}, slots_released{0}, memory_waits{0};
+    std::atomic<int> nslots{0};
     std::mutex mu;
     std::condition_variable cv;
     std::deque<Req*> inbox;
@@ -125,6 +139,7 @@ void finish_slot(pb_server_s* S, Slot& sl, int status)
     }
     sl.reqs.clear();
     sl.busy = false;
+    sl.last_used = Clock::now();
 }
 
 bool dispatch(pb_server_s* S, Slot& sl, std::deque<Req*>& q)
@@ -215,12 +230,144 @@ bool dispatch(pb_server_s* S, Slot& sl, std::deque<Req*>& q)
     return true;
 }
 
+// Capacity of a slot of grid g holding requests of up to (src, tgt, cells),
+// with the batch size of the resident slots (large grids hold fewer instances:
+// a slot's grids stay near an eighth of the per-slot budget share).
+pb_slot_config slot_config(const pb_server_s* S, int g, long long src, long long tgt, long long cells, int B)
+{
+    const pb_server_config& cfg = S->cfg;
+    pb_slot_config c{};
+    c.M[0] = c.M[1] = c.M[2] = g;
+    if (B <= 0) {
+        long long gbytes = 3LL * g * g * g * (cfg.precision == PB_PREC_FP64 ? 8 : 4) * 2;
+        long long share = cfg.budget_bytes / (long long)(S->grids.size() * std::max(1, cfg.slots_per_grid));
+        B = (int)std::max(1LL, std::min<long long>(cfg.max_batch, share / (2 * gbytes)));
+    }
+    c.max_instances = B;
+    c.max_src = (int)std::max<long long>(cfg.max_src, src);
+    c.max_tgt = (int)std::max<long long>(cfg.max_tgt, tgt);
+    // cells: the autotuner keeps rc >= ~4.6 grid spacings, so an instance has at most (M/2)^3 cells
+    c.max_cells = (int)std::min<long long>(1 << 21, (long long)B * (g / 2) * (g / 2) * (g / 2));
+    c.max_cells = (int)std::max<long long>(c.max_cells, cells);
+    c.precision = cfg.precision;
+    c.npoly = S->npoly;
+    return c;
+}
+
+bool holds(const Slot& sl, const Req* r)
+{
+    return r->p.n_src <= sl.cfg.max_src && r->n_tgt_eff <= sl.cfg.max_tgt && r->cells <= sl.cfg.max_cells;
+}
+
+void free_slot(Slot& sl)
+{
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    if (sl.plan) pb_plan_destroy(sl.plan);
+    if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+    for (double* p : {sl.x, sl.f, sl.y, sl.U})
+        if (p) cudaFreeHost(p);
+    sl.plan = nullptr;
+    sl.done = nullptr;
+    sl.stream = nullptr;
+    sl.x = sl.f = sl.y = sl.U = nullptr;
+}
+
+// Creates a slot with capacity c (device memory accounted by its estimate).
+int make_slot(pb_server_s* S, const pb_slot_config& c, bool dynamic, long long est, std::unique_ptr<Slot>& out)
+{
+    auto sl = std::make_unique<Slot>();
+    sl->grid = c.M[0];
+    sl->cfg = c;
+    sl->dynamic = dynamic;
+    sl->bytes = est;
+    sl->last_used = Clock::now();
+    int rc = pb_plan_create_slot(&c, &sl->plan);
+    if (rc != PB_OK) {
+        g_srv_err = pb_last_error();
+        free_slot(*sl);
+        return rc;
+    }
+    size_t xs = 3 * (size_t)c.max_src * sizeof(double), ts = 3 * (size_t)c.max_tgt * sizeof(double);
+    if (cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMallocHost(&sl->x, xs) != cudaSuccess || cudaMallocHost(&sl->f, xs) != cudaSuccess ||
+        cudaMallocHost(&sl->y, ts) != cudaSuccess || cudaMallocHost(&sl->U, ts) != cudaSuccess) {
+        cudaGetLastError();
+        free_slot(*sl);
+        return PB_ERR_NOMEM;
+    }
+    long long now = (S->device_bytes += est);
+    long long pk = S->peak_bytes.load();
+    while (now > pk && !S->peak_bytes.compare_exchange_weak(pk, now)) {
+    }
+    out = std::move(sl);
+    return PB_OK;
+}
+
+void release_slot(pb_server_s* S, size_t i)
+{
+    S->device_bytes -= S->slots[i]->bytes;
+    free_slot(*S->slots[i]);
+    S->slots.erase(S->slots.begin() + (long)i);
+    S->slots_released++;
+    S->nslots = (int)S->slots.size();
+}
+
+// Releases idle dynamic slots, least recently used first, until `need` bytes
+// fit the budget; true when they do.
+bool make_room(pb_server_s* S, long long need)
+{
+    while (S->device_bytes.load() + need > S->cfg.budget_bytes) {
+        long best = -1;
+        for (size_t i = 0; i < S->slots.size(); i++) {
+            const Slot& sl = *S->slots[i];
+            if (sl.dynamic && !sl.busy && (best < 0 || sl.last_used < S->slots[(size_t)best]->last_used)) best = (long)i;
+        }
+        if (best < 0) return false;
+        release_slot(S, (size_t)best);
+    }
+    return true;
+}
+
+// The head request of grid gi's queue has no slot to go to: a dynamic slot
+// sized for it (or of the resident size, to add concurrency), from the
+// unused budget; returns the new slot or null (then the request waits).
+Slot* grow(pb_server_s* S, int gi, const Req* head, bool for_capacity)
+{
+    const int g = S->grids[(size_t)gi];
+    int ndyn = 0;
+    for (auto& sl : S->slots)
+        if (sl->grid == g && sl->dynamic) ndyn++;
+    const int max_dyn = S->cfg.max_dynamic_per_grid < 0 ? 0
+                        : S->cfg.max_dynamic_per_grid > 0 ? S->cfg.max_dynamic_per_grid
+                                                          : std::max(1, S->cfg.slots_per_grid);
+    if (!for_capacity && ndyn >= max_dyn) return nullptr;
+    // the resident batch size when the budget allows it, else fewer instances
+    for (int B = slot_config(S, g, 0, 0, 0, 0).max_instances;; B /= 2) {
+        pb_slot_config c = slot_config(S, g, head->p.n_src, head->n_tgt_eff, head->cells, B);
+        const long long est = pb_slot_estimate_bytes(&c);
+        if (est > 0 && est <= S->cfg.budget_bytes && make_room(S, est)) {
+            std::unique_ptr<Slot> sl;
+            if (make_slot(S, c, true, est, sl) != PB_OK) return nullptr;
+            S->slots_created++;
+            S->slots.push_back(std::move(sl));
+            S->nslots = (int)S->slots.size();
+            return S->slots.back().get();
+        }
+        if (B <= 1 || !for_capacity) break;
+    }
+    return nullptr;
+}
+
 void worker_loop(pb_server_s* S)
 {
     cudaSetDevice(S->device);
+    const auto idle_release = std::chrono::milliseconds(S->cfg.dynamic_idle_ms > 0 ? S->cfg.dynamic_idle_ms : 1000);
     while (!S->stop.load()) {
         bool did = false;
-        for (Slot& sl : S->slots) {
+        for (auto& slp : S->slots) {
+            Slot& sl = *slp;
             if (!sl.busy) continue;
             cudaError_t e = cudaEventQuery(sl.done);
             if (e == cudaSuccess) {
@@ -241,10 +388,42 @@ void worker_loop(pb_server_s* S)
             }
         }
         auto t0 = Clock::now();
-        for (Slot& sl : S->slots) {
-            if (sl.busy) continue;
-            int gi = grid_index(S, sl.grid);
-            if (gi >= 0 && dispatch(S, sl, S->queues[gi])) did = true;
+        for (size_t gi = 0; gi < S->grids.size(); gi++) {
+            std::deque<Req*>& q = S->queues[gi];
+            const int g = S->grids[gi];
+            for (size_t k = 0; k < S->slots.size() && !q.empty(); k++) {
+                Slot& sl = *S->slots[k];
+                if (sl.grid == g && !sl.busy && dispatch(S, sl, q)) did = true;
+            }
+            if (q.empty()) continue;
+            // the head request still waits: no slot of its grid can hold it, or
+            // they are all busy while the queue backs up
+            Req* head = q.front();
+            bool fits = false, all_busy = true;
+            for (auto& sl : S->slots)
+                if (sl->grid == g) {
+                    fits = fits || holds(*sl, head);
+                    all_busy = all_busy && sl->busy;
+                }
+            const bool backlog = all_busy && (int)q.size() >= std::max(2, S->cfg.max_batch);
+            if (!fits || backlog) {
+                Slot* ns = grow(S, (int)gi, head, !fits);
+                if (ns) {
+                    if (dispatch(S, *ns, q)) did = true;
+                } else if (!fits && !head->waited) {
+                    head->waited = true;
+                    S->memory_waits++;
+                }
+            }
+        }
+        // dynamic slots idle for a while give their memory back
+        const auto now = Clock::now();
+        for (size_t i = 0; i < S->slots.size();) {
+            const Slot& sl = *S->slots[i];
+            if (sl.dynamic && !sl.busy && now - sl.last_used > idle_release)
+                release_slot(S, i);
+            else
+                i++;
         }
         if (did) S->busy_ns += std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count();
         if (!did) {
@@ -256,15 +435,10 @@ void worker_loop(pb_server_s* S)
 
 void destroy_slots(pb_server_s* S)
 {
-    for (Slot& sl : S->slots) {
-        if (sl.stream) cudaStreamSynchronize(sl.stream);
-        if (sl.plan) pb_plan_destroy(sl.plan);
-        if (sl.done) cudaEventDestroy(sl.done);
-        if (sl.stream) cudaStreamDestroy(sl.stream);
-        for (double* p : {sl.x, sl.f, sl.y, sl.U})
-            if (p) cudaFreeHost(p);
-    }
+    for (auto& sl : S->slots) free_slot(*sl);
     S->slots.clear();
+    S->device_bytes = 0;
+    S->nslots = 0;
 }
 
 }  // namespace
@@ -294,53 +468,26 @@ int pb_server_create(const pb_server_config* cfg_in, pb_server* out)
     for (int i = 0; i < cfg.n_grids; i++) S->grids.push_back(cfg.grids[i]);
     std::sort(S->grids.begin(), S->grids.end());
     S->queues.resize(S->grids.size());
-    long long used = 0;
     for (int g : S->grids) {
         for (int k = 0; k < cfg.slots_per_grid; k++) {
-            Slot sl;
-            sl.grid = g;
-            sl.cfg.M[0] = sl.cfg.M[1] = sl.cfg.M[2] = g;
-            // large grids hold fewer instances: keep the grids of one slot near 1/8 of the budget share
-            long long gbytes = 3LL * g * g * g * (cfg.precision == PB_PREC_FP64 ? 8 : 4) * 2;
-            long long share = cfg.budget_bytes / (long long)(S->grids.size() * cfg.slots_per_grid);
-            int B = (int)std::max(1LL, std::min<long long>(cfg.max_batch, share / (2 * gbytes)));
-            sl.cfg.max_instances = B;
-            sl.cfg.max_src = cfg.max_src;
-            sl.cfg.max_tgt = cfg.max_tgt;
-            // cells: the autotuner keeps rc >= ~4.6 grid spacings, so an instance has
-            // at most (M/2)^3 cells
-            sl.cfg.max_cells = (int)std::min<long long>(1 << 21, (long long)B * (g / 2) * (g / 2) * (g / 2));
-            sl.cfg.precision = cfg.precision;
-            sl.cfg.npoly = S->npoly;
-            long long est = pb_slot_estimate_bytes(&sl.cfg);
-            if (est < 0 || used + est > cfg.budget_bytes) continue;
-            int rc = pb_plan_create_slot(&sl.cfg, &sl.plan);
+            pb_slot_config c = slot_config(S, g, 0, 0, 0, 0);
+            long long est = pb_slot_estimate_bytes(&c);
+            if (est < 0 || S->device_bytes.load() + est > cfg.budget_bytes) continue;
+            std::unique_ptr<Slot> sl;
+            int rc = make_slot(S, c, false, est, sl);
             if (rc != PB_OK) {
-                g_srv_err = pb_last_error();
-                S->slots.push_back(sl);
                 destroy_slots(S);
                 delete S;
                 return rc;
             }
-            used += est;
-            cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
-            cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
-            size_t xs = 3 * (size_t)cfg.max_src * sizeof(double), ts = 3 * (size_t)cfg.max_tgt * sizeof(double);
-            if (cudaMallocHost(&sl.x, xs) != cudaSuccess || cudaMallocHost(&sl.f, xs) != cudaSuccess ||
-                cudaMallocHost(&sl.y, ts) != cudaSuccess || cudaMallocHost(&sl.U, ts) != cudaSuccess) {
-                S->slots.push_back(sl);
-                destroy_slots(S);
-                delete S;
-                return PB_ERR_NOMEM;
-            }
-            S->slots.push_back(sl);
+            S->slots.push_back(std::move(sl));
         }
     }
+    S->nslots = (int)S->slots.size();
     if (S->slots.empty()) {
         delete S;
         return PB_ERR_BUDGET;
     }
-    S->device_bytes = used;
     S->worker = std::thread(worker_loop, S);
     *out = S;
     return PB_OK;
@@ -377,11 +524,14 @@ int pb_server_submit(pb_server S, const pb_solve_params* p, const double* x, con
     }
     int n_tgt_eff = p->n_tgt > 0 ? p->n_tgt : p->n_src;
     const long long cells = (long long)info.ncell[0] * info.ncell[1] * info.ncell[2];
-    bool fits = false;
-    for (const Slot& sl : S->slots)
-        if (gi >= 0 && sl.grid == S->grids[gi] && p->n_src <= sl.cfg.max_src && n_tgt_eff <= sl.cfg.max_tgt &&
-            cells <= sl.cfg.max_cells)
-            fits = true;
+    // admitted when a slot of its own (one instance) would fit the whole budget;
+    // whether memory is free now is the scheduler's concern
+    bool fits = gi >= 0;
+    if (fits) {
+        pb_slot_config c = slot_config(S, S->grids[gi], p->n_src, n_tgt_eff, cells, 1);
+        const long long est = pb_slot_estimate_bytes(&c);
+        fits = est > 0 && est <= S->cfg.budget_bytes;
+    }
     if (!fits) {
         delete r;
         S->rejected++;
@@ -397,6 +547,7 @@ int pb_server_submit(pb_server S, const pb_solve_params* p, const double* x, con
     for (int a = 0; a < 3; a++) r->p.M[a] = info.M[a];
     r->grid = gi;
     r->n_tgt_eff = n_tgt_eff;
+    r->cells = cells;
     r->x = x;
     r->f = f;
     r->y = y;
@@ -484,8 +635,12 @@ int pb_server_stats(pb_server S, pb_server_counters* out)
     out->rejected = S->rejected.load();
     out->batches = S->batches.load();
     out->mean_batch = out->batches ? (double)S->batched_instances.load() / out->batches : 0.0;
-    out->device_bytes = S->device_bytes;
-    out->slots = (int)S->slots.size();
+    out->device_bytes = S->device_bytes.load();
+    out->slots = S->nslots.load();
+    out->peak_device_bytes = S->peak_bytes.load();
+    out->slots_created = S->slots_created.load();
+    out->slots_released = S->slots_released.load();
+    out->memory_waits = S->memory_waits.load();
     out->kernels = S->kernels.load();
     out->scheduler_busy_s = 1e-9 * (double)S->busy_ns.load();
     return PB_OK;

@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 import periodicbrinkman_gb300 as pb  # noqa: E402
 from periodicbrinkman_gb300 import _lib  # noqa: E402
-from periodicbrinkman_gb300.api import Server, bind, make_params, make_slot  # noqa: E402
+from periodicbrinkman_gb300.api import Server, bind, make_params, make_slot, resolve, slot_estimate_bytes  # noqa: E402
 
 MIX_TOL = 1e-6  # alone vs in the mix, relative to max |u|
 
@@ -87,13 +87,14 @@ def test_server_mix_equals_alone_and_oracle():
 
 
 def test_server_rejects_and_validates():
-    with Server(precision="mixed", budget_bytes=2 << 30, max_batch=4, slots_per_grid=1, grids=(16, 32),
+    with Server(precision="mixed", budget_bytes=64 << 20, max_batch=4, slots_per_grid=1, grids=(16, 32),
                 max_src=2000) as srv:
         rng = np.random.default_rng(33)
-        x = rng.random((5000, 3))
+        x = rng.random((400_000, 3))
         with pytest.raises(pb.PbError) as ei:
-            srv.submit(x, x.copy(), 1.0, 10.0, 0.01, tol=1e-6)  # larger than any slot
+            srv.submit(x, x.copy(), 1.0, 10.0, 0.01, tol=1e-6, M=32)  # a slot of its own exceeds the budget
         assert ei.value.code == _lib.PB_ERR_BUDGET
+        assert srv.stats()["peak_device_bytes"] <= 64 << 20
         with pytest.raises(pb.PbError):
             srv.submit(x[:10], x[:10].copy(), 1.0, -1.0, 0.01)
         t = srv.submit(x[:100], x[:100].copy(), 1.0, 10.0, 0.01, tol=1e-6)
@@ -120,3 +121,34 @@ def test_server_non_finite_request_fails_alone():
             srv.result(tickets[1])
         assert ei.value.code == _lib.PB_ERR_INVALID
         assert srv.stats()["failed"] >= 1
+
+
+def test_server_admits_by_memory_budget():
+    """Two requests larger than the resident slots, on different grids, with a
+    budget that holds the resident slots and ONE slot for such a request: the
+    first gets a dynamic slot at once, the second waits until that slot's
+    memory is released, and both complete; the slots never hold more device
+    memory than the budget."""
+    # one instance per slot execution: the resident slots' size does not depend on the budget
+    n, grids, res = 30000, (32, 64), dict(max_batch=1, slots_per_grid=1, max_src=2000)
+    with Server(precision="mixed", budget_bytes=64 << 30, grids=grids, max_dynamic_per_grid=-1, **res) as probe:
+        resident = probe.stats()["device_bytes"]
+    need = 0
+    for g in grids:
+        info = resolve(make_params(n, 1.0, 10.0, 0.01, n_tgt=n // 2, tol=1e-6, M=g))
+        cells = int(np.prod(info["ncell"]))
+        need = max(need, slot_estimate_bytes(g, 1, n, n // 2, max(cells, (g // 2) ** 3)))
+    budget = resident + need + need // 2
+    rng = np.random.default_rng(35)
+    reqs = [(rng.random((n, 3)), rng.standard_normal((n, 3)), rng.random((n // 2, 3)), g) for g in grids]
+    with Server(precision="mixed", budget_bytes=budget, grids=grids, dynamic_idle_ms=60000, **res) as srv:
+        assert srv.stats()["device_bytes"] == resident
+        tickets = [srv.submit(x, f, 1.0, 10.0, 0.01, y=y, tol=1e-6, M=g) for x, f, y, g in reqs]
+        outs = [srv.result(t, timeout=600)[0] for t in tickets]
+        st = srv.stats()
+    assert st["completed"] == 2 and st["failed"] == 0 and st["rejected"] == 0
+    assert st["slots_created"] >= 2 and st["slots_released"] >= 1 and st["memory_waits"] >= 1, st
+    assert st["peak_device_bytes"] <= budget, (st["peak_device_bytes"], budget)
+    for (x, f, y, g), U in zip(reqs, outs):
+        alone = pb.solve(_cuda(x), _cuda(f), 1.0, 10.0, 0.01, y=_cuda(y), tol=1e-6, M=g).cpu().numpy()
+        assert np.abs(U - alone).max() <= MIX_TOL * np.abs(alone).max(), g
