@@ -251,7 +251,6 @@ __device__ __forceinline__ void window_f32(const PbInst& I, float4 h4, float4 l4
 // need no bounds tests.  Points of another instance, or a box wider than
 // kBoxMax along an axis, are spread one point at a time through the same loops.
 constexpr int kSpreadGroup = 4;  // measured at N = 1e5: 2 -> 0.31 ms, 3 -> 0.26, 4 -> 0.24, 5 -> 0.244, 6 -> 0.276
-constexpr int kGatherGroup = 1;  // measured: 1 -> 0.22 ms, 2 -> 0.26, 3 -> 0.29, 4 -> 0.32 at N = 1e5
 constexpr int kBoxMax = 48;
 
 // 4 blocks per SM (64 registers, a few spilled): measured 0.286 ms vs 0.300 at
@@ -396,33 +395,78 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, 4)
     }
 }
 
-// One target's window sum (the whole warp), written to out[0..2] by lane 0.
-__device__ __forceinline__ void gather_point(const PbInst& I, float4 h4, float4 l4, int lane, float (*wgt)[kMaxP],
-                                             int (*gidx)[kMaxP], const float* __restrict__ grid, float* out)
+// Gathering, one target per warp: the target's window is walked with lanes
+// over its (y, z) points and a loop over x.  Each axis' weights and wrapped
+// grid offsets (32-bit element offsets: x M_y M_z, y M_z, z) are laid out in
+// the warp's shared rows once, so the inner loop is one broadcast shared
+// load, one integer add, one 16-byte grid load and three FMAs per point; x
+// rows are summed in plain FP32 (<= 32 same-sign-weighted terms) and rows
+// Kahan-summed.  The weights come from the FP32 window of the point-wise
+// spreading kernel (window_f32).  Grids of up to 1024^3 points keep the
+// offsets below 2^31.
+__global__ void __launch_bounds__(kSpreadWarps * 32)
+    k_gather_f4t(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
+                 const float4* __restrict__ pb, const float* __restrict__ grid, float* __restrict__ u_k)
 {
-    window_f32(I, h4, l4, lane, wgt, gidx);
+    __shared__ float2 xw[kSpreadWarps][kMaxP];  // x: (weight, offset bits)
+    __shared__ float2 yw[kSpreadWarps][kMaxP];  // y: (weight, offset bits)
+    __shared__ float2 zw[kSpreadWarps][kMaxP];  // z: (weight, offset bits)
+    const int ntot = *ntot_p;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int s = blockIdx.x * kSpreadWarps + w;
+    if (s >= ntot) return;
+    const float4 h4 = pa[s], l4 = pb[s];
+    const PbInst& I = inst[__float_as_int(h4.w)];
+    int g0 = 0;
+    float base = 0.f;
+    if (lane < 3) {  // the cell and the offset from the window start, as window_f32
+        const float xh = lane == 0 ? h4.x : lane == 1 ? h4.y : h4.z;
+        const float xl = lane == 0 ? l4.x : lane == 1 ? l4.y : l4.z;
+        const float gi = I.gihf[lane];
+        const int c = min(max((int)floorf(fmaf(xh, gi, xl * gi)), 0), I.M[lane] - 1);
+        g0 = c - I.Pa[lane] / 2 + 1;
+        const float gf = (float)g0, hh = I.ghh[lane];
+        const float p = gf * hh, e = fmaf(gf, hh, -p);  // g0 hh = p + e exactly
+        base = ((xh - p) - e) + (xl - gf * I.ghl[lane]);
+    }
+    const float inv_eta = I.inv_eta_f;
+    const int stride[3] = {I.M[1] * I.M[2], I.M[2], 1};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int ga = __shfl_sync(kFull, g0, a);
+        const float ba = __shfl_sync(kFull, base, a);
+        if (lane < I.Pa[a]) {
+            const float dx = fmaf(-(float)lane, I.ghh[a], ba);
+            const float2 v = make_float2(expf(-dx * dx * inv_eta),
+                                         __int_as_float(((ga + lane) & (I.M[a] - 1)) * stride[a]));
+            if (a == 0)
+                xw[w][lane] = v;
+            else if (a == 1)
+                yw[w][lane] = v;
+            else
+                zw[w][lane] = v;
+        }
+    }
     __syncwarp();
-    const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz, R = window_lanes(Py, Pz);
-    const size_t M12 = (size_t)I.M[1] * I.M[2];
+    const int Px = I.Pa[0], Py = I.Pa[1], Pz = I.Pa[2], P2 = Py * Pz;
+    const unsigned inv_pz = ((1u << 20) + Pz - 1) / Pz;  // exact quotients for yz < 2^15
     const float4* g4 = reinterpret_cast<const float4*>(grid + I.grid_off);
     float s0 = 0, s1 = 0, s2 = 0, c0 = 0, c1 = 0, c2 = 0;
-    // quotients by multiply and shift (exact for id < 2^15): no integer division in the loop
-    const unsigned inv_p2 = ((1u << 20) + P2 - 1) / P2, inv_pz = ((1u << 20) + Pz - 1) / Pz;
-    for (int id = lane; id < P2 * R; id += 32) {
-        const int xs = (int)(((unsigned)id * inv_p2) >> 20), yz = id - xs * P2;
+    for (int yz = lane; yz < P2; yz += 32) {
         const int py = (int)(((unsigned)yz * inv_pz) >> 20), pz = yz - py * Pz;
-        const size_t oyz = (size_t)gidx[1][py] * I.M[2] + gidx[2][pz];
-        // one x row of the window in plain FP32 (<= 32 same-sign-weighted terms), rows Kahan-summed
+        const float2 ey = yw[w][py], ez = zw[w][pz];
+        const int oyz = __float_as_int(ey.y) + __float_as_int(ez.y);
+        const float4* row = g4 + oyz;
         float r0 = 0, r1 = 0, r2 = 0;
 #pragma unroll 4
-        for (int px = xs; px < Px; px += R) {
-            const float wx = wgt[0][px];
-            const float4 v = __ldg(g4 + (size_t)gidx[0][px] * M12 + oyz);
-            r0 = fmaf(wx, v.x, r0);
-            r1 = fmaf(wx, v.y, r1);
-            r2 = fmaf(wx, v.z, r2);
+        for (int px = 0; px < Px; px++) {
+            const float2 ex = xw[w][px];
+            const float4 v = __ldg(row + __float_as_int(ex.y));
+            r0 = fmaf(ex.x, v.x, r0);
+            r1 = fmaf(ex.x, v.y, r1);
+            r2 = fmaf(ex.x, v.z, r2);
         }
-        const float wyz = wgt[1][py] * wgt[2][pz];
+        const float wyz = ey.x * ez.x;
         kahan_add(s0, c0, wyz * r0);
         kahan_add(s1, c1, wyz * r1);
         kahan_add(s2, c2, wyz * r2);
@@ -437,127 +481,10 @@ __device__ __forceinline__ void gather_point(const PbInst& I, float4 h4, float4 
         s2 += __shfl_xor_sync(kFull, s2, o);
     }
     if (lane == 0) {
-        out[0] = s0;
-        out[1] = s1;
-        out[2] = s2;
+        u_k[3 * (size_t)s] = s0;
+        u_k[3 * (size_t)s + 1] = s1;
+        u_k[3 * (size_t)s + 2] = s2;
     }
-}
-
-// Gathering over boxes: a warp takes kGatherGroup consecutive (nearby)
-// targets and reads each point of their common box once, accumulating every
-// target's weighted sum from it.  With one target per warp (the measured
-// best: more targets per warp cost registers and occupancy) the box is the
-// window, walked with per-axis weights laid out along it (no index tables,
-// no divisions in the loops).  Targets of another instance, or a box wider
-// than kBoxMax, are gathered one at a time.
-__global__ void __launch_bounds__(kSpreadWarps * 32)
-    k_gather_f4g(const PbInst* __restrict__ inst, const int* __restrict__ ntot_p, const float4* __restrict__ pa,
-                 const float4* __restrict__ pb, const float* __restrict__ grid, float* __restrict__ u_k)
-{
-    constexpr int G = kGatherGroup;
-    __shared__ float wgt[kSpreadWarps][3][kMaxP];
-    __shared__ int gidx[kSpreadWarps][3][kMaxP];
-    __shared__ float raw[kSpreadWarps][G][3][kMaxP];
-    __shared__ float pw[kSpreadWarps][G][3][kBoxMax];
-    __shared__ int gs[kSpreadWarps][G][3];
-    const int ntot = *ntot_p;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int sb = (blockIdx.x * kSpreadWarps + w) * G;
-    if (sb >= ntot) return;
-    const int cnt = min(G, ntot - sb);
-    const int q0 = __float_as_int(pa[sb].w);
-    const PbInst& I = inst[q0];
-    bool same = true;
-    for (int p = 0; p < cnt; p++) same = same && __float_as_int(pa[sb + p].w) == q0;
-    int b0[3] = {0, 0, 0}, B[3] = {0, 0, 0};
-    bool fits = same;
-    if (same) {
-        for (int p = 0; p < cnt; p++) {
-            window_f32(I, pa[sb + p], pb[sb + p], lane, wgt[w], gidx[w], gs[w][p]);
-            __syncwarp();
-            for (int i = lane; i < 3 * kMaxP; i += 32) raw[w][p][i / kMaxP][i % kMaxP] = wgt[w][i / kMaxP][i % kMaxP];
-            __syncwarp();
-        }
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            int lo = 1 << 30, hi = -(1 << 30);
-            for (int p = 0; p < cnt; p++) {
-                lo = min(lo, gs[w][p][a]);
-                hi = max(hi, gs[w][p][a] + I.Pa[a]);
-            }
-            b0[a] = lo;
-            B[a] = hi - lo;
-            fits = fits && B[a] <= kBoxMax;
-        }
-    }
-    if (!fits) {
-        for (int p = 0; p < cnt; p++) {
-            const float4 h4 = pa[sb + p];
-            __syncwarp();
-            gather_point(inst[__float_as_int(h4.w)], h4, pb[sb + p], lane, wgt[w], gidx[w], grid,
-                         u_k + 3 * (size_t)(sb + p));
-        }
-        return;
-    }
-    for (int i = lane; i < G * 3 * kBoxMax; i += 32) {
-        const int p = i / (3 * kBoxMax), r = i - p * 3 * kBoxMax, a = r / kBoxMax, x = r - a * kBoxMax;
-        float v = 0.f;
-        if (p < cnt) {
-            const int k = b0[a] + x - gs[w][p][a];
-            if (x < B[a] && k >= 0 && k < I.Pa[a]) v = raw[w][p][a][k];
-        }
-        pw[w][p][a][x] = v;
-    }
-    __syncwarp();
-    const size_t M12 = (size_t)I.M[1] * I.M[2];
-    const int mx = I.M[0] - 1, my = I.M[1] - 1, mz = I.M[2] - 1;
-    const float4* g4 = reinterpret_cast<const float4*>(grid + I.grid_off);
-    float s[G][3], c[G][3];
-#pragma unroll
-    for (int p = 0; p < G; p++)
-#pragma unroll
-        for (int k = 0; k < 3; k++) s[p][k] = c[p][k] = 0.f;
-    const int Byz = B[1] * B[2];
-    for (int yz = lane; yz < Byz; yz += 32) {
-        const int y = yz / B[2], z = yz - y * B[2];
-        float wyz[G];
-        bool any = false;
-#pragma unroll
-        for (int p = 0; p < G; p++) {
-            wyz[p] = pw[w][p][1][y] * pw[w][p][2][z];
-            any = any || wyz[p] != 0.f;
-        }
-        if (!any) continue;
-        const size_t oyz = (size_t)((b0[1] + y) & my) * I.M[2] + ((b0[2] + z) & mz);
-        // rows in plain FP32 (<= kBoxMax same-sign-weighted terms), rows Kahan-summed
-        float r[G][3];
-#pragma unroll
-        for (int p = 0; p < G; p++) r[p][0] = r[p][1] = r[p][2] = 0.f;
-#pragma unroll 4
-        for (int x = 0; x < B[0]; x++) {
-            const float4 v = __ldg(g4 + (size_t)((b0[0] + x) & mx) * M12 + oyz);
-#pragma unroll
-            for (int p = 0; p < G; p++) {
-                const float wx = pw[w][p][0][x];
-                r[p][0] = fmaf(wx, v.x, r[p][0]);
-                r[p][1] = fmaf(wx, v.y, r[p][1]);
-                r[p][2] = fmaf(wx, v.z, r[p][2]);
-            }
-        }
-#pragma unroll
-        for (int p = 0; p < G; p++)
-#pragma unroll
-            for (int k = 0; k < 3; k++) kahan_add(s[p][k], c[p][k], wyz[p] * r[p][k]);
-    }
-#pragma unroll
-    for (int p = 0; p < G; p++)
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            float v = s[p][k] - c[p][k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-            if (lane == 0 && p < cnt) u_k[3 * (size_t)(sb + p) + k] = v;
-        }
 }
 
 template <class T>
@@ -585,9 +512,8 @@ void launch_gather(const PbInst* inst, int ninst, const int* tgt_offsets, int nc
     int blocks = (ncap + kSpreadWarps - 1) / kSpreadWarps;
     const int* ntot = tgt_offsets + ninst;
     if (sizeof(T) == 4)
-        k_gather_f4g<<<(ncap + kSpreadWarps * kGatherGroup - 1) / (kSpreadWarps * kGatherGroup), kSpreadWarps * 32, 0,
-                       s>>>(inst, ntot, (const float4*)pos_a, (const float4*)pos_b, (const float*)grid,
-                            (float*)u_k);
+        k_gather_f4t<<<(ncap + kSpreadWarps - 1) / kSpreadWarps, kSpreadWarps * 32, 0, s>>>(
+            inst, ntot, (const float4*)pos_a, (const float4*)pos_b, (const float*)grid, (float*)u_k);
     else
         k_gather<T, Dbl4><<<blocks, kSpreadWarps * 32, 0, s>>>(inst, ntot, (const Dbl4*)pos_a,
                                                                     (const Dbl4*)pos_b, grid, u_k);

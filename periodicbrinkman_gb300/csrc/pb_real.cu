@@ -751,10 +751,15 @@ void launch_real_mixed(int npoly, const PbInst* inst, const PbTables* tab, const
     k_real_mixed<NP><<<blocks, kRealWarps * 32, 0, s>>>(inst, tab, items, nitems_ptr, spos_hi, spos_lo, sfrc,        \
                                                          src_start, tpos_hi, tpos_lo, u_real, counter,               \
                                                          nitems_max)
+    // one instantiation per even term count: a shorter Horner chain per pair
     if (npoly <= 16)
         PB_LAUNCH_REAL(16);
+    else if (npoly <= 18)
+        PB_LAUNCH_REAL(18);
     else if (npoly <= 20)
         PB_LAUNCH_REAL(20);
+    else if (npoly <= 22)
+        PB_LAUNCH_REAL(22);
     else if (npoly <= 24)
         PB_LAUNCH_REAL(24);
     else if (npoly <= 26)

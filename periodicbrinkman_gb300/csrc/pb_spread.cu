@@ -225,17 +225,21 @@ __global__ void __launch_bounds__(kSpreadThreads, 3)
                     if (((occ[0] >> ((ww & 1) << 3)) & 0xffu) && ((occ[1] >> ((ww >> 1) << 2)) & 0xfu)) m |= 1u << ww;
                 S.mask[tid] = m;
             }
-            // 3b. all threads: the K x 40 tile-aligned weights, zero outside the window
-            for (int e = tid; e < K * kWts; e += kSpreadThreads) {
-                const int q = e / kWts, r = e - q * kWts;
-                const int a = r < kTile ? 0 : r < 2 * kTile ? 1 : 2;
-                const int k = r - a * kTile;
+            // 3b. all threads, one (point, axis) row each: the K x 40 tile-aligned weights
+            // along the row, zero outside the window
+            for (int e = tid; e < 3 * K; e += kSpreadThreads) {
+                const int q = e / 3, a = e - 3 * q;
                 // per-axis values by selection (a runtime index would put the arrays in local memory)
                 const int ta = a == 0 ? t0[0] : a == 1 ? t0[1] : t0[2];
                 const int Ta = a == 0 ? T[0] : a == 1 ? T[1] : T[2];
-                const int o = (ta + k - S.g0[q][a]) & (I.M[a] - 1);
-                const float dx = fmaf(-(float)o, I.ghh[a], S.base[q][a]);
-                S.w[q][r] = (k < Ta && o < I.Pa[a]) ? expf(-dx * dx * inv_eta) : 0.f;
+                const int nk = a == 2 ? kTileZ : kTile, Mm = I.M[a] - 1, P = I.Pa[a];
+                const float hh = I.ghh[a], b = S.base[q][a];
+                float* row = &S.w[q][a * kTile];
+                int o = (ta - S.g0[q][a]) & Mm;  // window offset of the tile's first point on this axis
+                for (int k = 0; k < nk; k++, o = (o + 1) & Mm) {
+                    const float dx = fmaf(-(float)o, hh, b);
+                    row[k] = (k < Ta && o < P) ? expf(-dx * dx * inv_eta) : 0.f;
+                }
             }
             __syncthreads();
             // 4. warp w adds the kept points whose window meets its patch, two at a time
