@@ -655,7 +655,7 @@ def main():
                          "at tol 1e-9 on the FP64 path; clustered: the N = 1e6 solve of 200 Gaussian clusters "
                          "(L = 2, grid 256^3); batch: 512 instances in one plan")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", nargs="?", const="single", choices=["single", "slot", "serve"],
+    ap.add_argument("--profile", nargs="?", const="single", choices=["single", "slot", "slot64", "serve"],
                     help="for ncu: run the single-solve plan twice (eager, then capture+replay), (slot) one "
                          "128^3 serving slot holding two requests of the stream three times, or (serve) the "
                          "first 300 requests of the serving stream through the server, and exit")
@@ -671,8 +671,8 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    if args.profile == "slot":
-        profile_slot(torch)
+    if args.profile in ("slot", "slot64"):
+        profile_slot(torch, 128 if args.profile == "slot" else 64)
         return
     if args.profile == "serve":
         profile_serve(torch)
@@ -809,21 +809,25 @@ def main():
         dist.destroy_process_group()
 
 
-def profile_slot(torch):
-    """One 128^3 serving slot (the server's capacity) with two requests of the stream, executed three times."""
+def profile_slot(torch, grid=128):
+    """One serving slot of the stream's capacity with requests of the stream, executed three times:
+    grid 128, two requests of N in (6e4, 1.2e5); grid 64, eight requests that the autotuner puts on 64^3."""
     from periodicbrinkman_gb300.api import bind, make_params, make_slot
 
     w = SERVE
     arrive, N, alpha, eps, tol = gen_stream(w)
-    ks = [k for k in range(400) if 60000 < N[k] < 120000][:2]
+    if grid == 128:
+        ks = [k for k in range(400) if 60000 < N[k] < 120000][:2]
+    else:
+        ks = [k for k in range(2000) if grid_class(w, int(N[k]), float(alpha[k]), float(eps[k]), float(tol[k])) == grid][:8]
     pool = InputPool(w["nmax"], sets=2)
-    slot = make_slot(128, max_instances=16, max_src=w["nmax"], max_tgt=w["nmax"] // 2 + 1,
-                     max_cells=min(1 << 21, 16 * 64 ** 3))
+    slot = make_slot(grid, max_instances=16, max_src=w["nmax"], max_tgt=w["nmax"] // 2 + 1,
+                     max_cells=min(1 << 21, 16 * (grid // 2) ** 3))
     ps, xs, fs, ys = [], [], [], []
     for k in ks:
         x, f, y = pool.get(int(k), int(N[k]))
         ps.append(make_params(x.shape[0], 1.0, float(alpha[k]), float(eps[k]), n_tgt=y.shape[0],
-                              tol=float(tol[k]), M=128))
+                              tol=float(tol[k]), M=grid))
         xs.append(x)
         fs.append(f)
         ys.append(y)
@@ -832,7 +836,7 @@ def profile_slot(torch):
     for _ in range(3):
         slot.execute(X, F, Y)
     torch.cuda.synchronize()
-    print(json.dumps({"profile": "slot_128_two_stream_requests", "n_src": [int(N[k]) for k in ks],
+    print(json.dumps({"profile": f"slot_{grid}_stream_requests", "n_src": [int(N[k]) for k in ks],
                       "kernels_per_execution": slot.kernel_count}))
     slot.close()
 
