@@ -62,8 +62,8 @@ METRIC = "Brinkman solves/s + p50/p99 latency at <=1e-6 rel err, served vs plain
 # kernels, taken from a separate ncu capture of the same code (not measured by this run); reported
 # with that label as `traffic`
 REAL_DRAM_BYTES = 7.57e6
-# the k-space kernels of that solve (spread 77.7 MB, five FFT passes 136.4 MB, gather 36.8 MB)
-KSPACE_DRAM_BYTES = 250.9e6
+# the k-space kernels of that solve (tiled spread 5.0 MB, five FFT passes 136.4 MB, gather 36.8 MB)
+KSPACE_DRAM_BYTES = 178.2e6
 TRAFFIC_SOURCE = "ncu dram read+write bytes per launch from a separate capture of this workload, not this run"
 
 
@@ -500,9 +500,9 @@ def roofline_single(torch, local, steps_warm=3):
     ach = by / tk / 1e9
     roof_k = {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": ach / pk["hbm_gbs"],
               "traffic": KSPACE_DRAM_BYTES, "traffic_source": TRAFFIC_SOURCE,
-              "kernel": "k_spread_f4g + FFT passes + k_gather_f4g",
-              "note": f"peak of {src}; the grid stays in L2, so the path is bound by L2 reductions (spread) and the "
-                      "L1 data pipe (gather), not by HBM"}
+              "kernel": "k_spread_tile + FFT passes + k_gather_f4t",
+              "note": f"peak of {src}; the grid stays in L2, so the path is bound by issue latency (tiled spread) "
+                      "and the L1 data pipe (gather), not by HBM"}
     roof["kspace"] = roof_k
     plan.close()
     return roof, dict(zip(names, stages.tolist())), info
