@@ -23,6 +23,7 @@
 
 #include "pb_device.cuh"
 #include "pb_kernels.h"
+#include "pb_tile.cuh"
 
 namespace pb {
 
@@ -43,52 +44,6 @@ struct SpreadSmem {
     int seg_pre[2 * kSegRound + 1];   // exclusive prefix of the segment lengths
     int wsum[kSpreadThreads / 32 + 1];
 };
-
-__device__ __forceinline__ int block_scan256(int v, int* wsum, int* total)
-{
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(kFull, x, o);
-        if (lane >= o) x += y;
-    }
-    __syncthreads();  // wsum is reused between calls
-    if (lane == 31) wsum[w] = x;
-    __syncthreads();
-    int base = 0, tot = 0;
-#pragma unroll
-    for (int k = 0; k < kSpreadThreads / 32; k++) {
-        const int s = wsum[k];
-        base += k < w ? s : 0;
-        tot += s;
-    }
-    *total = tot;
-    return base + x - v;
-}
-
-// Cells of one axis whose points can reach grid indices [t0, t0 + T) through a
-// window of P points: physical range [(t0 - P/2 - 1) h, (t0 + T + P/2) h) (one
-// grid cell of margin each side for the FP32 cell of a point), as a first
-// cell (any integer, taken mod nc) and a count (nc: all of them).
-__device__ __forceinline__ void cell_range(const PbInst& I, int a, int t0, int T, int& first, int& count)
-{
-    const double lo = (double)(t0 - I.Pa[a] / 2 - 1) * I.gh[a], hi = (double)(t0 + T + I.Pa[a] / 2) * I.gh[a];
-    const int cl = (int)floor(lo * I.ih[a] - 1e-9), ch = (int)floor(hi * I.ih[a] + 1e-9);
-    count = ch - cl + 1;
-    if (count >= I.nc[a]) {
-        first = 0;
-        count = I.nc[a];
-    } else {
-        first = cl;
-    }
-}
-
-__device__ __forceinline__ int pmod(int v, int n)
-{
-    const int r = v % n;
-    return r < 0 ? r + n : r;
-}
 
 __global__ void __launch_bounds__(kSpreadThreads, 3)
     k_spread_tile(const PbInst* __restrict__ inst, const int* __restrict__ bucket_inst, int ntx, int nty, int ntz,
