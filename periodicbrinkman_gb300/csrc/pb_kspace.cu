@@ -6,10 +6,12 @@
 // gather).  Also the final FP64 combine of real space, k space, self and the
 // optional k = 0 mode.
 //
-// FFT: hand-written shared-memory Stockham radix-2 passes along z (real-to-
-// complex by the packed half-length transform), y, and x; the x pass of the
-// forward transform is fused with the Green multiplication and the x pass of
-// the inverse, so the spectrum is read and written once for all three.
+// FFT: hand-written passes along z (real-to-complex by the packed half-length
+// transform), y, and x: register-resident four-step line transforms for FP32
+// grids with lines of 4 to 256 points, shared-memory Stockham radix-2 passes
+// for FP64 grids and longer lines.  The x pass of the forward transform is
+// fused with the Green multiplication and the x pass of the inverse, so the
+// spectrum is read and written once for all three.
 #include <algorithm>
 
 #include "pb_device.cuh"
