@@ -319,12 +319,14 @@ struct pb_plan_s {
     PbInst* d_inst = nullptr;
     PbTables* d_tab = nullptr;
     int *d_src_off = nullptr, *d_tgt_off = nullptr, *d_cell_off = nullptr, *d_y_off = nullptr;
-    double *x = nullptr, *f = nullptr, *y = nullptr, *ypack = nullptr, *U = nullptr;
-    int *cell_of_s = nullptr, *cnt_s = nullptr, *start_s = nullptr, *fill_s = nullptr, *perm_s = nullptr,
-        *perm_tmp_s = nullptr;
-    int *cell_of_t = nullptr, *cnt_t = nullptr, *start_t = nullptr, *fill_t = nullptr, *perm_t = nullptr,
-        *perm_tmp_t = nullptr;
-    int *scan_tmp = nullptr, *counter = nullptr;
+    double *x = nullptr, *f = nullptr, *y = nullptr, *U = nullptr;
+    // cell lists: per particle (cell, arrival slot); counts, scan flags and tickets (zeroed before
+    // every build); starts of the source cells and, cell_list_stride apart, of the target cells
+    int2 *key_s = nullptr, *key_t = nullptr;
+    int *cl_zero = nullptr, *start_s = nullptr, *start_t = nullptr;
+    size_t cl_zero_bytes = 0;
+    int *perm_s = nullptr, *perm_tmp_s = nullptr, *perm_t = nullptr, *perm_tmp_t = nullptr;
+    int* counter = nullptr;
     int4* items = nullptr;
     void *spos_a = nullptr, *spos_b = nullptr, *sfrc = nullptr, *tpos_a = nullptr, *tpos_b = nullptr;
     double *u_real = nullptr, *fsum = nullptr;
@@ -384,20 +386,16 @@ size_t plan_layout(pb_plan_s* P, bool assign)
     size_t o_so = L.take<int>(q + 1), o_to = L.take<int>(q + 1), o_co = L.take<int>(q + 1), o_yo = L.take<int>(q + 1);
     size_t o_x = L.take<double>(3 * (size_t)ns), o_f = L.take<double>(3 * (size_t)ns);
     size_t o_y = P->all_same ? 0 : L.take<double>(3 * (size_t)std::max(P->n_y, 1));
-    size_t o_yp = P->all_same ? 0 : L.take<double>(3 * (size_t)nt);
     size_t o_U = L.take<double>(3 * (size_t)nt);
-    size_t o_cs = L.take<int>(ns), o_cnts = L.take<int>(nc + 1), o_sts = L.take<int>(nc + 1),
-           o_fs = L.take<int>(nc + 1), o_ps = L.take<int>(ns), o_pts = L.take<int>(ns);
-    size_t o_ct = 0, o_cntt = 0, o_stt = 0, o_ft = 0, o_pt = 0, o_ptt = 0;
+    const size_t zero_bytes = cell_list_zero_bytes(nc);
+    size_t o_ks = L.take<int2>(ns), o_clz = L.take<char>(zero_bytes), o_sts = L.take<int>(2 * (size_t)cell_list_stride(nc)),
+           o_ps = L.take<int>(ns), o_pts = L.take<int>(ns);
+    size_t o_kt = 0, o_pt = 0, o_ptt = 0;
     if (!P->all_same) {
-        o_ct = L.take<int>(nt);
-        o_cntt = L.take<int>(nc + 1);
-        o_stt = L.take<int>(nc + 1);
-        o_ft = L.take<int>(nc + 1);
+        o_kt = L.take<int2>(nt);
         o_pt = L.take<int>(nt);
         o_ptt = L.take<int>(nt);
     }
-    size_t o_st = L.take<int>(scan_tmp_ints(nc + 1));
     const int item_cap = 4 * nt + 4096;
     size_t o_cnt = L.take<int>(4), o_it = L.take<int4>(item_cap);
     size_t o_sa, o_sb = 0, o_sf, o_ta = 0, o_tb = 0;
@@ -439,26 +437,24 @@ size_t plan_layout(pb_plan_s* P, bool assign)
         P->x = (double*)(A + o_x);
         P->f = (double*)(A + o_f);
         P->y = P->all_same ? nullptr : (double*)(A + o_y);
-        P->ypack = P->all_same ? P->x : (double*)(A + o_yp);
         P->U = (double*)(A + o_U);
-        P->cell_of_s = (int*)(A + o_cs);
-        P->cnt_s = (int*)(A + o_cnts);
+        P->key_s = (int2*)(A + o_ks);
+        P->cl_zero = (int*)(A + o_clz);
+        P->cl_zero_bytes = zero_bytes;
         P->start_s = (int*)(A + o_sts);
-        P->fill_s = (int*)(A + o_fs);
         P->perm_s = (int*)(A + o_ps);
         P->perm_tmp_s = (int*)(A + o_pts);
         if (!P->all_same) {
-            P->cell_of_t = (int*)(A + o_ct);
-            P->cnt_t = (int*)(A + o_cntt);
-            P->start_t = (int*)(A + o_stt);
-            P->fill_t = (int*)(A + o_ft);
+            P->key_t = (int2*)(A + o_kt);
+            P->start_t = P->start_s + cell_list_stride(nc);
             P->perm_t = (int*)(A + o_pt);
             P->perm_tmp_t = (int*)(A + o_ptt);
         } else {
+            P->key_t = nullptr;
             P->start_t = P->start_s;
             P->perm_t = P->perm_s;
+            P->perm_tmp_t = nullptr;
         }
-        P->scan_tmp = (int*)(A + o_st);
         P->counter = (int*)(A + o_cnt);
         P->items = (int4*)(A + o_it);
         P->spos_a = A + o_sa;
@@ -729,15 +725,40 @@ int plan_alloc(pb_plan_s* P)
     return PB_OK;
 }
 
-void bin_and_sort(pb_plan_s* P, const double* pos, int n, const int* d_off, int* cell_of, int* cnt, int* start,
-                  int* fill, int* perm_tmp, int* perm, cudaStream_t s)
+// Cell lists and sorted records of the sources and (when they have their own)
+// the targets.
+void build_cell_lists(pb_plan_s* P, cudaStream_t s)
 {
-    cudaMemsetAsync(cnt, 0, sizeof(int) * (P->ncell + 1), s);
-    cudaMemsetAsync(fill, 0, sizeof(int) * (P->ncell + 1), s);
-    launch_bin(pos, n, d_off, P->d_inst, P->count, cell_of, cnt, P->d_bad, s);
-    launch_exclusive_scan(cnt, start, P->ncell, P->scan_tmp, s, P->d_cell_off + P->count);
-    launch_scatter(cell_of, n, d_off + P->count, start, fill, perm_tmp, s);
-    launch_sort_cells(perm_tmp, perm, start, P->ncell, P->d_cell_off, P->d_inst, P->count, pos, P->nsm, s);
+    cudaMemsetAsync(P->cl_zero, 0, P->cl_zero_bytes, s);
+    CellListArgs a;
+    a.x = P->x;
+    a.f = P->f;
+    a.y = P->y;
+    a.src_off = P->d_src_off;
+    a.tgt_off = P->d_tgt_off;
+    a.y_off = P->d_y_off;
+    a.cell_off = P->d_cell_off;
+    a.inst = P->d_inst;
+    a.ninst = P->count;
+    a.ncap_s = P->n_src;
+    a.ncap_t = P->all_same ? 0 : P->n_tgt;
+    a.two = P->all_same ? 0 : 1;
+    a.ncell_cap = std::max(P->ncell, 1);
+    a.key_s = P->key_s;
+    a.key_t = P->key_t;
+    a.zero = P->cl_zero;
+    a.start = P->start_s;
+    a.perm_tmp_s = P->perm_tmp_s;
+    a.perm_tmp_t = P->perm_tmp_t;
+    a.perm_s = P->perm_s;
+    a.perm_t = P->perm_t;
+    a.spos_a = P->spos_a;
+    a.spos_b = P->spos_b;
+    a.sfrc = P->sfrc;
+    a.tpos_a = P->tpos_a;
+    a.tpos_b = P->tpos_b;
+    a.bad = P->d_bad;
+    launch_cell_lists(a, P->prec == PB_PREC_MIXED, P->nsm, s);
 }
 
 // PB_SPREAD=atomic selects the point-wise spreading kernel (with a grid
@@ -766,25 +787,15 @@ void run_compute(pb_plan_s* P, cudaStream_t s, bool forces_only)
     NvtxRange nv_all("pb.compute");
     record(P, 0, s);
     cudaMemsetAsync(P->d_bad, 0, sizeof(int) * (P->count + 1), s);
-    if (!forces_only)
-        bin_and_sort(P, P->x, P->n_src, P->d_src_off, P->cell_of_s, P->cnt_s, P->start_s, P->fill_s, P->perm_tmp_s,
-                     P->perm_s, s);
-    if (mixed)
-        launch_prepare_mixed(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count, (float4*)P->spos_a,
-                             (float4*)P->spos_b, (float4*)P->sfrc, P->d_bad, s);
-    else
-        launch_prepare_fp64(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count, (Dbl4*)P->spos_a,
-                            (Dbl4*)P->sfrc, P->d_bad, s);
-    if (!P->all_same && !forces_only) {
-        launch_pack_targets(P->x, P->y, P->n_tgt, P->d_tgt_off, P->d_src_off, P->d_y_off, P->count, P->ypack, s);
-        bin_and_sort(P, P->ypack, P->n_tgt, P->d_tgt_off, P->cell_of_t, P->cnt_t, P->start_t, P->fill_t,
-                     P->perm_tmp_t, P->perm_t, s);
+    if (forces_only) {  // the source records again, in the sorted order of the last full execution
         if (mixed)
-            launch_prepare_mixed(P->ypack, nullptr, P->perm_t, P->n_tgt, P->d_tgt_off, P->d_inst, P->count,
-                                 (float4*)P->tpos_a, (float4*)P->tpos_b, nullptr, P->d_bad, s);
+            launch_prepare_mixed(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count,
+                                 (float4*)P->spos_a, (float4*)P->spos_b, (float4*)P->sfrc, P->d_bad, s);
         else
-            launch_prepare_fp64(P->ypack, nullptr, P->perm_t, P->n_tgt, P->d_tgt_off, P->d_inst, P->count,
-                                (Dbl4*)P->tpos_a, nullptr, P->d_bad, s);
+            launch_prepare_fp64(P->x, P->f, P->perm_s, P->n_src, P->d_src_off, P->d_inst, P->count,
+                                (Dbl4*)P->spos_a, (Dbl4*)P->sfrc, P->d_bad, s);
+    } else {
+        build_cell_lists(P, s);
     }
     if (!forces_only)
         launch_build_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items, P->item_cap,

@@ -11,29 +11,41 @@ namespace pb {
 // Every particle kernel is launched for a capacity `ncap` and reads the actual
 // count from device memory (offsets[ninst]), so one captured graph serves any
 // set of instances that fits the capacity.
-// cell_of[p] = global cell index of particle p (instance cell_off + local cell),
-// counts[cell] += 1.  pos: AoS doubles of all instances, offsets: ninst+1 prefix.
-// Non-finite coordinates (and forces, in the prepare kernels) are replaced by 0
-// and set bad[instance] = 1 (bad may be null).
-void launch_bin(const double* pos, int ncap, const int* offsets, const PbInst* inst, int ninst,
-                int* cell_of, int* counts, int* bad, cudaStream_t s);
-// Exclusive scan of n ints into out (out has n+1 entries; out[n] = total).
-// tmp must hold scan_tmp_ints(n) ints.  With n_act (device), only the first
-// *n_act entries may be nonzero and out is valid up to index *n_act.
-size_t scan_tmp_ints(int n);
-void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s, const int* n_act = nullptr);
-// perm[start[c] + k] = particle, fill must be zeroed.
-void launch_scatter(const int* cell_of, int ncap, const int* ntot, const int* start, int* fill, int* perm,
-                    cudaStream_t s);
-// Sort each cell's perm entries by (wrapped z as FP32, index); cell_offsets[ninst] = actual cells.
-void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap, const int* cell_offsets,
-                       const PbInst* inst, int ninst, const double* pos, int nsm, cudaStream_t s);
-// Sorted particle records.  Mixed: pos_hi (x,y,z, w = instance bits), pos_lo, frc.
+// Sorted particle records again from the permutation of the last cell-list
+// build (new forces at the same positions).  Mixed: pos_hi (x,y,z, w =
+// instance bits), pos_lo, frc.  Non-finite coordinates and forces are replaced
+// by 0 and set bad[instance] = 1 (bad may be null).
 void launch_prepare_mixed(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                           const PbInst* inst, int ninst, float4* pos_hi, float4* pos_lo, float4* frc_out, int* bad,
                           cudaStream_t s);
 void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                          const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, int* bad, cudaStream_t s);
+// Cell lists of the sources and, when they have their own, of the targets, in
+// four launches shared by both sets: binning (cell and arrival slot of every
+// particle), one decoupled look-back scan per set, the scatter, and a sort of
+// every cell by (wrapped z as FP32, index) fused with the writing of the
+// sorted particle records.  Instance q's targets are read from y when
+// y_off[q] >= 0, else they are its sources.  The zero region (counts, scan
+// flags, tickets; cell_list_zero_bytes) must be zeroed before every build.
+struct CellListArgs {
+    const double *x, *f, *y;
+    const int *src_off, *tgt_off, *y_off, *cell_off;
+    const PbInst* inst;
+    int ninst;
+    int ncap_s, ncap_t;   // launch capacities
+    int two;              // the targets have their own cell list (else they are the sources)
+    int ncell_cap;
+    int cstride, ntiles;  // set by launch_cell_lists: count stride, scan tiles per set
+    int2 *key_s, *key_t;  // per particle: (global cell, arrival slot in the cell)
+    int* zero;            // zero region: counts [2][cstride], tickets, look-back flags
+    int* start;           // cell starts [2][cstride] (targets at cstride)
+    int *perm_tmp_s, *perm_tmp_t, *perm_s, *perm_t;
+    void *spos_a, *spos_b, *sfrc, *tpos_a, *tpos_b;  // records (mixed: hi, lo, force; FP64: pos, force)
+    int* bad;             // per instance, then the execution status word at [ninst]
+};
+int cell_list_stride(int ncell_cap);
+size_t cell_list_zero_bytes(int ncell_cap);
+void launch_cell_lists(const CellListArgs& a, bool mixed, int nsm, cudaStream_t s);
 // Work items: up to 32 consecutive targets of one cell row spanning <= 8 cells,
 // times csplit stencil column groups:
 // int4 {inst, first target, local row, count | za << 8 | zb << 16 | group << 24}.
@@ -79,11 +91,6 @@ void launch_spread_tiles(const PbInst* inst, const int* bucket_inst, int nb, con
 void launch_zero_grids(const PbInst* inst, int ninst, void* grid, int esz, cudaStream_t s);
 size_t twiddle_bytes(const int* M, bool fp64);
 void fill_twiddles(const int* M, bool fp64, void* host_buf);
-
-// Gather the packed target list: instance q's targets come from y (its own
-// targets) or from x (targets are its sources).
-void launch_pack_targets(const double* x, const double* y, int ncap, const int* tgt_off, const int* src_off,
-                         const int* y_off, int ninst, double* out, cudaStream_t s);
 
 // ---- final combine ----
 void launch_combine_mixed(const PbInst* inst, int ninst, const int* tgt_offsets, int ncap, const int* tperm,

@@ -1,5 +1,6 @@
-// Cell binning, counting sort and work-item construction for the real-space
-// sum (device-built cell list over all instances of a batch).
+// Cell binning, counting sort, sorted particle records and work-item
+// construction for the real-space sum and the tiled spreading (device-built
+// cell lists over all instances of a batch).
 #include "pb_device.cuh"
 #include "pb_kernels.h"
 
@@ -13,36 +14,7 @@ __device__ __forceinline__ double finite_or_flag(double v, int* bad, int q)
     return 0.0;
 }
 
-__global__ void k_bin(const double* __restrict__ pos, const int* __restrict__ offsets,
-                      const PbInst* __restrict__ inst, int ninst, int* __restrict__ cell_of, int* __restrict__ counts,
-                      int* __restrict__ bad)
-{
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= offsets[ninst]) return;
-    int q = find_instance(offsets, ninst, p);
-    const PbInst& I = inst[q];
-    int c[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        double w = wrap_coord_r(finite_or_flag(pos[3 * (size_t)p + a], bad, q), I.L[a], I.iL[a]);
-        int ci = (int)(w * I.ih[a]);
-        c[a] = ci >= I.nc[a] ? I.nc[a] - 1 : ci;
-    }
-    int g = I.cell_off + (c[0] * I.nc[1] + c[1]) * I.nc[2] + c[2];
-    cell_of[p] = g;
-    atomicAdd(&counts[g], 1);
-}
-
-void launch_bin(const double* pos, int ncap, const int* offsets, const PbInst* inst, int ninst, int* cell_of,
-                int* counts, int* bad, cudaStream_t s)
-{
-    if (ncap <= 0) return;
-    k_bin<<<(ncap + 255) / 256, 256, 0, s>>>(pos, offsets, inst, ninst, cell_of, counts, bad);
-}
-
-// ---- exclusive scan (reduce-then-scan, recursive over block sums) ----
-constexpr int kScanBlock = 1024;
-
+// Block-wide exclusive prefix sum (all threads of the block take part).
 __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums)
 {
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -66,152 +38,6 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums)
     __syncthreads();
     int base = wid > 0 ? warp_sums[wid - 1] : 0;
     return base + x - v;
-}
-
-// n_act (optional): entries at and beyond *n_act are zero and their outputs are
-// not needed past index *n_act, so blocks that start beyond it only report 0.
-__global__ void k_scan_blocks(const int* __restrict__ in, int* __restrict__ out, int n, int* __restrict__ block_sums,
-                              const int* __restrict__ n_act)
-{
-    __shared__ int ws[32];
-    if (n_act && blockIdx.x * kScanBlock > *n_act) {
-        if (threadIdx.x == 0) block_sums[blockIdx.x] = 0;
-        return;
-    }
-    int i = blockIdx.x * kScanBlock + threadIdx.x;
-    int v = i < n ? in[i] : 0;
-    int ex = block_exclusive_scan(v, ws);
-    if (i < n) out[i] = ex;
-    if (threadIdx.x == blockDim.x - 1) block_sums[blockIdx.x] = ex + v;
-}
-
-__global__ void k_scan_add(int* __restrict__ out, int n, const int* __restrict__ block_offsets,
-                           const int* __restrict__ n_act)
-{
-    if (n_act && blockIdx.x * kScanBlock > *n_act) return;
-    int i = blockIdx.x * kScanBlock + threadIdx.x;
-    if (i < n) out[i] += block_offsets[blockIdx.x];
-}
-
-__global__ void k_set_total(int* out, int n, const int* in, const int* n_act)
-{
-    // out[n] = out[n-1] + in[n-1] (with fewer actual entries, out[n_act] is the total already)
-    if (n_act && *n_act < n) return;
-    out[n] = (n > 0) ? out[n - 1] + in[n - 1] : 0;
-}
-
-size_t scan_tmp_ints(int n)
-{
-    size_t total = 0;
-    int m = n;
-    while (m > 1) {
-        int nb = (m + kScanBlock - 1) / kScanBlock;
-        total += 2 * (size_t)nb + 2;
-        m = nb;
-    }
-    return total + 4;
-}
-
-static void scan_rec(const int* in, int* out, int n, int* tmp, const int* n_act, cudaStream_t s)
-{
-    int nb = (n + kScanBlock - 1) / kScanBlock;
-    int* sums = tmp;
-    int* sums_scan = tmp + nb + 1;
-    k_scan_blocks<<<nb, kScanBlock, 0, s>>>(in, out, n, sums, n_act);
-    if (nb > 1) {
-        scan_rec(sums, sums_scan, nb, tmp + 2 * (size_t)nb + 2, nullptr, s);
-        k_scan_add<<<nb, kScanBlock, 0, s>>>(out, n, sums_scan, n_act);
-    }
-}
-
-void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s, const int* n_act)
-{
-    if (n <= 0) {
-        cudaMemsetAsync(out, 0, sizeof(int), s);
-        return;
-    }
-    scan_rec(in, out, n, tmp, n_act, s);
-    k_set_total<<<1, 1, 0, s>>>(out, n, in, n_act);
-}
-
-__global__ void k_scatter(const int* __restrict__ cell_of, const int* __restrict__ ntot, const int* __restrict__ start,
-                          int* __restrict__ fill, int* __restrict__ perm)
-{
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= *ntot) return;
-    int c = cell_of[p];
-    int slot = start[c] + atomicAdd(&fill[c], 1);
-    perm[slot] = p;
-}
-
-void launch_scatter(const int* cell_of, int ncap, const int* ntot, const int* start, int* fill, int* perm,
-                    cudaStream_t s)
-{
-    if (ncap <= 0) return;
-    k_scatter<<<(ncap + 255) / 256, 256, 0, s>>>(cell_of, ntot, start, fill, perm);
-}
-
-// Rank sort of each cell's entries by (z, index) (a warp per cell, persistent
-// over the actual cells): entry v goes to slot start + #{u in cell : (z_u, u) <
-// (z_v, v)}, z the coordinate wrapped in FP32.  Consecutive targets
-// then lie close in z, which narrows the z-range of a real-space work item.
-// Cells of more than kSortMax entries keep the (index) scatter order.
-constexpr int kSortMax = 1024;
-
-__global__ void k_sort_cells(const int* __restrict__ perm_in, int* __restrict__ perm_out,
-                             const int* __restrict__ start, const int* __restrict__ cell_offsets,
-                             const PbInst* __restrict__ inst, int ninst, const double* __restrict__ pos)
-{
-    const int ncell = cell_offsets[ninst];
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < ncell; cell += nwarps) {
-        const int b = start[cell], e = start[cell + 1], n = e - b;
-        if (n <= 1) {
-            if (n == 1 && lane == 0) perm_out[b] = perm_in[b];
-            continue;
-        }
-        const int q = find_instance(cell_offsets, ninst, cell);
-        if (n > kSortMax) {
-            for (int i = lane; i < n; i += 32) perm_out[b + i] = perm_in[b + i];
-            continue;
-        }
-        const PbInst& I = inst[q];
-        // FP32 key (the order only shapes the work items; FP64 would cost the GPU's slow FP64 pipe)
-        const float Lz = (float)I.L[2], iLz = (float)I.iL[2];
-        auto zkey = [&](int v) {
-            float z = (float)pos[3 * (size_t)v + 2];
-            z -= Lz * floorf(z * iLz);
-            return (z == z) ? z : 0.f;
-        };
-        for (int ib = 0; ib < n; ib += 32) {
-            const int i = ib + lane;
-            const int v = i < n ? perm_in[b + i] : 0;
-            const float z = i < n ? zkey(v) : 0.f;
-            int rank = 0;
-            for (int jb = 0; jb < n; jb += 32) {
-                const int j = jb + lane;
-                const int u = j < n ? perm_in[b + j] : 0;
-                const float zu = j < n ? zkey(u) : 0.f;
-                const int m = min(32, n - jb);
-                for (int k = 0; k < m; k++) {
-                    const int uk = __shfl_sync(kFull, u, k);
-                    const float zk = __shfl_sync(kFull, zu, k);
-                    rank += (zk < z) || (zk == z && uk < v);
-                }
-            }
-            if (i < n) perm_out[b + rank] = v;
-        }
-    }
-}
-
-void launch_sort_cells(int* perm, int* perm_tmp, const int* start, int ncell_cap, const int* cell_offsets,
-                       const PbInst* inst, int ninst, const double* pos, int nsm, cudaStream_t s)
-{
-    if (ncell_cap <= 0) return;
-    long long blocks = ((long long)ncell_cap * 32 + 255) / 256;
-    if (blocks > (long long)nsm * 16) blocks = (long long)nsm * 16;
-    k_sort_cells<<<(int)blocks, 256, 0, s>>>(perm, perm_tmp, start, cell_offsets, inst, ninst, pos);
 }
 
 __global__ void k_prepare_mixed(const double* __restrict__ pos, const double* __restrict__ frc,
@@ -363,29 +189,257 @@ void launch_build_items(const int* start, int ncell_cap, const int* cell_offsets
                                                           status);
 }
 
-}  // namespace pb
+// ---- cell lists of sources and targets, four launches for both ----
+// Particle side: index p < ncap_s is source p, p >= ncap_s is target p - ncap_s.
+// The counts of the two sets are cstride apart, as are their starts.
+constexpr int kCellScanThreads = 1024;
+constexpr int kCellScanTile = 4 * kCellScanThreads;  // counts per scan block (four per thread)
+constexpr unsigned long long kFlagAgg = 1ull << 62, kFlagPrefix = 2ull << 62;
+constexpr int kScanSpinLimit = 1 << 22;  // look-back waits (with back-off) before a block gives up
+constexpr int kSortMax = 1024;           // larger cells keep the scatter order
 
-namespace pb {
+int cell_list_stride(int ncell_cap) { return (ncell_cap + 1 + 3) & ~3; }
 
-__global__ void k_pack_targets(const double* __restrict__ x, const double* __restrict__ y,
-                               const int* __restrict__ tgt_off, const int* __restrict__ src_off,
-                               const int* __restrict__ y_off, int ninst, double* __restrict__ out)
+static int cell_scan_tiles(int ncell_cap) { return (cell_list_stride(ncell_cap) + kCellScanTile - 1) / kCellScanTile; }
+
+// counts [2][cstride], two tickets (+ padding to 16 bytes), look-back flags [2][tiles]
+size_t cell_list_zero_bytes(int ncell_cap)
 {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= tgt_off[ninst]) return;
-    int q = find_instance(tgt_off, ninst, p);
-    int local = p - tgt_off[q];
-    const double* src = (y_off[q] >= 0) ? (y + 3 * (size_t)(y_off[q] + local)) : (x + 3 * (size_t)(src_off[q] + local));
-    out[3 * (size_t)p] = src[0];
-    out[3 * (size_t)p + 1] = src[1];
-    out[3 * (size_t)p + 2] = src[2];
+    return sizeof(int) * (2 * (size_t)cell_list_stride(ncell_cap) + 4) +
+           sizeof(unsigned long long) * 2 * (size_t)cell_scan_tiles(ncell_cap);
 }
 
-void launch_pack_targets(const double* x, const double* y, int ncap, const int* tgt_off, const int* src_off,
-                         const int* y_off, int ninst, double* out, cudaStream_t s)
+// Position of target t of instance q: its own targets (y) or its sources (x).
+__device__ __forceinline__ const double* cl_target(const CellListArgs& A, int q, int t)
 {
-    if (ncap <= 0) return;
-    k_pack_targets<<<(ncap + 255) / 256, 256, 0, s>>>(x, y, tgt_off, src_off, y_off, ninst, out);
+    const int yo = A.y_off[q], local = t - A.tgt_off[q];
+    return yo >= 0 ? A.y + 3 * (size_t)(yo + local) : A.x + 3 * (size_t)(A.src_off[q] + local);
+}
+
+__global__ void k_bin_cells(CellListArgs A)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= A.ncap_s + A.ncap_t) return;  // (with no target set, tgt_off counts the sources)
+    const bool tgt = p >= A.ncap_s;
+    const int i = tgt ? p - A.ncap_s : p;
+    const int* off = tgt ? A.tgt_off : A.src_off;
+    if (i >= off[A.ninst]) return;
+    const int q = find_instance(off, A.ninst, i);
+    const PbInst& I = A.inst[q];
+    const double* pos = tgt ? cl_target(A, q, i) : A.x + 3 * (size_t)i;
+    int c[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const double w = wrap_coord_r(finite_or_flag(pos[a], A.bad, q), I.L[a], I.iL[a]);
+        const int ci = (int)(w * I.ih[a]);
+        c[a] = ci >= I.nc[a] ? I.nc[a] - 1 : ci;
+    }
+    const int g = I.cell_off + (c[0] * I.nc[1] + c[1]) * I.nc[2] + c[2];
+    const int slot = atomicAdd(&A.zero[(tgt ? A.cstride : 0) + g], 1);
+    (tgt ? A.key_t : A.key_s)[i] = make_int2(g, slot);
+}
+
+// Exclusive scan of the counts [0, n_act] of each set (the entry at n_act is
+// zero and receives the total), single pass: blocks take tiles in the order
+// they start (a ticket per set), publish their tile's sum, and add the sums
+// of the tiles before theirs by looking back until a tile with its inclusive
+// prefix published.  A block waits only on tiles whose blocks started before
+// it, so every wait ends; each wait is bounded all the same (kScanStall).
+__global__ void __launch_bounds__(kCellScanThreads) k_scan_cells(CellListArgs A, int nsets)
+{
+    __shared__ int ws[32];
+    __shared__ int s_ticket, s_prefix;
+    const int cstride = A.cstride, ntiles = A.ntiles;
+    int* tickets = A.zero + 2 * cstride;
+    unsigned long long* flags = reinterpret_cast<unsigned long long*>(tickets + 4);
+    const int set = nsets == 2 ? (int)(blockIdx.x & 1) : 0;
+    if (threadIdx.x == 0) s_ticket = atomicAdd(&tickets[set], 1);
+    __syncthreads();
+    const int tile = s_ticket;
+    const int n = A.cell_off[A.ninst] + 1;
+    const int base = tile * kCellScanTile;
+    if (tile >= ntiles || base >= n) return;
+    const int* cnt = A.zero + set * cstride;
+    int* out = A.start + set * cstride;
+    unsigned long long* fl = flags + (size_t)set * ntiles;
+    const int i0 = base + 4 * threadIdx.x;
+    int4 v = make_int4(0, 0, 0, 0);
+    if (i0 < n) v = *reinterpret_cast<const int4*>(cnt + i0);  // cstride is a multiple of 4: in bounds
+    const int sum = v.x + v.y + v.z + v.w;
+    const int ex = block_exclusive_scan(sum, ws);
+    if (threadIdx.x == kCellScanThreads - 1) {
+        const int total = ex + sum;
+        if (tile == 0) {
+            atomicExch(&fl[0], kFlagPrefix | (unsigned)total);
+            s_prefix = 0;
+        } else {
+            atomicExch(&fl[tile], kFlagAgg | (unsigned)total);
+            int prefix = 0, j = tile - 1, spins = 0;
+            while (j >= 0) {
+                const unsigned long long w = atomicAdd(&fl[j], 0ull);
+                if ((w >> 62) == 0) {
+                    if (++spins > kScanSpinLimit) {
+                        atomicOr(&A.bad[A.ninst], kScanStall);
+                        break;
+                    }
+                    __nanosleep(spins < 64 ? 32 : 256);
+                    continue;
+                }
+                prefix += (int)(unsigned)(w & 0xffffffffu);
+                if ((w >> 62) == 2) break;
+                j--;
+            }
+            atomicExch(&fl[tile], kFlagPrefix | (unsigned)(prefix + total));
+            s_prefix = prefix;
+        }
+    }
+    __syncthreads();
+    const int e = s_prefix + ex;
+    const int r[4] = {e, e + v.x, e + v.x + v.y, e + v.x + v.y + v.z};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (i0 + k < n) out[i0 + k] = r[k];
+}
+
+__global__ void k_scatter_cells(CellListArgs A)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= A.ncap_s + A.ncap_t) return;
+    const bool tgt = p >= A.ncap_s;
+    const int i = tgt ? p - A.ncap_s : p;
+    if (i >= (tgt ? A.tgt_off : A.src_off)[A.ninst]) return;
+    const int2 k = (tgt ? A.key_t : A.key_s)[i];
+    const int* start = A.start + (tgt ? A.cstride : 0);
+    (tgt ? A.perm_tmp_t : A.perm_tmp_s)[start[k.x] + k.y] = i;
+}
+
+// The sorted record of particle v of instance q at position `slot` of its list.
+template <bool MIXED>
+__device__ __forceinline__ void cl_record(const CellListArgs& A, bool tgt, int q, int v, const double* pos, int slot)
+{
+    const PbInst& I = A.inst[q];
+    double w[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) w[a] = wrap_coord_r(finite_or_flag(pos[a], A.bad, q), I.L[a], I.iL[a]);
+    const double* fr = tgt ? nullptr : A.f + 3 * (size_t)v;
+    if constexpr (MIXED) {
+        float hi[3], lo[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) split_double(w[a], hi[a], lo[a]);
+        float4* ph = (float4*)(tgt ? A.tpos_a : A.spos_a);
+        float4* pl = (float4*)(tgt ? A.tpos_b : A.spos_b);
+        ph[slot] = make_float4(hi[0], hi[1], hi[2], __int_as_float(q));
+        pl[slot] = make_float4(lo[0], lo[1], lo[2], 0.f);
+        if (fr)
+            ((float4*)A.sfrc)[slot] = make_float4((float)finite_or_flag(fr[0], A.bad, q),
+                                                  (float)finite_or_flag(fr[1], A.bad, q),
+                                                  (float)finite_or_flag(fr[2], A.bad, q), 0.f);
+    } else {
+        ((Dbl4*)(tgt ? A.tpos_a : A.spos_a))[slot] = make_dbl4(w[0], w[1], w[2], (double)q);
+        if (fr)
+            ((Dbl4*)A.sfrc)[slot] = make_dbl4(finite_or_flag(fr[0], A.bad, q), finite_or_flag(fr[1], A.bad, q),
+                                              finite_or_flag(fr[2], A.bad, q), 0.0);
+    }
+}
+
+// Sort of every cell by (z wrapped in FP32, index), eight lanes per cell,
+// fused with the writing of the sorted records: entry v goes to slot
+// start + #{u in cell : (z_u, u) < (z_v, v)}.  Consecutive targets then lie
+// close in z (narrower real-space work items) and the order, hence every
+// summation order downstream, does not depend on the scatter's atomics.
+// Cells of more than kSortMax entries keep the scatter order.
+template <bool MIXED>
+__global__ void k_sort_prepare(CellListArgs A, int nsets)
+{
+    const int ncell = A.cell_off[A.ninst];
+    const int lane = threadIdx.x & 31, l8 = lane & 7;
+    const unsigned gmask = 0xffu << (lane & ~7);
+    const int ngroups = (gridDim.x * blockDim.x) >> 3;
+    const int cstride = A.cstride;
+    for (int cg = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; cg < nsets * ncell; cg += ngroups) {
+        const bool tgt = cg >= ncell;
+        const int cell = tgt ? cg - ncell : cg;
+        const int* start = A.start + (tgt ? cstride : 0);
+        const int b = start[cell], n = start[cell + 1] - b;
+        if (n == 0) continue;
+        const int q = find_instance(A.cell_off, A.ninst, cell);
+        const int* ptmp = tgt ? A.perm_tmp_t : A.perm_tmp_s;
+        int* perm = tgt ? A.perm_t : A.perm_s;
+        // the instance's particle range: after a scan that gave up (kScanStall) slots may be stale
+        const int* off = tgt ? A.tgt_off : A.src_off;
+        const int vlo = off[q], vhi = off[q + 1];
+        auto valid = [&](int v) {
+            if (v >= vlo && v < vhi) return true;
+            atomicOr(&A.bad[A.ninst], kScanStall);
+            return false;
+        };
+        auto position = [&](int v) { return tgt ? cl_target(A, q, v) : A.x + 3 * (size_t)v; };
+        if (n > kSortMax) {
+            for (int i = l8; i < n; i += 8) {
+                const int v = ptmp[b + i];
+                if (!valid(v)) continue;
+                perm[b + i] = v;
+                cl_record<MIXED>(A, tgt, q, v, position(v), b + i);
+            }
+            continue;
+        }
+        // FP32 key (the order only shapes the work items; FP64 would cost the GPU's slow FP64 pipe)
+        const PbInst& I = A.inst[q];
+        const float Lz = (float)I.L[2], iLz = (float)I.iL[2];
+        auto zkey = [&](const double* pv) {
+            float z = (float)pv[2];
+            z -= Lz * floorf(z * iLz);
+            return (z == z) ? z : 0.f;
+        };
+        for (int ib = 0; ib < n; ib += 8) {
+            const int i = ib + l8;
+            const int v = i < n ? ptmp[b + i] : vlo;
+            const bool ok = i < n && valid(v);
+            const double* pv = ok ? position(v) : nullptr;
+            const float z = ok ? zkey(pv) : 0.f;
+            int rank = 0;
+            for (int jb = 0; jb < n; jb += 8) {
+                int u = v;
+                float zu = z;
+                if (jb != ib) {
+                    const int j = jb + l8;
+                    u = j < n ? ptmp[b + j] : vlo;
+                    zu = (j < n && u >= vlo && u < vhi) ? zkey(position(u)) : 0.f;
+                }
+                const int m = min(8, n - jb);
+                for (int k = 0; k < m; k++) {
+                    const int uk = __shfl_sync(gmask, u, k, 8);
+                    const float zk = __shfl_sync(gmask, zu, k, 8);
+                    rank += (zk < z) || (zk == z && uk < v);
+                }
+            }
+            if (ok) {
+                perm[b + rank] = v;
+                cl_record<MIXED>(A, tgt, q, v, pv, b + rank);
+            }
+        }
+    }
+}
+
+void launch_cell_lists(const CellListArgs& args, bool mixed, int nsm, cudaStream_t s)
+{
+    CellListArgs a = args;
+    a.cstride = cell_list_stride(a.ncell_cap);
+    a.ntiles = cell_scan_tiles(a.ncell_cap);
+    const int nsets = a.two ? 2 : 1;
+    if (!a.two) a.ncap_t = 0;
+    if (a.ncell_cap <= 0) return;
+    const long long np = (long long)a.ncap_s + a.ncap_t;
+    const unsigned pblocks = (unsigned)((np + 255) / 256);
+    if (np > 0) k_bin_cells<<<pblocks, 256, 0, s>>>(a);
+    k_scan_cells<<<(unsigned)(nsets * a.ntiles), kCellScanThreads, 0, s>>>(a, nsets);  // empty sets get zero starts
+    if (np > 0) k_scatter_cells<<<pblocks, 256, 0, s>>>(a);
+    long long blocks = ((long long)nsets * a.ncell_cap * 8 + 255) / 256;
+    if (blocks > (long long)nsm * 16) blocks = (long long)nsm * 16;
+    if (mixed)
+        k_sort_prepare<true><<<(unsigned)blocks, 256, 0, s>>>(a, nsets);
+    else
+        k_sort_prepare<false><<<(unsigned)blocks, 256, 0, s>>>(a, nsets);
 }
 
 }  // namespace pb

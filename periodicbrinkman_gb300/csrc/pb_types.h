@@ -27,6 +27,7 @@ constexpr int kMaxCheb = 40;    // max terms of the near and blob Chebyshev seri
 constexpr int kNumSeries = 16;  // terms of the FP64 small-r series
 constexpr int kMaxCheb64 = 48;  // max terms of the FP64 far Chebyshev series (FP64 path)
 constexpr int kCapItems = 1;    // execution status bit: real-space work items beyond the item array
+constexpr int kScanStall = 2;   // execution status bit: a cell-count scan gave up waiting for a predecessor
 
 // Per-instance real-space kernel tables (built in FP64 on the host).  The pair
 // kernel H = (R_eps - R_d) inside the blob region, S - R_d outside it, is
