@@ -21,10 +21,10 @@ void launch_prepare_mixed(const double* pos, const double* frc, const int* perm,
 void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, int ncap, const int* offsets,
                          const PbInst* inst, int ninst, Dbl4* pos_out, Dbl4* frc_out, int* bad, cudaStream_t s);
 // Cell lists of the sources and, when they have their own, of the targets, in
-// four launches shared by both sets: binning (cell and arrival slot of every
-// particle), one decoupled look-back scan per set, the scatter, and a sort of
-// every cell by (wrapped z as FP32, index) fused with the writing of the
-// sorted particle records.  Instance q's targets are read from y when
+// four launches shared by both sets: binning (cell, arrival slot and z key of
+// every particle), one decoupled look-back scan per set, the scatter, and a
+// thread per particle ranking it in its cell by (wrapped z as FP32, index)
+// and writing its sorted record.  Instance q's targets are read from y when
 // y_off[q] >= 0, else they are its sources.  The zero region (counts, scan
 // flags, tickets; cell_list_zero_bytes) must be zeroed before every build.
 struct CellListArgs {
@@ -36,17 +36,18 @@ struct CellListArgs {
     int two;              // the targets have their own cell list (else they are the sources)
     int ncell_cap;
     int cstride, ntiles;  // set by launch_cell_lists: count stride, scan tiles per set
-    int2 *key_s, *key_t;  // per particle: (global cell, arrival slot in the cell)
+    int4 *key_s, *key_t;  // per particle: {global cell, arrival slot in it, instance, z key bits}
     int* zero;            // zero region: counts [2][cstride], tickets, look-back flags
     int* start;           // cell starts [2][cstride] (targets at cstride)
-    int *perm_tmp_s, *perm_tmp_t, *perm_s, *perm_t;
+    int2 *perm_tmp_s, *perm_tmp_t;  // per cell, in arrival order: {particle, z key bits}
+    int *perm_s, *perm_t;           // sorted position -> particle
     void *spos_a, *spos_b, *sfrc, *tpos_a, *tpos_b;  // records (mixed: hi, lo, force; FP64: pos, force)
     int* bad;             // per instance, then the execution status word at [ninst]
 };
 int cell_list_stride(int ncell_cap);
 size_t cell_list_zero_bytes(int ncell_cap);
 void launch_cell_lists(const CellListArgs& a, bool mixed, int nsm, cudaStream_t s);
-// Work items: up to 32 consecutive targets of one cell row spanning <= 8 cells,
+// Work items: up to 32 consecutive targets of one cell row spanning <= kItemCells cells,
 // times csplit stencil column groups:
 // int4 {inst, first target, local row, count | za << 8 | zb << 16 | group << 24}.
 // Builds the items of all row-start cells (cell_offsets[ninst] = actual cells);

@@ -1,7 +1,7 @@
 // Real-space Ewald sum over a device-built cell list.
 //
-// Work item = (instance, cell row (c0, c1), z-range [za, zb] of at most 8
-// cells, up to 32 consecutive sorted targets, a group of the stencil's
+// Work item = (instance, cell row (c0, c1), z-range [za, zb] of at most
+// kItemCells cells, up to 32 consecutive sorted targets, a group of the stencil's
 // columns), one warp per item, items pulled from a global counter by a
 // persistent grid.  Each lane owns one target.  Each stencil column is cut to
 // the part of the cutoff ball around the targets' box; its contiguous z-runs
@@ -36,7 +36,7 @@ namespace pb {
 constexpr int kRealWarps = 4;
 
 constexpr int kMaxReach = 15;  // stencil reach S per axis
-constexpr int kZTab = 8 + 2 * kMaxReach;
+constexpr int kZTab = kItemCells + 2 * kMaxReach;
 
 // item = {instance, first target, local row c0*nc1 + c1, count | za << 8 | zb << 16 | group << 24}:
 // the item covers the stencil columns col = group, group + csplit, ... of its rows

@@ -121,8 +121,10 @@ void finish_slot(pb_server_s* S, Slot& sl, int status)
 {
     pb::NvtxRange nv("pb_server.finish");
     size_t off = 0;
-    // work items beyond the slot's item array: every request of the execution lost pairs
+    // work items beyond the slot's item array: every request of the execution lost pairs;
+    // a cell-count scan that gave up: the cell lists of the execution are not valid
     if (status == PB_OK && (pb::plan_exec_status(sl.plan) & pb::kCapItems)) status = PB_ERR_UNSUPPORTED;
+    if (status == PB_OK && (pb::plan_exec_status(sl.plan) & pb::kScanStall)) status = PB_ERR_CUDA;
     const int* bad = status == PB_OK ? pb::plan_bad_flags(sl.plan) : nullptr;
     for (size_t k = 0; k < sl.reqs.size(); k++) {
         Req* r = sl.reqs[k];

@@ -102,15 +102,18 @@ void launch_prepare_fp64(const double* pos, const double* frc, const int* perm, 
 // Work items of the real-space kernel: each cell row (c0, c1) of an instance
 // is walked along z and cut into row items of 32 consecutive targets (cells
 // may be split between items, so warps stay full), fewer where the row ends
-// or where 32 targets would span more than 8 cells.  Each row item becomes
+// or where 32 targets would span more than the instance's zspan cells (sparse targets,
+// such as a target set half the size of the sources, fill a warp only over
+// many cells: a longer item costs more candidates per item but fewer per
+// target, and every lane then holds one).  Each row item becomes
 // `G` = csplit work items, one per group of stencil columns, so that small
 // instances still fill the GPU.  One thread per row start: a counting walk,
 // then the emitting walk into its range.  A row gives at most
 // targets/32 + cells items.
 // Item = {instance, first target, local row, count | za << 8 | zb << 16 | group << 24}.
 template <bool EMIT>
-__device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q, int rowl, int G, int4* items,
-                         int k0, int cap, int& nitems)
+__device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q, int rowl, int G, int zspan,
+                         int4* items, int k0, int cap, int& nitems)
 {
     int k = 0, z = 0;
     int t = start[row0];
@@ -118,7 +121,7 @@ __device__ void walk_row(const int* __restrict__ start, int row0, int nz, int q,
     while (t < end) {
         while (start[row0 + z + 1] <= t) z++;  // za: the cell of target t
         const int za = z;
-        const int lim = min(min(t + 32, end), start[row0 + min(za + 8, nz)]);
+        const int lim = min(min(t + 32, end), start[row0 + min(za + zspan, nz)]);
         while (start[row0 + z + 1] <= lim - 1) z++;  // zb: the cell of target lim - 1
         for (int g = 0; g < G; g++, k++)
             if (EMIT && k0 + k < cap)
@@ -165,13 +168,13 @@ __global__ void __launch_bounds__(kItemWarps * 32)
             for (int z = lane; z <= nz; z += 32) st[w][z] = start[rc + z];
             __syncwarp();
             if (lane == 0) {
-                const int G = max(1, I.csplit);
+                const int G = max(1, I.csplit), zspan = min(max(I.zspan, 1), kItemCells);
                 int n = 0;
-                walk_row<false>(st[w], 0, nz, rq, rl / nz, G, nullptr, 0, 0, n);
+                walk_row<false>(st[w], 0, nz, rq, rl / nz, G, zspan, nullptr, 0, 0, n);
                 if (n > 0) {
                     const int k0 = atomicAdd(nitems, n);
                     if (k0 + n > cap) atomicOr(status, kCapItems);  // items dropped: reported, not silent
-                    walk_row<true>(st[w], 0, nz, rq, rl / nz, G, items, k0, cap, n);
+                    walk_row<true>(st[w], 0, nz, rq, rl / nz, G, zspan, items, k0, cap, n);
                 }
             }
         }
@@ -216,6 +219,27 @@ __device__ __forceinline__ const double* cl_target(const CellListArgs& A, int q,
     return yo >= 0 ? A.y + 3 * (size_t)(yo + local) : A.x + 3 * (size_t)(A.src_off[q] + local);
 }
 
+// wrap_coord_r without its FP64 arithmetic for a coordinate already inside
+// [0, L) by more than a few ulps (the usual case; compared as bit patterns,
+// which order non-negative doubles): there wrap_coord_r returns v itself.
+__device__ __forceinline__ double wrap_in_box(double v, double L, double iL)
+{
+    const long long vb = __double_as_longlong(v), lb = __double_as_longlong(L);
+    if (vb >= 0 && vb < lb - 8) return v;
+    return wrap_coord_r(v, L, iL);
+}
+
+// FP32 sort key of a particle within its cell: z wrapped in FP32.
+__device__ __forceinline__ float cl_zkey(const PbInst& I, double z64)
+{
+    const float Lz = (float)I.L[2], iLz = (float)I.iL[2];
+    float z = (float)z64;
+    z -= Lz * floorf(z * iLz);
+    return (z == z) ? z : 0.f;
+}
+
+// Per particle: its cell, its arrival slot in the cell, its instance and its
+// z key (key = {cell, slot, instance, z bits}).
 __global__ void k_bin_cells(CellListArgs A)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -230,13 +254,13 @@ __global__ void k_bin_cells(CellListArgs A)
     int c[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const double w = wrap_coord_r(finite_or_flag(pos[a], A.bad, q), I.L[a], I.iL[a]);
+        const double w = wrap_in_box(finite_or_flag(pos[a], A.bad, q), I.L[a], I.iL[a]);
         const int ci = (int)(w * I.ih[a]);
         c[a] = ci >= I.nc[a] ? I.nc[a] - 1 : ci;
     }
     const int g = I.cell_off + (c[0] * I.nc[1] + c[1]) * I.nc[2] + c[2];
     const int slot = atomicAdd(&A.zero[(tgt ? A.cstride : 0) + g], 1);
-    (tgt ? A.key_t : A.key_s)[i] = make_int2(g, slot);
+    (tgt ? A.key_t : A.key_s)[i] = make_int4(g, slot, q, __float_as_int(cl_zkey(I, pos[2])));
 }
 
 // Exclusive scan of the counts [0, n_act] of each set (the entry at n_act is
@@ -301,6 +325,7 @@ __global__ void __launch_bounds__(kCellScanThreads) k_scan_cells(CellListArgs A,
         if (i0 + k < n) out[i0 + k] = r[k];
 }
 
+// Each cell's entries {particle, z bits} in arrival order.
 __global__ void k_scatter_cells(CellListArgs A)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -308,9 +333,9 @@ __global__ void k_scatter_cells(CellListArgs A)
     const bool tgt = p >= A.ncap_s;
     const int i = tgt ? p - A.ncap_s : p;
     if (i >= (tgt ? A.tgt_off : A.src_off)[A.ninst]) return;
-    const int2 k = (tgt ? A.key_t : A.key_s)[i];
+    const int4 k = (tgt ? A.key_t : A.key_s)[i];
     const int* start = A.start + (tgt ? A.cstride : 0);
-    (tgt ? A.perm_tmp_t : A.perm_tmp_s)[start[k.x] + k.y] = i;
+    (tgt ? A.perm_tmp_t : A.perm_tmp_s)[start[k.x] + k.y] = make_int2(i, k.w);
 }
 
 // The sorted record of particle v of instance q at position `slot` of its list.
@@ -320,7 +345,7 @@ __device__ __forceinline__ void cl_record(const CellListArgs& A, bool tgt, int q
     const PbInst& I = A.inst[q];
     double w[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++) w[a] = wrap_coord_r(finite_or_flag(pos[a], A.bad, q), I.L[a], I.iL[a]);
+    for (int a = 0; a < 3; a++) w[a] = wrap_in_box(finite_or_flag(pos[a], A.bad, q), I.L[a], I.iL[a]);
     const double* fr = tgt ? nullptr : A.f + 3 * (size_t)v;
     if constexpr (MIXED) {
         float hi[3], lo[3];
@@ -342,83 +367,40 @@ __device__ __forceinline__ void cl_record(const CellListArgs& A, bool tgt, int q
     }
 }
 
-// Sort of every cell by (z wrapped in FP32, index), eight lanes per cell,
-// fused with the writing of the sorted records: entry v goes to slot
-// start + #{u in cell : (z_u, u) < (z_v, v)}.  Consecutive targets then lie
-// close in z (narrower real-space work items) and the order, hence every
-// summation order downstream, does not depend on the scatter's atomics.
-// Cells of more than kSortMax entries keep the scatter order.
+// Sort of every cell by (z wrapped in FP32, index), a thread per particle,
+// fused with the writing of the sorted records: particle v goes to slot
+// start + #{u in cell : (z_u, u) < (z_v, v)}, counted over the cell's entries
+// (contiguous, so the threads of a cell read the same few lines).  Consecutive
+// targets then lie close in z (narrower real-space work items) and the order,
+// hence every summation order downstream, does not depend on the scatter's
+// atomics.  Cells of more than kSortMax entries keep the scatter order.
 template <bool MIXED>
-__global__ void k_sort_prepare(CellListArgs A, int nsets)
+__global__ void k_sort_prepare(CellListArgs A)
 {
-    const int ncell = A.cell_off[A.ninst];
-    const int lane = threadIdx.x & 31, l8 = lane & 7;
-    const unsigned gmask = 0xffu << (lane & ~7);
-    const int ngroups = (gridDim.x * blockDim.x) >> 3;
-    const int cstride = A.cstride;
-    for (int cg = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; cg < nsets * ncell; cg += ngroups) {
-        const bool tgt = cg >= ncell;
-        const int cell = tgt ? cg - ncell : cg;
-        const int* start = A.start + (tgt ? cstride : 0);
-        const int b = start[cell], n = start[cell + 1] - b;
-        if (n == 0) continue;
-        const int q = find_instance(A.cell_off, A.ninst, cell);
-        const int* ptmp = tgt ? A.perm_tmp_t : A.perm_tmp_s;
-        int* perm = tgt ? A.perm_t : A.perm_s;
-        // the instance's particle range: after a scan that gave up (kScanStall) slots may be stale
-        const int* off = tgt ? A.tgt_off : A.src_off;
-        const int vlo = off[q], vhi = off[q + 1];
-        auto valid = [&](int v) {
-            if (v >= vlo && v < vhi) return true;
-            atomicOr(&A.bad[A.ninst], kScanStall);
-            return false;
-        };
-        auto position = [&](int v) { return tgt ? cl_target(A, q, v) : A.x + 3 * (size_t)v; };
-        if (n > kSortMax) {
-            for (int i = l8; i < n; i += 8) {
-                const int v = ptmp[b + i];
-                if (!valid(v)) continue;
-                perm[b + i] = v;
-                cl_record<MIXED>(A, tgt, q, v, position(v), b + i);
-            }
-            continue;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= A.ncap_s + A.ncap_t) return;
+    const bool tgt = p >= A.ncap_s;
+    const int v = tgt ? p - A.ncap_s : p;
+    if (v >= (tgt ? A.tgt_off : A.src_off)[A.ninst]) return;
+    const int4 k = (tgt ? A.key_t : A.key_s)[v];
+    const int q = k.z;
+    const double* pos = tgt ? cl_target(A, q, v) : A.x + 3 * (size_t)v;
+    const int* start = A.start + (tgt ? A.cstride : 0);
+    const int b = start[k.x], n = start[k.x + 1] - b;
+    int rank = k.y;
+    if (n <= kSortMax) {
+        const int2* ent = (tgt ? A.perm_tmp_t : A.perm_tmp_s) + b;
+        const float z = __int_as_float(k.w);
+        rank = 0;
+        for (int j = 0; j < n; j++) {
+            const int2 u = ent[j];
+            const float zu = __int_as_float(u.y);
+            rank += (zu < z) || (zu == z && u.x < v);
         }
-        // FP32 key (the order only shapes the work items; FP64 would cost the GPU's slow FP64 pipe)
-        const PbInst& I = A.inst[q];
-        const float Lz = (float)I.L[2], iLz = (float)I.iL[2];
-        auto zkey = [&](const double* pv) {
-            float z = (float)pv[2];
-            z -= Lz * floorf(z * iLz);
-            return (z == z) ? z : 0.f;
-        };
-        for (int ib = 0; ib < n; ib += 8) {
-            const int i = ib + l8;
-            const int v = i < n ? ptmp[b + i] : vlo;
-            const bool ok = i < n && valid(v);
-            const double* pv = ok ? position(v) : nullptr;
-            const float z = ok ? zkey(pv) : 0.f;
-            int rank = 0;
-            for (int jb = 0; jb < n; jb += 8) {
-                int u = v;
-                float zu = z;
-                if (jb != ib) {
-                    const int j = jb + l8;
-                    u = j < n ? ptmp[b + j] : vlo;
-                    zu = (j < n && u >= vlo && u < vhi) ? zkey(position(u)) : 0.f;
-                }
-                const int m = min(8, n - jb);
-                for (int k = 0; k < m; k++) {
-                    const int uk = __shfl_sync(gmask, u, k, 8);
-                    const float zk = __shfl_sync(gmask, zu, k, 8);
-                    rank += (zk < z) || (zk == z && uk < v);
-                }
-            }
-            if (ok) {
-                perm[b + rank] = v;
-                cl_record<MIXED>(A, tgt, q, v, pv, b + rank);
-            }
-        }
+        rank = min(rank, max(n - 1, 0));  // (stale entries after a scan that gave up: stay in the cell)
     }
+    (tgt ? A.perm_t : A.perm_s)[b + rank] = v;
+    cl_record<MIXED>(A, tgt, q, v, pos, b + rank);
 }
 
 void launch_cell_lists(const CellListArgs& args, bool mixed, int nsm, cudaStream_t s)
@@ -434,12 +416,8 @@ void launch_cell_lists(const CellListArgs& args, bool mixed, int nsm, cudaStream
     if (np > 0) k_bin_cells<<<pblocks, 256, 0, s>>>(a);
     k_scan_cells<<<(unsigned)(nsets * a.ntiles), kCellScanThreads, 0, s>>>(a, nsets);  // empty sets get zero starts
     if (np > 0) k_scatter_cells<<<pblocks, 256, 0, s>>>(a);
-    long long blocks = ((long long)nsets * a.ncell_cap * 8 + 255) / 256;
-    if (blocks > (long long)nsm * 16) blocks = (long long)nsm * 16;
-    if (mixed)
-        k_sort_prepare<true><<<(unsigned)blocks, 256, 0, s>>>(a, nsets);
-    else
-        k_sort_prepare<false><<<(unsigned)blocks, 256, 0, s>>>(a, nsets);
+    if (np > 0 && mixed) k_sort_prepare<true><<<pblocks, 256, 0, s>>>(a);
+    if (np > 0 && !mixed) k_sort_prepare<false><<<pblocks, 256, 0, s>>>(a);
 }
 
 }  // namespace pb

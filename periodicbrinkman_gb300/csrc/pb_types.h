@@ -26,6 +26,7 @@ constexpr int kMaxPoly = 28;    // max terms of the far polynomial (held in regi
 constexpr int kMaxCheb = 40;    // max terms of the near and blob Chebyshev series (shared memory)
 constexpr int kNumSeries = 16;  // terms of the FP64 small-r series
 constexpr int kMaxCheb64 = 48;  // max terms of the FP64 far Chebyshev series (FP64 path)
+constexpr int kItemCells = 32;  // bound of the cells along z of a real-space work item (PbInst::zspan)
 constexpr int kCapItems = 1;    // execution status bit: real-space work items beyond the item array
 constexpr int kScanStall = 2;   // execution status bit: a cell-count scan gave up waiting for a predecessor
 
@@ -92,7 +93,7 @@ struct PbInst {
     int same;                 // targets are the sources
     int bucket;               // FFT size bucket
     int csplit;               // real-space work items per row item (stencil columns split into groups)
-    int pad;
+    int zspan;                // max cells along z of a real-space work item (<= kItemCells)
 };
 
 }  // namespace pb
