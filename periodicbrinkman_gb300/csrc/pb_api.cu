@@ -349,6 +349,8 @@ struct pb_plan_s {
     cudaEvent_t ev_upload = nullptr;
 
     cudaStream_t stream = nullptr;
+    cudaStream_t stream_k = nullptr;  // the k-space branch of an execution (forked after the cell lists)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     cudaGraphExec_t gexec = nullptr;
     cudaGraphExec_t gexec_f = nullptr;  // forces-only executions (positions of the last full one)
@@ -701,6 +703,9 @@ void plan_free(pb_plan_s* P)
     if (P->ev_out) cudaEventDestroy(P->ev_out);
     for (auto& e : P->tev)
         if (e) cudaEventDestroy(e);
+    if (P->ev_fork) cudaEventDestroy(P->ev_fork);
+    if (P->ev_join) cudaEventDestroy(P->ev_join);
+    if (P->stream_k) cudaStreamDestroy(P->stream_k);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
 }
@@ -718,6 +723,9 @@ int plan_alloc(pb_plan_s* P)
     }
     plan_layout(P, true);
     PB_CK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+    PB_CK(cudaStreamCreateWithFlags(&P->stream_k, cudaStreamNonBlocking));
+    PB_CK(cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming));
+    PB_CK(cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming));
     P->staging_bytes = (sizeof(PbInst) + sizeof(PbTables)) * (size_t)P->count + 4 * sizeof(int) * (P->count + 1);
     PB_CK(cudaMallocHost(&P->staging, P->staging_bytes));
     PB_CK(cudaMallocHost(&P->h_bad, sizeof(int) * (P->count + 1)));
@@ -819,59 +827,77 @@ void run_compute(pb_plan_s* P, cudaStream_t s, bool forces_only)
         launch_build_items(P->start_t, P->ncell, P->d_cell_off, P->d_inst, P->count, P->items, P->item_cap,
                            P->counter + 1, P->d_bad + P->count, P->nsm, s);
     record(P, 1, s);
-    nvtxRangePushA("pb.real_space");
-    if (P->any_real) {
+    auto real_part = [&](cudaStream_t rs) {
+        NvtxRange nv("pb.real_space");
+        if (!P->any_real) return;
         const int* nitems = P->counter + 1;
         if (mixed)
             launch_real_mixed(P->npoly, P->d_inst, P->d_tab, P->items, nitems, P->item_cap,
                               (const float4*)P->spos_a, (const float4*)P->spos_b, (const float4*)P->sfrc, P->start_s,
                               (const float4*)P->tpos_a, (const float4*)P->tpos_b, P->n_tgt, P->u_real, P->counter,
-                              P->nsm, s);
+                              P->nsm, rs);
         else
             launch_real_fp64(P->d_inst, P->d_tab, P->items, nitems, P->item_cap, (const Dbl4*)P->spos_a,
                              (const Dbl4*)P->sfrc, P->start_s, (const Dbl4*)P->tpos_a, P->n_tgt, P->u_real,
-                             P->counter, P->nsm, s);
-    }
-    nvtxRangePop();
-    record(P, 2, s);
-    nvtxRangePushA("pb.kspace");
-    if (P->any_k) {
+                             P->counter, P->nsm, rs);
+    };
+    auto kspace_part = [&](cudaStream_t ks) {
+        NvtxRange nv("pb.kspace");
+        if (!P->any_k) {
+            record(P, 3, ks);
+            record(P, 4, ks);
+            return;
+        }
         if (mixed && !spread_atomic()) {
             for (auto& B : P->buckets)
                 launch_spread_tiles(P->d_inst, B.d_inst, (int)B.inst.size(), B.M, P->start_s, (const float4*)P->spos_a,
-                                    (const float4*)P->spos_b, (const float4*)P->sfrc, (float*)P->grid, s);
+                                    (const float4*)P->spos_b, (const float4*)P->sfrc, (float*)P->grid, ks);
         } else if (mixed) {
-            launch_zero_grids(P->d_inst, P->count, P->grid, 4, s);
+            launch_zero_grids(P->d_inst, P->count, P->grid, 4, ks);
             launch_spread<float>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
-                                 (float*)P->grid, s);
+                                 (float*)P->grid, ks);
         } else {
-            launch_zero_grids(P->d_inst, P->count, P->grid, 8, s);
+            launch_zero_grids(P->d_inst, P->count, P->grid, 8, ks);
             launch_spread<double>(P->d_inst, P->count, P->d_src_off, P->n_src, P->spos_a, P->spos_b, P->sfrc,
-                                  (double*)P->grid, s);
+                                  (double*)P->grid, ks);
         }
-        record(P, 3, s);
+        record(P, 3, ks);
         for (auto& B : P->buckets) {
             const PbInst& I0 = P->hinst[B.inst[0]];
             if (mixed)
                 launch_kspace_fft<float>(P->d_inst, B.d_inst, (int)B.inst.size(), I0.spec_off, B.M,
-                                         (float*)P->grid + I0.grid_off, (float2*)P->spec + I0.spec_off, B.d_tw, s);
+                                         (float*)P->grid + I0.grid_off, (float2*)P->spec + I0.spec_off, B.d_tw, ks);
             else
                 launch_kspace_fft<double>(P->d_inst, B.d_inst, (int)B.inst.size(), I0.spec_off, B.M,
                                           (double*)P->grid + I0.grid_off, (double2*)P->spec + I0.spec_off, B.d_tw,
-                                          s);
+                                          ks);
         }
-        record(P, 4, s);
+        record(P, 4, ks);
         if (mixed)
             launch_gather<float>(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->tpos_a, P->tpos_b,
-                                 (const float*)P->grid, (float*)P->u_k, s);
+                                 (const float*)P->grid, (float*)P->u_k, ks);
         else
             launch_gather<double>(P->d_inst, P->count, P->d_tgt_off, P->n_tgt, P->tpos_a, P->tpos_b,
-                                  (const double*)P->grid, (double*)P->u_k, s);
+                                  (const double*)P->grid, (double*)P->u_k, ks);
+    };
+    // The real-space sum and the k-space chain share only the sorted records:
+    // the k-space chain runs on a branch forked here and joined before the
+    // combine (in the captured graph, two independent branches), so the FFT
+    // passes' low occupancy and each kernel's tail are filled by the other
+    // branch (N = 1e5 solve 0.866 -> 0.826 ms; the serving stream's large
+    // requests 6% faster).  Stage timing keeps the serial order.
+    if (P->timing || !P->any_real || !P->any_k) {
+        real_part(s);
+        record(P, 2, s);
+        kspace_part(s);
     } else {
-        record(P, 3, s);
-        record(P, 4, s);
+        cudaEventRecord(P->ev_fork, s);
+        cudaStreamWaitEvent(P->stream_k, P->ev_fork, 0);
+        kspace_part(P->stream_k);
+        real_part(s);
+        cudaEventRecord(P->ev_join, P->stream_k);
+        cudaStreamWaitEvent(s, P->ev_join, 0);
     }
-    nvtxRangePop();
     record(P, 5, s);
     if (P->any_zero) launch_force_sums(P->d_inst, P->f, P->d_src_off, P->count, P->fsum, s);
     if (mixed)
