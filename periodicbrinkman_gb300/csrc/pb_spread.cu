@@ -2,16 +2,16 @@
 // Gaussian spreading of cuda/fftBrinkman.h:120-155 onto float4 grids
 // (three components interleaved), organised by grid tile instead of by point.
 //
-// A block owns a tile of 16 x 16 x 16 grid points of one instance (8 along
-// an axis whose grid has 8 points).  Each of its 256 threads owns one (x, y)
-// column of the tile and keeps the column's 16 z values of the three
+// A block owns a tile of 16 x 16 x 8 grid points of one instance (fewer along
+// an axis whose grid is smaller).  Each of its 256 threads owns one (x, y)
+// column of the tile and keeps the column's 8 z values of the three
 // components in registers.  The block enumerates the real-space cells whose
 // points' windows can reach the tile (the cell list is already sorted), and
 // streams those points through shared memory 256 at a time: each thread
 // loads one candidate, the block keeps the points whose window meets the
-// tile, and for each kept point the loading thread lays its Gaussian weights
-// out along the tile's three axes (zero outside the window, periodic wrap
-// included).  Every column then adds f w_x w_y w_z over its 16 z values with
+// tile, and the threads lay the kept points' Gaussian weights out along the
+// tile's three axes, one (point, axis) row each (zero outside the window,
+// periodic wrap included).  Every column then adds f w_x w_y w_z over its 8 z values with
 // packed FP32x2 FMAs; warps whose 8 x 4 column patch the window misses skip
 // the point.  At the end each column is stored once: no atomics, no grid
 // clear, and a fixed summation order (the result does not depend on the
