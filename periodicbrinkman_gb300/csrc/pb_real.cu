@@ -102,8 +102,20 @@ __device__ __forceinline__ void fill_frame_tabs(const PbInst& I, const ItemFrame
             g = F.za + k - I.S[2];
         }
         const int n = I.nc[ax];
-        int w = ((g % n) + n) % n;
-        int sc = (g - w) / n;  // image shift count
+        int w, sc;  // wrapped cell and image shift count (one wrap at most, unless the box has few cells)
+        if (g >= 0 && g < n) {
+            w = g;
+            sc = 0;
+        } else if (g < 0 && g >= -n) {
+            w = g + n;
+            sc = -1;
+        } else if (g >= n && g < 2 * n) {
+            w = g - n;
+            sc = 1;
+        } else {
+            w = ((g % n) + n) % n;
+            sc = (g - w) / n;
+        }
         float hi, lo;  // Q = O - sc L, O = the frame cell's corner
         frame_offset(I, ax, ax == 0 ? F.c0 : ax == 1 ? F.c1 : F.za, sc, hi, lo);
         if (ax == 0) {
@@ -282,7 +294,8 @@ __device__ __forceinline__ void rare_pair(RealWarpSmem& S, const PbTables& T, fl
 
 // Evaluate the `n` (<= 32) deferred near pairs [end - n, end), one per lane,
 // into the per-target accumulators: each lane writes its pair's contribution
-// over the entry, then lane t sums the entries of target t (no atomics).
+// over the entry, then lane t sums the entries of target t (no atomics; shared
+// float atomics measured slower here).
 __device__ __forceinline__ void near_flush(RealWarpSmem& S, const PbTables& T, int end, int n, int lane)
 {
     const int e0 = end - n;
