@@ -556,7 +556,7 @@ int fill_instance(pb_plan_s* P, int q, const pb_solve_params& p, const Resolved&
                   int cell_off, int max_terms)
 {
     set_inst_fields(P->hinst[q], p, R, src_off, tgt_off, cell_off);
-    int trc = build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, &P->htab[q], max_terms, p.precision == PB_PREC_FP64);
+    int trc = build_tables(p.alpha, R.d, p.eps, R.rc, kTableTol, &P->htab[q], max_terms, p.precision == PB_PREC_FP64);
     if (trc) return fail(PB_ERR_INVALID, "table construction failed");
     return PB_OK;
 }
@@ -1210,7 +1210,7 @@ int prepare_instance(const pb_solve_params& p, int npoly_cap, PbTables* tab, pb_
     Resolved R;
     int rc = resolve(p, R);
     if (rc) return rc;
-    if (build_tables(p.alpha, R.d, p.eps, R.rc, 1e-9, tab, npoly_cap, p.precision == PB_PREC_FP64))
+    if (build_tables(p.alpha, R.d, p.eps, R.rc, kTableTol, tab, npoly_cap, p.precision == PB_PREC_FP64))
         return fail(PB_ERR_INVALID, "table construction failed");
     fill_info(R, tab->nd, info);
     return PB_OK;
@@ -1269,7 +1269,7 @@ int pb_resolve(const pb_solve_params* p, pb_instance_info* info)
     int rc = resolve(*p, R);
     if (rc) return rc;
     PbTables T;
-    if (build_tables(p->alpha, R.d, p->eps, R.rc, 1e-9, &T)) return fail(PB_ERR_INVALID, "table construction failed");
+    if (build_tables(p->alpha, R.d, p->eps, R.rc, kTableTol, &T)) return fail(PB_ERR_INVALID, "table construction failed");
     info->d = R.d;
     info->rc = R.rc;
     info->eta = R.eta;
@@ -1560,7 +1560,7 @@ int pb_debug_pair_kernel64(double alpha, double d, double eps, double rc, int n,
                            double* H2)
 {
     PbTables T;
-    if (build_tables(alpha, d, eps, rc, 1e-9, &T, 0, true)) return fail(PB_ERR_INVALID, "bad kernel parameters");
+    if (build_tables(alpha, d, eps, rc, kTableTol, &T, 0, true)) return fail(PB_ERR_INVALID, "bad kernel parameters");
     for (int i = 0; i < n; i++) {
         const double ri = r[i], r2 = ri * ri;
         if (r2 < T.rtiny2 || r2 == 0.0) {  // the FP64 small-r series (eps > 0) or the r -> 0 limit
@@ -1654,7 +1654,7 @@ int pb_debug_pair_kernel(double alpha, double d, double eps, double rc, int n, c
                          double* H2)
 {
     PbTables T;
-    if (build_tables(alpha, d, eps, rc, 1e-9, &T)) return fail(PB_ERR_INVALID, "bad kernel parameters");
+    if (build_tables(alpha, d, eps, rc, kTableTol, &T)) return fail(PB_ERR_INVALID, "bad kernel parameters");
     for (int i = 0; i < n; i++) {
         float rf = (float)r[i];
         float r2 = rf * rf;

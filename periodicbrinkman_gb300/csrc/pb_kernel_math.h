@@ -49,8 +49,18 @@ std::vector<double> fit_chebyshev(const std::function<double(double)>& f, double
 void fit_chebyshev_pair(const std::function<void(double, double*, double*)>& f, double lo, double hi, int nodes,
                         double rel_tol, int max_terms, std::vector<double>& c1, std::vector<double>& c2);
 
+// Relative truncation of the FP32 tables' Chebyshev series.  The tables are
+// evaluated in FP32 from an FP32 argument, whose rounding alone gives 1-5e-7
+// of max |T| near the steep end of the far piece; truncating at 2e-8
+// instead of 1e-9 leaves that error unchanged and drops two to three terms
+// of the far polynomial (20 -> 17 for most instances).
+#ifndef PB_TABLE_TOL
+#define PB_TABLE_TOL 2e-8
+#endif
+constexpr double kTableTol = PB_TABLE_TOL;
+
 // Fill the per-instance real-space tables.  poly_tol: relative truncation of
-// the Chebyshev series (1e-9 keeps ~20 terms); max_terms caps the screened
+// the Chebyshev series (kTableTol; 1e-9 keeps ~20 terms); max_terms caps the screened
 // polynomial (<= 0: kMaxPoly); fp64_far: also fit the FP64 far series of
 // the FP64 path (nf = 0 otherwise).  Returns 0 or an error code.
 int build_tables(double a, double d, double eps, double rc, double poly_tol, PbTables* t, int max_terms = 0,

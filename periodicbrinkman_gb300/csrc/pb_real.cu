@@ -336,6 +336,20 @@ __device__ __forceinline__ void chunk_sums(RealWarpSmem& S, int lane)
     }
 }
 
+// Segment of candidate pos + lane, without a search: the segment holding
+// `pos` plus the segment starts in (pos, pos + lane] (at most 64 segments,
+// two per lane).  `pos` is the same for the whole warp.
+__device__ __forceinline__ int candidate_segment(const RealWarpSmem& S, int nseg, int pos, int lane)
+{
+    const int ka = lane, kb = lane + 32;
+    const int pa = ka < nseg ? S.sg_pre[ka] : 0x7fffffff, pb = kb < nseg ? S.sg_pre[kb] : 0x7fffffff;
+    const int k0 = __popc(__ballot_sync(kFull, pa <= pos)) + __popc(__ballot_sync(kFull, pb <= pos)) - 1;
+    const unsigned bits = (pa > pos && pa - pos < 32 ? 1u << (pa - pos) : 0u) |
+                          (pb > pos && pb - pos < 32 ? 1u << (pb - pos) : 0u);
+    const unsigned starts = __reduce_or_sync(kFull, bits);
+    return k0 + __popc(starts & ((2u << lane) - 2u));
+}
+
 // Stream the gathered candidate segments through the warp 32 sources at a
 // time: stage, classify against the item's targets, queue the pairs inside
 // the cutoff target-major and evaluate them (far polynomial; pairs below
@@ -368,18 +382,7 @@ __device__ __forceinline__ void stream_segments(RealWarpSmem& S, const PbInst& I
         int fill = 0;
         while (fill < 32 && pos < total) {
             const int p = pos + lane;
-            // segment of candidate p without a search: the segment holding `pos`
-            // plus the segment starts in (pos, p] (at most 64 segments, two per lane)
-            int seg;
-            {
-                const int ka = lane, kb = lane + 32;
-                const int pa = ka < nseg ? S.sg_pre[ka] : 0x7fffffff, pb = kb < nseg ? S.sg_pre[kb] : 0x7fffffff;
-                const int k0 = __popc(__ballot_sync(kFull, pa <= pos)) + __popc(__ballot_sync(kFull, pb <= pos)) - 1;
-                const unsigned bits = (pa > pos && pa - pos < 32 ? 1u << (pa - pos) : 0u) |
-                                      (pb > pos && pb - pos < 32 ? 1u << (pb - pos) : 0u);
-                const unsigned starts = __reduce_or_sync(kFull, bits);
-                seg = k0 + __popc(starts & ((2u << lane) - 2u));
-            }
+            const int seg = candidate_segment(S, nseg, pos, lane);
             bool keep = false, zs = false;
             int j = 0;
             float p3[3] = {0.f, 0.f, 0.f}, l3[3] = {0.f, 0.f, 0.f};
