@@ -81,7 +81,7 @@ typedef struct pb_slot_config {
     int max_tgt;       /* total targets (an instance whose targets are its sources counts n_src) */
     int max_cells;     /* total real-space cells over the bound instances */
     int precision;     /* PB_PREC_FP64 or PB_PREC_MIXED */
-    int npoly;         /* terms of the FP32 far-piece polynomial (16..28; 0 = 20) */
+    int npoly;         /* terms of the FP32 far-piece polynomial (16..28; 0 = 18; longer fits are truncated) */
 } pb_slot_config;
 
 typedef struct pb_plan_s* pb_plan;

@@ -179,7 +179,7 @@ class Plan:
 
 
 def make_slot(M: int, max_instances: int, max_src: int, max_tgt: int, max_cells: int = 1 << 20,
-              precision: str | int = "mixed", npoly: int = 20) -> "Plan":
+              precision: str | int = "mixed", npoly: int = 18) -> "Plan":
     """A capacity plan (serving slot) for instances on an M^3 grid."""
     c = SlotConfig()
     for a in range(3):
@@ -197,7 +197,7 @@ def make_slot(M: int, max_instances: int, max_src: int, max_tgt: int, max_cells:
 
 
 def slot_estimate_bytes(M: int, max_instances: int, max_src: int, max_tgt: int, max_cells: int,
-                        precision: str | int = "mixed", npoly: int = 20) -> int:
+                        precision: str | int = "mixed", npoly: int = 18) -> int:
     """Device bytes of a capacity plan (pb_slot_estimate_bytes), host only."""
     c = SlotConfig()
     for a in range(3):

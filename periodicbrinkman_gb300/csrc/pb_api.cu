@@ -931,7 +931,7 @@ int build_slot_host(const pb_slot_config* cfg, pb_plan_s* P)
     P->n_tgt = std::max(cfg->max_tgt, 1);
     P->n_y = P->n_tgt;
     P->ncell = cfg->max_cells;
-    P->npoly = P->npoly_cap = std::max(16, std::min(kMaxPoly, cfg->npoly > 0 ? cfg->npoly : 20));
+    P->npoly = P->npoly_cap = std::max(16, std::min(kMaxPoly, cfg->npoly > 0 ? cfg->npoly : 18));
     P->res.resize(B);
     P->hinst.resize(B);
     P->htab.resize(B);

@@ -94,7 +94,7 @@ struct pb_server_s {
     std::atomic<long long> next_id{1}, submitted{0}, completed{0}, failed{0}, rejected{0}, batches{0}, kernels{0},
         batched_instances{0};
     int device = 0;
-    int npoly = 20;  // far-polynomial terms of every slot
+    int npoly = 18;  // far-polynomial terms of every slot (longer fits are truncated to it)
     std::atomic<long long> busy_ns{0};
 };
 
