@@ -472,7 +472,15 @@ __device__ __forceinline__ void stream_segments(RealWarpSmem& S, const PbInst& I
         {
             const unsigned short tag = (unsigned short)(lane << 5);
             int pn = ex & 0xffff, pr = 1023 - (ex >> 16);
-            for (unsigned m = mi; m; m &= m - 1) S.q[pn++] = tag | (__ffs(m) - 1);
+            {  // lowest and highest set bits per step: half the dependent iterations of one bit per step
+                int pe = pn + __popc(mi) - 1;
+                for (unsigned m = mi; m;) {
+                    const int lo = __ffs(m) - 1, hi = 31 - __clz(m);
+                    S.q[pn++] = tag | lo;
+                    if (hi != lo) S.q[pe--] = tag | hi;
+                    m &= ~((1u << lo) | (1u << hi));
+                }
+            }
             for (unsigned m = mr; m; m &= m - 1) S.q[pr--] = tag | (__ffs(m) - 1);
         }
         __syncwarp();
