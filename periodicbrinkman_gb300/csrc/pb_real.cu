@@ -516,8 +516,10 @@ __device__ __forceinline__ void stream_segments(RealWarpSmem& S, const PbInst& I
             const int eb = min(lane * KB, nn), ee = min(eb + KB, nn);
             int cur = -1, first = -1;
             float a0 = 0, a1 = 0, a2 = 0, f0 = 0, f1 = 0, f2 = 0;
+            int qn = eb < ee ? S.q[eb] : 0;  // the next entry, loaded one pair ahead
             for (int ei = eb; ei < ee; ei++) {
-                const int qv = S.q[ei], t = qv >> 5, jj = qv & 31;
+                const int qv = qn, t = qv >> 5, jj = qv & 31;
+                if (ei + 1 < ee) qn = S.q[ei + 1];
                 const float4 p = S.s_hi[jj], pl = S.s_lo[jj], f = S.s_f[jj];
                 const float4 a = S.t_hi[t], al = S.t_lo[t];
                 const float dx = (a.x - p.x) + (al.x - pl.x);
