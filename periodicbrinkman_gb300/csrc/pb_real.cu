@@ -65,9 +65,10 @@ __device__ __forceinline__ void item_frame(const PbInst& I, int4 it, ItemFrame& 
 // hi/lo pair, so the inner loops need no FP64.
 struct __align__(8) FrameTabs {
     float2 qx[2 * kMaxReach + 1], qy[2 * kMaxReach + 1], qz[kZTab];
-    int wx[2 * kMaxReach + 1], wy[2 * kMaxReach + 1], wz[kZTab];
-    int zx[2 * kMaxReach + 1], zy[2 * kMaxReach + 1], zz[kZTab];
+    short wx[2 * kMaxReach + 1], wy[2 * kMaxReach + 1], wz[kZTab];  // wrapped cells (< 128)
+    unsigned zx, zy, zz[2];  // bit k: the image shift of offset k is zero
 };
+static_assert(2 * kMaxReach + 1 <= 32 && kZTab <= 64, "zero-shift bitmasks");
 
 // c h - s L as an FP32 hi/lo pair (double-float arithmetic: the products are
 // split exactly by FMAs), for a cell index c and an image shift count s.
@@ -86,6 +87,8 @@ __device__ __forceinline__ void frame_offset(const PbInst& I, int ax, int c, int
 __device__ __forceinline__ void fill_frame_tabs(const PbInst& I, const ItemFrame& F, FrameTabs& T, int lane)
 {
     const int nx = 2 * I.S[0] + 1, ny = 2 * I.S[1] + 1, nz = F.zb - F.za + 2 * I.S[2] + 1;
+    if (lane < 4) (&T.zx)[lane] = 0u;
+    __syncwarp();
     for (int i = lane; i < nx + ny + nz; i += 32) {
         int ax, g, k;
         if (i < nx) {
@@ -120,16 +123,16 @@ __device__ __forceinline__ void fill_frame_tabs(const PbInst& I, const ItemFrame
         frame_offset(I, ax, ax == 0 ? F.c0 : ax == 1 ? F.c1 : F.za, sc, hi, lo);
         if (ax == 0) {
             T.qx[k] = make_float2(hi, lo);
-            T.wx[k] = w;
-            T.zx[k] = sc == 0;
+            T.wx[k] = (short)w;
+            if (sc == 0) atomicOr(&T.zx, 1u << k);
         } else if (ax == 1) {
             T.qy[k] = make_float2(hi, lo);
-            T.wy[k] = w;
-            T.zy[k] = sc == 0;
+            T.wy[k] = (short)w;
+            if (sc == 0) atomicOr(&T.zy, 1u << k);
         } else {
             T.qz[k] = make_float2(hi, lo);
-            T.wz[k] = w;
-            T.zz[k] = sc == 0;
+            T.wz[k] = (short)w;
+            if (sc == 0) atomicOr(&T.zz[k >> 5], 1u << (k & 31));
         }
     }
 }
@@ -170,7 +173,7 @@ __device__ __forceinline__ float horner_g(const float* __restrict__ c, int n, fl
 
 // Per-warp shared memory of the mixed-precision kernel.
 constexpr int kSeg = 64;   // candidate segments gathered before they are streamed
-constexpr int kNear = 64;  // deferred near pairs (evaluated 32 at a time; <= 31 wait)
+constexpr int kNear = 40;  // deferred near pairs (evaluated 32 at a time; <= 31 wait)
 
 struct __align__(16) RealWarpSmem {
     float4 s_hi[32], s_lo[32], s_f[32];     // staged sources: frame-relative hi, lo; force
@@ -179,7 +182,6 @@ struct __align__(16) RealWarpSmem {
     float c_x[32], c_y[32], c_z[32];        // staged sources, hi parts by axis (classification)
     float acc[3][32];                       // per-target partial sums of the current chunk
     float ks[6][32];                        // per-target Kahan sums (3) and compensations (3) of the item
-    double acc64[3][32];                    // per-target FP64 sums of series pairs
     unsigned selfm[32];                     // per target: the staged candidate that is its own source
     int sg_b[kSeg], sg_n[kSeg], sg_pre[kSeg], sg_meta[kSeg];  // segments: first source, count, prefix, frame
     float box[6];                           // the item's targets: frame-relative bounding box (hi parts)
@@ -243,9 +245,10 @@ struct MixedConsts {
 
 // A pair below r_mid: the blob piece (R_eps - R_d itself) inside the blob
 // region, else the near piece of S - R_d; below r_tiny (or at r = 0) the FP64
-// series, summed into the target's FP64 accumulator (then v = 0).
+// series, added to the target's FP64 sum u_t[3 t..] in global memory (then
+// v = 0).
 __device__ __forceinline__ void rare_pair(RealWarpSmem& S, const PbTables& T, float4 h, float4 l, float4 f, int t,
-                                          float& v0, float& v1, float& v2)
+                                          float& v0, float& v1, float& v2, double* __restrict__ u_t)
 {
     const auto& K = S.rk;
     const float dx = h.x + l.x, dy = h.y + l.y, dz = h.z + l.z;
@@ -268,9 +271,9 @@ __device__ __forceinline__ void rare_pair(RealWarpSmem& S, const PbTables& T, fl
             H2 = (double)(T12.y * (ri * ri * ri));
         }
         const double fd = f.x * ddx + f.y * ddy + f.z * ddz;
-        atomicAdd(&S.acc64[0][t], H1 * f.x + H2 * fd * ddx);
-        atomicAdd(&S.acc64[1][t], H1 * f.y + H2 * fd * ddy);
-        atomicAdd(&S.acc64[2][t], H1 * f.z + H2 * fd * ddz);
+        atomicAdd(u_t + 3 * t, H1 * f.x + H2 * fd * ddx);
+        atomicAdd(u_t + 3 * t + 1, H1 * f.y + H2 * fd * ddy);
+        atomicAdd(u_t + 3 * t + 2, H1 * f.z + H2 * fd * ddz);
         return;
     }
     float ri = rsqrtf(r2);
@@ -296,7 +299,8 @@ __device__ __forceinline__ void rare_pair(RealWarpSmem& S, const PbTables& T, fl
 // into the per-target accumulators: each lane writes its pair's contribution
 // over the entry, then lane t sums the entries of target t (no atomics; shared
 // float atomics measured slower here).
-__device__ __forceinline__ void near_flush(RealWarpSmem& S, const PbTables& T, int end, int n, int lane)
+__device__ __forceinline__ void near_flush(RealWarpSmem& S, const PbTables& T, int end, int n, int lane,
+                                           double* __restrict__ u_t)
 {
     const int e0 = end - n;
     if (lane < n) {
@@ -304,7 +308,7 @@ __device__ __forceinline__ void near_flush(RealWarpSmem& S, const PbTables& T, i
         const float4 h = S.nq_h[e];
         const int t = __float_as_int(h.w);
         float v0, v1, v2;
-        rare_pair(S, T, h, S.nq_l[e], S.nq_f[e], t, v0, v1, v2);
+        rare_pair(S, T, h, S.nq_l[e], S.nq_f[e], t, v0, v1, v2, u_t);
         S.nq_h[e] = make_float4(v0, v1, v2, h.w);
     }
     __syncwarp();
@@ -358,7 +362,8 @@ template <int NP>
 __device__ __forceinline__ void stream_segments(RealWarpSmem& S, const PbInst& I, const PbTables& T,
                                                 const MixedConsts& K, const float2 (&c12)[NP], const ItemFrame& F,
                                                 int nseg, int lane, const float4* __restrict__ spos_hi,
-                                                const float4* __restrict__ spos_lo, const float4* __restrict__ sfrc)
+                                                const float4* __restrict__ spos_lo, const float4* __restrict__ sfrc,
+                                                double* __restrict__ u_real)
 {
     // exclusive prefix of the segment counts (two segments per lane)
     int total;
@@ -410,7 +415,7 @@ __device__ __forceinline__ void stream_segments(RealWarpSmem& S, const PbInst& I
                     d2 = fmaf(da, da, d2);
                 }
                 keep = d2 < keep2;
-                zs = I.same && S.ft.zx[i0] && S.ft.zy[i1] && S.ft.zz[i2];
+                zs = I.same && ((S.ft.zx >> i0) & (S.ft.zy >> i1) & (S.ft.zz[i2 >> 5] >> (i2 & 31)) & 1u);
             }
             const unsigned bal = __ballot_sync(kFull, keep);
             const int need = 32 - fill, k = __popc(bal), rank = __popc(bal & lt);
@@ -500,7 +505,7 @@ __device__ __forceinline__ void stream_segments(RealWarpSmem& S, const PbInst& I
             __syncwarp();
             int n = nq + k;
             while (n >= 32) {
-                near_flush(S, T, n, 32, lane);
+                near_flush(S, T, n, 32, lane, u_real + 3 * (size_t)F.first);
                 n -= 32;
             }
             if (lane == 0) S.nq_n = n;
@@ -580,6 +585,9 @@ __device__ __forceinline__ void stream_segments(RealWarpSmem& S, const PbInst& I
     }
 }
 
+// Four blocks of four warps per SM (128 registers; 44.7 KB of shared memory a
+// block, which leaves about 45 KB of L1).  Five blocks (96 registers, with
+// spills) measured 8% slower.
 template <int NP>
 __global__ void __launch_bounds__(kRealWarps * 32, 4)
     k_real_mixed(const PbInst* __restrict__ inst, const PbTables* __restrict__ tab, const int4* __restrict__ items,
@@ -599,7 +607,6 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         S.acc[c][lane] = 0.f;
-        S.acc64[c][lane] = 0.0;
     }
     S.selfm[lane] = 0u;
     if (lane == 0) S.nq_n = 0;
@@ -736,14 +743,14 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
             }
             if (nseg == 0) break;
             __syncwarp();
-            stream_segments<NP>(S, I, T, K, c12, F, nseg, lane, spos_hi, spos_lo, sfrc);
+            stream_segments<NP>(S, I, T, K, c12, F, nseg, lane, spos_hi, spos_lo, sfrc, u_real);
             nseg = 0;
         }
         // the rest of the near queue, then the item's sums
         {
             const int nq = S.nq_n;
             __syncwarp();
-            if (nq > 0) near_flush(S, T, nq, nq, lane);
+            if (nq > 0) near_flush(S, T, nq, nq, lane, u_real + 3 * (size_t)F.first);
             if (lane == 0) S.nq_n = 0;
         }
         __syncwarp();
@@ -752,11 +759,8 @@ __global__ void __launch_bounds__(kRealWarps * 32, 4)
             size_t o = 3 * (size_t)tidx;
 #pragma unroll
             for (int c = 0; c < 3; c++)
-                atomicAdd(u_real + o + c, ((double)S.ks[c][lane] - (double)S.ks[3 + c][lane]) + S.acc64[c][lane]);
+                atomicAdd(u_real + o + c, (double)S.ks[c][lane] - (double)S.ks[3 + c][lane]);
         }
-        S.acc64[0][lane] = 0.0;
-        S.acc64[1][lane] = 0.0;
-        S.acc64[2][lane] = 0.0;
         __syncwarp();
     }
 }
