@@ -244,8 +244,8 @@ int pb_plan_destroy(pb_plan plan);
 typedef struct pb_server_config {
     long long budget_bytes; /* device memory for all slots, resident and dynamic (0: 150 GiB) */
     int precision;          /* PB_PREC_MIXED or PB_PREC_FP64 */
-    int max_batch;          /* instances per slot execution (0: 16) */
-    int slots_per_grid;     /* resident slots per grid size, created with the server (0: 2) */
+    int max_batch;          /* instances per slot execution (0: 4) */
+    int slots_per_grid;     /* resident slots per grid size, created with the server (0: 4) */
     int n_grids;            /* grid sizes provisioned (0: 8, 16, ..., 256) */
     int grids[8];
     int max_src;            /* source capacity of a resident slot (0: 262144) */

@@ -225,8 +225,8 @@ def bind(plan: "Plan", params) -> None:
 class Server:
     """Continuous-batching server (pb_server_*): submit host requests, wait."""
 
-    def __init__(self, precision: str | int = "mixed", budget_bytes: int = 150 << 30, max_batch: int = 16,
-                 slots_per_grid: int = 2, grids=(8, 16, 32, 64, 128, 256), max_src: int = 1 << 18,
+    def __init__(self, precision: str | int = "mixed", budget_bytes: int = 150 << 30, max_batch: int = 4,
+                 slots_per_grid: int = 4, grids=(8, 16, 32, 64, 128, 256), max_src: int = 1 << 18,
                  max_tgt: int = 0, queue_capacity: int = 0, linger_us: int = 0, max_dynamic_per_grid: int = 0,
                  dynamic_idle_ms: int = 0):
         c = ServerConfig()

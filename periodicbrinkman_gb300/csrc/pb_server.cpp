@@ -454,8 +454,8 @@ int pb_server_create(const pb_server_config* cfg_in, pb_server* out)
     if (pb_device_count() <= 0) return PB_ERR_CUDA;
     pb_server_config cfg = cfg_in ? *cfg_in : pb_server_config{};
     if (cfg.budget_bytes <= 0) cfg.budget_bytes = 150LL << 30;
-    if (cfg.max_batch <= 0) cfg.max_batch = 16;
-    if (cfg.slots_per_grid <= 0) cfg.slots_per_grid = 2;
+    if (cfg.max_batch <= 0) cfg.max_batch = 4;
+    if (cfg.slots_per_grid <= 0) cfg.slots_per_grid = 4;
     if (cfg.max_src <= 0) cfg.max_src = 1 << 18;
     if (cfg.max_tgt <= 0) cfg.max_tgt = cfg.max_src;
     if (cfg.n_grids <= 0) {
