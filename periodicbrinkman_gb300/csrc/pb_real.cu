@@ -19,8 +19,8 @@
 // in the frame of the target cell (error-free TwoSum), so displacements carry
 // FP32 relative accuracy even at r << cell size; the pair kernel is the FP32
 // polynomial T(r) of the instance tables (FMA only); per-chunk partial sums are
-// Kahan-accumulated; pairs below r_tiny use the FP64 series and an FP64
-// accumulator.  The self pair of targets that are the sources is skipped here
+// Kahan-accumulated; pairs below r_tiny use the FP64 series, added straight to
+// the target's FP64 sum.  The self pair of targets that are the sources is skipped here
 // and added in FP64 by the combine kernel (R_eps(0) - R_d(0)) f_i.
 //
 // FP64 (k_real_fp64): beyond r_mid an FP64 Chebyshev series of the screened
