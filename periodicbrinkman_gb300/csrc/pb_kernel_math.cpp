@@ -354,6 +354,22 @@ int build_tables(double a, double d, double eps, double rc, double poly_tol, PbT
     {
         std::vector<double> c1, c2;
         fit_chebyshev_pair(Td, r_far, rc, 40, poly_tol, max_terms, c1, c2);
+        // Terms past the 18th that are below 1e-7 of the largest coefficient
+        // are dropped as well (the FP32 evaluation's own error is 1-5e-7 of
+        // max |T|), so that a batch where a few instances would need 19 or 20
+        // terms still runs the 18-term kernel.
+        if ((int)c1.size() > kPreferredTerms) {
+            double cmax = 0, tail = 0;
+            for (size_t k = 0; k < c1.size(); k++) {
+                const double m = std::max(std::fabs(c1[k]), std::fabs(c2[k]));
+                cmax = std::max(cmax, m);
+                if ((int)k >= kPreferredTerms) tail = std::max(tail, m);
+            }
+            if (tail <= 1e-7 * cmax) {
+                c1.resize(kPreferredTerms);
+                c2.resize(kPreferredTerms);
+            }
+        }
         std::vector<double> p1 = cheb_to_monomial(c1), p2 = cheb_to_monomial(c2);
         t->nd = (int)p1.size();
         for (int k = 0; k < t->nd; k++) {

@@ -54,10 +54,10 @@ void fit_chebyshev_pair(const std::function<void(double, double*, double*)>& f, 
 // of max |T| near the steep end of the far piece; truncating at 2e-8
 // instead of 1e-9 leaves that error unchanged and drops two to three terms
 // of the far polynomial (20 -> 17 for most instances).
-#ifndef PB_TABLE_TOL
-#define PB_TABLE_TOL 2e-8
-#endif
-constexpr double kTableTol = PB_TABLE_TOL;
+constexpr double kTableTol = 2e-8;
+// Far-polynomial length of the serving slots' kernel; longer fits whose extra
+// terms are negligible are cut to it (build_tables).
+constexpr int kPreferredTerms = 18;
 
 // Fill the per-instance real-space tables.  poly_tol: relative truncation of
 // the Chebyshev series (kTableTol; 1e-9 keeps ~20 terms); max_terms caps the screened
