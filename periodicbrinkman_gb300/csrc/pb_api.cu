@@ -1269,7 +1269,8 @@ int pb_resolve(const pb_solve_params* p, pb_instance_info* info)
     int rc = resolve(*p, R);
     if (rc) return rc;
     PbTables T;
-    if (build_tables(p->alpha, R.d, p->eps, R.rc, kTableTol, &T)) return fail(PB_ERR_INVALID, "table construction failed");
+    if (build_tables(p->alpha, R.d, p->eps, R.rc, kTableTol, &T, 0, p->precision == PB_PREC_FP64))
+        return fail(PB_ERR_INVALID, "table construction failed");
     info->d = R.d;
     info->rc = R.rc;
     info->eta = R.eta;
