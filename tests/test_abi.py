@@ -90,8 +90,11 @@ def test_fp64_kernel_tables_match_oracle():
 
 
 def test_kernel_tables_match_oracle():
-    # FP32 polynomial tables evaluated as on the GPU vs the FP64 oracle kernel
-    for a, d, e, rc in [(10, 0.125, 0.01, 0.35), (20, 0.02, 0.005, 0.08), (1, 0.05, 0.005, 0.2), (3, 0.1, 0.0, 0.4)]:
+    # FP32 polynomial tables evaluated as on the GPU vs the FP64 oracle kernel; the
+    # last three put alpha delta at 0.001 (closed-form series moments at their
+    # smallest), at 5 and 4 (moments by quadrature above alpha delta = 3)
+    for a, d, e, rc in [(10, 0.125, 0.01, 0.35), (20, 0.02, 0.005, 0.08), (1, 0.05, 0.005, 0.2), (3, 0.1, 0.0, 0.4),
+                        (1, 0.02, 0.001, 0.08), (50, 0.1, 0.02, 0.35), (45, 0.09, 0.0, 0.3)]:
         r = np.linspace(0, rc, 801)[1:-1]
         if e > 0:
             r = np.concatenate([r, e * np.array([0.0, 0.1, 0.5, 0.79, 0.81, 1.0, 2.0, 5.5])])
