@@ -429,8 +429,18 @@ void worker_loop(pb_server_s* S)
         }
         if (did) S->busy_ns += std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count();
         if (!did) {
-            std::unique_lock<std::mutex> lk(S->mu);
-            S->cv.wait_for(lk, std::chrono::microseconds(50), [&] { return !S->inbox.empty() || S->stop.load(); });
+            // While a slot runs, keep polling its completion event (a timed sleep
+            // here is rounded up by the OS timer slack, and every request that
+            // finishes meanwhile waits out the rest of it); with nothing on the
+            // GPU, sleep until a submission arrives.
+            bool any_busy = false;
+            for (auto& sl : S->slots) any_busy = any_busy || sl->busy;
+            if (any_busy) {
+                std::this_thread::yield();
+            } else {
+                std::unique_lock<std::mutex> lk(S->mu);
+                S->cv.wait_for(lk, std::chrono::microseconds(50), [&] { return !S->inbox.empty() || S->stop.load(); });
+            }
         }
     }
 }
