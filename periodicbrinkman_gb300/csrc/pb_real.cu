@@ -87,7 +87,12 @@ __device__ __forceinline__ void frame_offset(const PbInst& I, int ax, int c, int
 __device__ __forceinline__ void fill_frame_tabs(const PbInst& I, const ItemFrame& F, FrameTabs& T, int lane)
 {
     const int nx = 2 * I.S[0] + 1, ny = 2 * I.S[1] + 1, nz = F.zb - F.za + 2 * I.S[2] + 1;
-    if (lane < 4) (&T.zx)[lane] = 0u;
+    if (lane == 0) {
+        T.zx = 0u;
+        T.zy = 0u;
+        T.zz[0] = 0u;
+        T.zz[1] = 0u;
+    }
     __syncwarp();
     for (int i = lane; i < nx + ny + nz; i += 32) {
         int ax, g, k;
